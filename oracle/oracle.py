@@ -1,0 +1,281 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``oracle/libkpt_oracle.so`` (our FP32 restatement of the reference hot
+path, built by ``oracle/build_oracle.sh``) or, with ``prefix="ref"``,
+``oracle/_ref/libkpt_ref_host.so`` (the reference's own code compiled for the
+host by ``oracle/build_ref.sh``; only where the reference tree exists).  Both
+export the same C ABI, so every helper below drives either one.
+
+Only tests, the smoke check and the benchmark's CPU-baseline leg use this
+module; the product path (``kittlespt_gb300``) never imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libkpt_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libkpt_ref_host.so")
+
+_f = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_i64 = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_u64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_v = C.c_void_p
+
+_libs = {}
+
+
+def build(ref: bool = False) -> None:
+    script = "build_ref.sh" if ref else "build_oracle.sh"
+    subprocess.run(["sh", os.path.join(HERE, script)], check=True,
+                   stdout=subprocess.DEVNULL)
+
+
+def available(prefix: str = "orc") -> bool:
+    return os.path.exists(REF_SO if prefix == "ref" else ORACLE_SO)
+
+
+def lib(prefix: str = "orc"):
+    if prefix in _libs:
+        return _libs[prefix]
+    path = REF_SO if prefix == "ref" else ORACLE_SO
+    if not os.path.exists(path):
+        if prefix == "ref":
+            raise FileNotFoundError(path)
+        build(False)
+    L = C.CDLL(path)
+    g = lambda n: getattr(L, f"{prefix}_{n}")
+    g("scene_create").restype = _v
+    g("scene_create").argtypes = [C.c_int, _f, _f, _f, _i, C.c_int, _i, _i, _f, C.c_int, _v,
+                                  C.c_int, _v, C.c_longlong, _v]
+    g("scene_destroy").argtypes = [_v]
+    g("scene_counts").argtypes = [_v, _i64]
+    g("scene_bvh").argtypes = [_v, _i, _u, _f, _i, _i64, _f, _f]
+    g("scene_tlas").argtypes = [_v, _u, _i, _f]
+    g("trace").argtypes = [_v, C.c_int, _f, _f, C.c_float, C.c_float, _i, _i, _f, _v, C.c_int, _v, C.c_int]
+    g("trace_bounces").argtypes = [_v, C.c_int, _f, _f, C.c_int, _i, _f, _v, C.c_int]
+    g("render_samples").argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, _v, _v, _v, _v, _v, C.c_int]
+    g("sky").argtypes = [_v, C.c_int, _f, _f]
+    g("bsdf_eval").argtypes = [C.c_int, _f, _f, _f, _f]
+    g("lum_bins").argtypes = [C.c_int, _f, C.c_float, C.c_float, _i]
+    g("modulate").argtypes = [C.c_int, C.c_int, _f, C.c_int, _f, _f]
+    g("bloom").argtypes = [C.c_int, C.c_int, _f, C.c_int, C.c_float, _f]
+    g("post_image").argtypes = [C.c_int, C.c_int, _f, _v, C.c_int, C.c_float, C.c_float, C.c_float,
+                                C.c_float, _f]
+    g("metering_weights").argtypes = [C.c_int, C.c_int, _f]
+    if prefix == "orc":
+        g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _u64]
+        g("exposure").argtypes = [_u64, _v, C.c_float, C.c_float, _f]
+        g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
+    else:
+        g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _f]
+        g("exposure").argtypes = [_f] + [C.c_float] * 12 + [_f]
+    _libs[prefix] = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Scene:
+    """A scene in the reference's layout (one mesh per instance)."""
+
+    def __init__(self, scene, prefix: str = "orc"):
+        self.prefix = prefix
+        self.L = lib(prefix)
+        ex = scene.expanded()
+        self.ex = ex
+        self._keep = ex
+        self.materials = np.ascontiguousarray(scene.materials)
+        fn = getattr(self.L, f"{prefix}_scene_create")
+        n = int(ex["positions"].shape[0])
+        self.h = fn(n, ex["positions"].reshape(-1), ex["normals"].reshape(-1), ex["uvs"].reshape(-1),
+                    ex["material"], len(ex["mesh_offset"]), ex["mesh_offset"], ex["mesh_count"],
+                    np.ascontiguousarray(np.transpose(ex["models"], (0, 2, 1))).reshape(-1),
+                    len(self.materials), _ptr(self.materials), 0, None, 0, None)
+        self.scene = scene
+
+    def close(self):
+        if self.h:
+            getattr(self.L, f"{self.prefix}_scene_destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _fn(self, n):
+        return getattr(self.L, f"{self.prefix}_{n}")
+
+    def counts(self):
+        out = np.zeros(5, np.int64)
+        self._fn("scene_counts")(self.h, out)
+        return dict(nodes=int(out[0]), tri_index=int(out[1]), tlas_nodes=int(out[2]),
+                    lights=int(out[3]), meshes=int(out[4]))
+
+    def bvh(self):
+        c = self.counts()
+        nn, nt, nb = c["nodes"], c["tri_index"], c["meshes"]
+        lf = np.zeros(nn, np.int32); cnt = np.zeros(nn, np.uint32); bd = np.zeros(nn * 6, np.float32)
+        ti = np.zeros(nt, np.int32); br = np.zeros(nb, np.int64); bb = np.zeros(nb * 6, np.float32)
+        bi = np.zeros(nb * 16, np.float32)
+        self._fn("scene_bvh")(self.h, lf, cnt, bd, ti, br, bb, bi)
+        nt_ = c["tlas_nodes"]
+        lr = np.zeros(nt_, np.uint32); tb = np.zeros(nt_, np.int32); tbd = np.zeros(nt_ * 6, np.float32)
+        self._fn("scene_tlas")(self.h, lr, tb, tbd)
+        return dict(left_first=lf, count=cnt, bounds=bd.reshape(-1, 6), tri_index=ti, blas_root=br,
+                    blas_bounds=bb.reshape(-1, 6), blas_inv=bi.reshape(-1, 16),
+                    tlas_lr=lr, tlas_blas=tb, tlas_bounds=tbd.reshape(-1, 6))
+
+    def trace(self, o, d, tmin=0.0, tmax=np.inf, brute=False, nthreads=None):
+        n = int(o.shape[0])
+        o = np.ascontiguousarray(o, np.float32).reshape(-1)
+        d = np.ascontiguousarray(d, np.float32).reshape(-1)
+        prim = np.zeros(n, np.int32); inst = np.zeros(n, np.int32); t = np.zeros(n, np.float32)
+        bary = np.zeros(n * 3, np.float32); cnt = np.zeros(8, np.int64)
+        self._fn("trace")(self.h, n, o, d, tmin, tmax, prim, inst, t, _ptr(bary), int(brute), _ptr(cnt),
+                          nthreads or os.cpu_count())
+        return dict(prim=prim, inst=inst, t=t, bary=bary.reshape(-1, 3), counters=cnt)
+
+    def trace_bounces(self, o, d, nbounces, nthreads=None):
+        n = int(o.shape[0])
+        prim = np.zeros((nbounces + 1) * n, np.int32); t = np.zeros((nbounces + 1) * n, np.float32)
+        cnt = np.zeros(8, np.int64)
+        self._fn("trace_bounces")(self.h, n, np.ascontiguousarray(o, np.float32).reshape(-1),
+                                  np.ascontiguousarray(d, np.float32).reshape(-1), nbounces, prim, t,
+                                  _ptr(cnt), nthreads or os.cpu_count())
+        return dict(prim=prim.reshape(nbounces + 1, n), t=t.reshape(nbounces + 1, n), counters=cnt)
+
+    def render_samples(self, sample0=0, nsamples=1, rng_order=0, width=None, height=None,
+                       row0=0, nrows=0, max_depth=None, nthreads=None, want_radiance=True):
+        sc = self.scene
+        W = width or sc.width
+        H = height or sc.height
+        rows = nrows if nrows > 0 else H - row0
+        st = sc.settings.copy()
+        if max_depth is not None:
+            st["max_depth"] = max_depth
+        rad = np.zeros((nsamples, rows, W, 3), np.float32) if want_radiance else None
+        alb = np.zeros((rows, W, 3), np.float32)
+        fh = np.zeros((rows, W, 2), np.int32)
+        ft = np.zeros((rows, W), np.float32)
+        cnt = np.zeros(8, np.int64)
+        ip = np.ascontiguousarray(sc.camera.inv_proj.T, np.float32).reshape(-1)
+        iv = np.ascontiguousarray(sc.camera.inv_view.T, np.float32).reshape(-1)
+        env = np.ascontiguousarray(sc.env)
+        self._fn("render_samples")(self.h, ip, iv, _ptr(env), _ptr(st), W, H, sample0, nsamples, rng_order,
+                                   row0, nrows, _ptr(rad) if rad is not None else None, _ptr(alb), _ptr(fh),
+                                   _ptr(ft), _ptr(cnt), nthreads or os.cpu_count())
+        return dict(radiance=rad, albedo=alb, first_hit=fh, first_t=ft, counters=cnt)
+
+
+def sky(env, dirs, prefix="orc"):
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros_like(dirs)
+    e = np.ascontiguousarray(env)
+    getattr(lib(prefix), f"{prefix}_sky")(_ptr(e), int(dirs.shape[0]), dirs.reshape(-1), out.reshape(-1))
+    return out
+
+
+def bsdf_eval(params, dirs, u, prefix="orc"):
+    n = int(params.shape[0])
+    out = np.zeros((n, 12), np.float32)
+    getattr(lib(prefix), f"{prefix}_bsdf_eval")(n, np.ascontiguousarray(params, np.float32).reshape(-1),
+                                                np.ascontiguousarray(dirs, np.float32).reshape(-1),
+                                                np.ascontiguousarray(u, np.float32).reshape(-1), out.reshape(-1))
+    return out
+
+
+def lum_bins(Y, black_ev=-10.0, white_ev=6.5, prefix="orc"):
+    Y = np.ascontiguousarray(Y, np.float32)
+    out = np.zeros(Y.shape[0], np.int32)
+    getattr(lib(prefix), f"{prefix}_lum_bins")(int(Y.shape[0]), Y, black_ev, white_ev, out)
+    return out
+
+
+def hist_thresholds(black_ev=-10.0, white_ev=6.5):
+    thr = np.zeros(255, np.float32)
+    lib("orc").orc_hist_thresholds(black_ev, white_ev, thr)
+    return thr
+
+
+def modulate(acc_sum, nsamples, albedo, prefix="orc"):
+    H, W = acc_sum.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    getattr(lib(prefix), f"{prefix}_modulate")(W, H, np.ascontiguousarray(acc_sum, np.float32).reshape(-1),
+                                               nsamples, np.ascontiguousarray(albedo, np.float32).reshape(-1),
+                                               out.reshape(-1))
+    return out
+
+
+def bloom(render, karis=False, internal_blend=0.65, prefix="orc"):
+    H, W = render.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    getattr(lib(prefix), f"{prefix}_bloom")(W, H, np.ascontiguousarray(render, np.float32).reshape(-1),
+                                            int(karis), internal_blend, out.reshape(-1))
+    return out
+
+
+def post_image(render, bloom_img, final_blend, expo, white_ev=6.5, black_ev=-10.0, prefix="orc"):
+    H, W = render.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    b = np.ascontiguousarray(bloom_img, np.float32) if bloom_img is not None else None
+    getattr(lib(prefix), f"{prefix}_post_image")(W, H, np.ascontiguousarray(render, np.float32).reshape(-1),
+                                                 _ptr(b) if b is not None else None, int(b is not None),
+                                                 final_blend, expo, white_ev, black_ev, out.reshape(-1))
+    return out
+
+
+def metering_weights(W, H, prefix="orc"):
+    out = np.zeros((H, W), np.float32)
+    getattr(lib(prefix), f"{prefix}_metering_weights")(W, H, out.reshape(-1))
+    return out
+
+
+def histogram(render, black_ev=-10.0, white_ev=6.5, prefix="orc"):
+    """orc: fixed-point (2^24) uint64 bins; ref: float bins."""
+    H, W = render.shape[:2]
+    r = np.ascontiguousarray(render, np.float32).reshape(-1)
+    if prefix == "orc":
+        out = np.zeros(256, np.uint64)
+        lib("orc").orc_histogram(W, H, r, black_ev, white_ev, out)
+    else:
+        out = np.zeros(256, np.float32)
+        lib("ref").ref_histogram(W, H, r, black_ev, white_ev, out)
+    return out
+
+
+def exposure(hist, expo, last_lum, delta_ms, prefix="orc"):
+    """[avg bin, avg lum, adapted lum, exposure scalar, iso, shutter]."""
+    out = np.zeros(6, np.float32)
+    if prefix == "orc":
+        e = np.ascontiguousarray(expo)
+        lib("orc").orc_exposure(np.ascontiguousarray(hist, np.uint64), _ptr(e), last_lum, delta_ms, out)
+    else:
+        e = expo
+        lib("ref").ref_exposure(np.ascontiguousarray(hist, np.float32), float(e["aperture"]), float(e["iso"]),
+                                float(e["shutter"]), float(e["ev_comp"]), float(e["white_ev"]),
+                                float(e["black_ev"]), float(e["min_iso"]), float(e["max_iso"]),
+                                float(e["min_shutter"]), float(e["max_shutter"]), last_lum, delta_ms, out)
+    return out
+
+
+def exposure_scalar(expo) -> float:
+    """Film exposure scalar for fixed camera values
+    (AutoExposureProgram::getStandardOutputBasedExposure), in double."""
+    N = float(expo["aperture"])
+    lavg = (10.0 / 0.65) * ((N * N) / (float(expo["iso"]) * float(expo["shutter"])))
+    return float(np.float32(0.18 / lavg))

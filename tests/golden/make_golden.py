@@ -1,0 +1,129 @@
+"""Generates the golden fixtures in this directory from the reference's own
+code compiled for the host (oracle/_ref/libkpt_ref_host.so, built by
+oracle/build_ref.sh from the reference source tree).
+
+The reference ships no tests or golden vectors, so these fixtures are the
+pin for the CPU oracle: tests/test_oracle_golden.py checks that the oracle
+reproduces every array here bit for bit.  The right-to-left RNG argument order
+of this host build (g++) is recorded as rng_order=1.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from kittlespt_gb300 import scenes as S  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def bvh_digest(sc):
+    b = sc.bvh()
+    return digest(b["left_first"], b["count"], b["bounds"], b["tri_index"], b["blas_root"],
+                  b["blas_bounds"], b["blas_inv"], b["tlas_lr"], b["tlas_blas"], b["tlas_bounds"])
+
+
+def small_scene():
+    return S.scene_small(48, 48, 2, 4)
+
+
+def full_scene():
+    return S.scene_full(64, 36, 2, 8, n_variants=2, subdiv=3, grid=3, n_lights=4)
+
+
+def traversal_scene():
+    return S.scene_traversal(20000)
+
+
+def main():
+    if not O.available("ref"):
+        O.build(ref=True)
+    rng = np.random.default_rng(2024)
+    out = {}
+
+    # plain method, small scene
+    r = O.Scene(small_scene(), "ref")
+    rs = r.render_samples(0, 2)
+    o, d = S.random_rays(4096, 5, center=(0, 0, 0), radius=6.0)
+    h = r.trace(o, d)
+    out.update(small_radiance=rs["radiance"], small_albedo=rs["albedo"], small_first_hit=rs["first_hit"],
+               small_first_t=rs["first_t"], small_ray_o=o, small_ray_d=d, small_prim=h["prim"],
+               small_inst=h["inst"], small_t=h["t"], small_bvh=np.array(bvh_digest(r)))
+
+    # plain method, reduced full scene (lights, MIS, three material kinds)
+    r = O.Scene(full_scene(), "ref")
+    rs = r.render_samples(0, 2)
+    out.update(full_radiance=rs["radiance"], full_albedo=rs["albedo"], full_first_hit=rs["first_hit"],
+               full_bvh=np.array(bvh_digest(r)))
+
+    # traversal scene: closest hits and the 4-bounce chain
+    r = O.Scene(traversal_scene(), "ref")
+    o, d = S.random_rays(4096, 4)
+    h = r.trace(o, d)
+    b = r.trace_bounces(o, d, 4)
+    out.update(trav_ray_o=o, trav_ray_d=d, trav_prim=h["prim"], trav_t=h["t"],
+               trav_bounce_prim=b["prim"], trav_bounce_t=b["t"], trav_bvh=np.array(bvh_digest(r)))
+
+    # sky
+    dirs = rng.normal(size=(512, 3)).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    env = S.environment(sun_theta=np.radians(30.0))
+    out.update(sky_dirs=dirs, sky_rgb=O.sky(env, dirs, "ref"))
+
+    # BSDF lobes
+    n = 4096
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    p = np.zeros((n, 12), np.float32)
+    p[:, 0:3] = nrm
+    p[:, 3:6] = rng.uniform(0.05, 0.95, (n, 3))
+    kind = rng.integers(0, 3, n)
+    p[:, 6] = kind == 2
+    p[:, 7] = rng.uniform(0.0, 1.0, n)
+    p[:, 8] = kind == 1
+    p[:, 9] = rng.choice([1.45, 1.5], n)
+    p[:, 10] = rng.integers(0, 2, n)
+    p[:, 11] = rng.integers(0, 2, n)
+    dd = rng.normal(size=(n, 6))
+    dd[:, :3] /= np.linalg.norm(dd[:, :3], axis=1, keepdims=True)
+    dd[:, 3:] /= np.linalg.norm(dd[:, 3:], axis=1, keepdims=True)
+    dd = dd.astype(np.float32)
+    u = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+    out.update(bsdf_params=p, bsdf_dirs=dd, bsdf_u=u, bsdf_out=O.bsdf_eval(p, dd, u, "ref"))
+
+    # post chain on the reduced full-scene frame
+    acc = out["full_radiance"][0] + out["full_radiance"][1]
+    render = O.modulate(acc, 2, out["full_albedo"], "ref")
+    bl = O.bloom(render, False, 0.65, "ref")
+    blk = O.bloom(render, True, 0.65, "ref")
+    ex = S.exposure()
+    es = O.exposure_scalar(ex)
+    img = O.post_image(render, bl, 0.175, es, prefix="ref")
+    hist = O.histogram(render, prefix="ref")
+    expo = O.exposure(hist, ex, 0.5, 16.0, "ref")
+    Y = np.exp(rng.uniform(np.log(1e-4), np.log(2e3), 8192)).astype(np.float32)
+    out.update(post_acc=acc, post_render=render, post_bloom=bl, post_bloom_karis=blk, post_expo_scalar=np.float32(es),
+               post_image=img, post_hist_float=hist, post_exposure=expo, lum=Y,
+               lum_bins=O.lum_bins(Y, prefix="ref"), meter_96x54=O.metering_weights(96, 54, "ref"),
+               meter_100x37=O.metering_weights(100, 37, "ref"))
+    np.savez_compressed(os.path.join(OUT, "reference_host.npz"), **out)
+    print("wrote", os.path.join(OUT, "reference_host.npz"))
+
+
+if __name__ == "__main__":
+    main()

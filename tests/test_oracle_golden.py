@@ -1,0 +1,107 @@
+"""The CPU oracle reproduces the reference's own code bit for bit.
+
+The fixtures in tests/golden/reference_host.npz were produced by
+tests/golden/make_golden.py from the reference source compiled for the host
+(oracle/build_ref.sh).  RNG argument order there is right-to-left
+(rng_order=1).
+"""
+
+import numpy as np
+import pytest
+
+from kittlespt_gb300 import scenes as S
+from oracle import oracle as O
+
+from tests.golden.make_golden import bvh_digest, full_scene, small_scene, traversal_scene
+
+
+def bits(a):
+    a = np.ascontiguousarray(a, np.float32)
+    return a.view(np.uint32)
+
+
+def test_small_scene_bvh_matches_reference(golden):
+    assert bvh_digest(O.Scene(small_scene())) == str(golden["small_bvh"])
+
+
+def test_full_scene_bvh_matches_reference(golden):
+    assert bvh_digest(O.Scene(full_scene())) == str(golden["full_bvh"])
+
+
+def test_traversal_scene_bvh_matches_reference(golden):
+    assert bvh_digest(O.Scene(traversal_scene())) == str(golden["trav_bvh"])
+
+
+def test_small_scene_closest_hits(golden):
+    sc = O.Scene(small_scene())
+    h = sc.trace(golden["small_ray_o"], golden["small_ray_d"])
+    np.testing.assert_array_equal(h["prim"], golden["small_prim"])
+    np.testing.assert_array_equal(h["inst"], golden["small_inst"])
+    np.testing.assert_array_equal(bits(h["t"]), bits(golden["small_t"]))
+
+
+def test_brute_force_agrees_with_bvh(golden):
+    sc = O.Scene(small_scene())
+    h = sc.trace(golden["small_ray_o"], golden["small_ray_d"], brute=True)
+    np.testing.assert_array_equal(h["prim"], golden["small_prim"])
+
+
+def test_small_scene_per_sample_radiance(golden):
+    r = O.Scene(small_scene()).render_samples(0, 2, rng_order=1)
+    np.testing.assert_array_equal(bits(r["radiance"]), bits(golden["small_radiance"]))
+    np.testing.assert_array_equal(bits(r["albedo"]), bits(golden["small_albedo"]))
+    np.testing.assert_array_equal(r["first_hit"], golden["small_first_hit"])
+    np.testing.assert_array_equal(bits(r["first_t"]), bits(golden["small_first_t"]))
+
+
+def test_full_scene_per_sample_radiance(golden):
+    r = O.Scene(full_scene()).render_samples(0, 2, rng_order=1)
+    np.testing.assert_array_equal(bits(r["radiance"]), bits(golden["full_radiance"]))
+    np.testing.assert_array_equal(bits(r["albedo"]), bits(golden["full_albedo"]))
+    np.testing.assert_array_equal(r["first_hit"], golden["full_first_hit"])
+
+
+def test_traversal_hits_and_bounces(golden):
+    sc = O.Scene(traversal_scene())
+    h = sc.trace(golden["trav_ray_o"], golden["trav_ray_d"])
+    np.testing.assert_array_equal(h["prim"], golden["trav_prim"])
+    np.testing.assert_array_equal(bits(h["t"]), bits(golden["trav_t"]))
+    b = sc.trace_bounces(golden["trav_ray_o"], golden["trav_ray_d"], 4)
+    np.testing.assert_array_equal(b["prim"], golden["trav_bounce_prim"])
+    np.testing.assert_array_equal(bits(b["t"]), bits(golden["trav_bounce_t"]))
+
+
+def test_sky(golden):
+    env = S.environment(sun_theta=np.radians(30.0))
+    np.testing.assert_array_equal(bits(O.sky(env, golden["sky_dirs"])), bits(golden["sky_rgb"]))
+
+
+def test_bsdf_lobes(golden):
+    out = O.bsdf_eval(golden["bsdf_params"], golden["bsdf_dirs"], golden["bsdf_u"])
+    ref = golden["bsdf_out"]
+    same = (bits(out) == bits(ref)) | (np.isnan(out) & np.isnan(ref))
+    assert same.all()
+
+
+def test_post_chain(golden):
+    render = O.modulate(golden["post_acc"], 2, golden["full_albedo"])
+    np.testing.assert_array_equal(bits(render), bits(golden["post_render"]))
+    np.testing.assert_array_equal(bits(O.bloom(render, False, 0.65)), bits(golden["post_bloom"]))
+    np.testing.assert_array_equal(bits(O.bloom(render, True, 0.65)), bits(golden["post_bloom_karis"]))
+    img = O.post_image(render, golden["post_bloom"], 0.175, float(golden["post_expo_scalar"]))
+    np.testing.assert_array_equal(bits(img), bits(golden["post_image"]))
+
+
+def test_histogram_bins_and_weights(golden):
+    np.testing.assert_array_equal(O.lum_bins(golden["lum"]), golden["lum_bins"])
+    np.testing.assert_array_equal(bits(O.metering_weights(96, 54)), bits(golden["meter_96x54"]))
+    np.testing.assert_array_equal(bits(O.metering_weights(100, 37)), bits(golden["meter_100x37"]))
+
+
+def test_histogram_and_exposure_close_to_float_reference(golden):
+    # the reference sums float weights with atomics (order dependent); the
+    # oracle sums 2^-24 fixed point, so agreement is to float rounding
+    h = O.histogram(golden["post_render"])
+    np.testing.assert_allclose(h.astype(np.float64) / 2 ** 24, golden["post_hist_float"], rtol=1e-5, atol=1e-4)
+    e = O.exposure(h, S.exposure(), 0.5, 16.0)
+    np.testing.assert_allclose(e, golden["post_exposure"], rtol=1e-4)
