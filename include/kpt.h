@@ -1,0 +1,209 @@
+/* kpt.h -- C ABI of the GB300 path tracer (libkpt.so).
+ *
+ * The reference exposes its path-tracing hot path through the C++ class
+ * KittlesPT::Renderer (KittlesPT/src/renderer.hpp:13-58) and the POD scene
+ * types of KittlesPT/src/pod_types.hpp.  This header is the plain-C boundary
+ * a host binding (ctypes, cgo, JNI, N-API) calls; include/kittlespt_gb300/
+ * renderer.hpp puts the reference's C++ method set back on top of it.
+ *
+ * Conventions: every function returns a kpt_status (0 = KPT_OK); on error
+ * kpt_last_error() returns a message for the calling thread.  Matrices are
+ * 16 floats, column-major (the reference's Mat4 / glm layout).  Host arrays
+ * passed in are copied; the library owns all device memory of a context.
+ * Functions whose name ends in _device take device pointers and enqueue work
+ * on the context's stream without synchronising.  A context belongs to one
+ * host thread at a time.
+ */
+#ifndef KPT_H
+#define KPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int kpt_status;
+enum {
+    KPT_OK = 0,
+    KPT_ERR_INVALID = -1,     /* bad argument or index out of range */
+    KPT_ERR_CUDA = -2,        /* a CUDA call failed; see kpt_last_error() */
+    KPT_ERR_STATE = -3,       /* call not valid in the current state (e.g. no scene) */
+    KPT_ERR_NOMEM = -4,       /* device allocation failed */
+    KPT_ERR_TRAVERSAL = -5    /* a ray exceeded the traversal stack (result incomplete) */
+};
+
+typedef struct kpt_context kpt_context;
+
+/* MaterialSceneEntity (pod_types.hpp:60-123) / Material (shaders/material.cuh:91-145). */
+typedef struct kpt_material {
+    float albedo[3];
+    float metallic, roughness, transmission, ior;
+    float emission[3];
+    float emission_scale;      /* nits */
+    float normal_scale;
+    int32_t albedo_tex, orm_tex, transmission_tex, emission_tex, normal_tex;  /* -1: none */
+    int32_t pad;
+} kpt_material;
+
+/* ProceduralEnvironmentSettings (pod_types.hpp:37-44) plus the Nishita
+ * coefficients that the reference hard-codes (shaders/atmosphere.cuh:292-310);
+ * kpt_environment_default() fills the reference values. */
+typedef struct kpt_environment {
+    float sun_angular_diameter, sun_phi, sun_theta, sun_emission_factor;
+    float rayleigh[3];         /* sea-level Rayleigh scattering, 1/m */
+    float mie;                 /* sea-level Mie scattering, 1/m */
+    float mie_absorption;      /* sea-level Mie absorption, 1/m */
+    float rayleigh_height, mie_height;   /* scale heights, m */
+    float pad;
+} kpt_environment;
+
+/* RendererSettings (pod_types.hpp:46-57); the temporal, upscale and effects
+ * switches of the reference are not part of this path. */
+typedef struct kpt_settings {
+    int32_t max_depth;
+    int32_t bloom, karis, auto_exposure;
+    float bloom_final_blend, bloom_internal_blend;
+    float frame_delta_ms;
+    int32_t rng_order;         /* argument order of the reference's paired RNG draws: 0 left-to-right, 1 right-to-left */
+} kpt_settings;
+
+/* ExposureValues (pod_types.hpp:9-33) with the compensation and white/black
+ * points passed to Renderer::setExposure (renderer.cu:312-329). */
+typedef struct kpt_exposure {
+    float aperture, iso, shutter, ev_comp, white_ev, black_ev;
+    float max_iso, min_iso, max_shutter, min_shutter;
+    float pad0, pad1;
+} kpt_exposure;
+
+/* Frame statistics of the last render (algorithmic work counted in-kernel). */
+typedef struct kpt_stats {
+    uint64_t box_tests, tri_tests, inst_xforms, overflows;
+    float avg_luminance, adapted_luminance, exposure_scalar, iso, shutter, avg_bin;
+    int32_t frame_index, pad;
+} kpt_stats;
+
+const char* kpt_last_error(void);
+void kpt_environment_default(kpt_environment* env);
+void kpt_settings_default(kpt_settings* s);
+void kpt_exposure_default(kpt_exposure* e);
+
+/* Renderer::initialize / shutdown (renderer.cu:22-53). */
+kpt_status kpt_create(int device, kpt_context** out);
+kpt_status kpt_destroy(kpt_context* ctx);
+
+/* Renderer::resizeResolution (renderer.cu:55-101): render size; clears the accumulation. */
+kpt_status kpt_resize(kpt_context* ctx, int width, int height);
+
+/* Scene upload, Renderer::loadScene (renderer.cu:356-436).  A mesh is a
+ * triangle list (positions and normals 9 floats per triangle, uvs 6, one
+ * material id per triangle); its BLAS is built on upload.  An instance places
+ * a mesh with a model matrix and an optional material override (-1: the
+ * mesh's ids); the reference has no instancing and copies one mesh per
+ * instance, which gives the same images.  kpt_commit_scene builds the TLAS
+ * and the light list and uploads everything. */
+kpt_status kpt_set_materials(kpt_context* ctx, int n, const kpt_material* materials);
+kpt_status kpt_set_textures(kpt_context* ctx, int n, const int32_t* desc /* n x (w, h, channels, byte offset) */,
+                            size_t nbytes, const uint8_t* pixels);
+kpt_status kpt_upload_mesh(kpt_context* ctx, int ntris, const float* positions, const float* normals,
+                           const float* uvs, const int32_t* material_ids, int* mesh_out);
+kpt_status kpt_add_instance(kpt_context* ctx, int mesh, const float* model, int material_override, int* instance_out);
+kpt_status kpt_commit_scene(kpt_context* ctx);
+kpt_status kpt_clear_scene(kpt_context* ctx);
+
+/* getMaterialsCount / getMeshCount (renderer.cu:280-288); the reference's
+ * meshes are this library's instances. */
+kpt_status kpt_counts(kpt_context* ctx, int* materials, int* meshes, int* instances, int* lights);
+
+/* Renderer::setMaterial / getMaterial (renderer.cu:207-248): KPT_ERR_INVALID
+ * for an index out of range (the reference returns false / asserts). */
+kpt_status kpt_set_material(kpt_context* ctx, int index, const kpt_material* m);
+kpt_status kpt_get_material(kpt_context* ctx, int index, kpt_material* m);
+
+/* Renderer::setMeshTransform / getMeshTransform (renderer.cu:250-278): the
+ * TLAS is rebuilt before the next frame. */
+kpt_status kpt_set_instance_transform(kpt_context* ctx, int index, const float* model);
+kpt_status kpt_get_instance_transform(kpt_context* ctx, int index, float* model);
+
+/* Renderer::setView (renderer.cu:342-354) takes projection and view and
+ * inverts them; kpt_set_camera_inverse takes the inverses directly
+ * (Camera::setView, shaders/camera.cuh:28-36). */
+kpt_status kpt_set_view(kpt_context* ctx, const float* projection, const float* view);
+kpt_status kpt_set_camera_inverse(kpt_context* ctx, const float* inv_projection, const float* inv_view);
+
+/* setProceduralEnvironmentData / setRendererSettings / setExposure and their
+ * getters (renderer.cu:290-334). */
+kpt_status kpt_set_environment(kpt_context* ctx, const kpt_environment* env);
+kpt_status kpt_get_environment(kpt_context* ctx, kpt_environment* env);
+kpt_status kpt_set_settings(kpt_context* ctx, const kpt_settings* s);
+kpt_status kpt_get_settings(kpt_context* ctx, kpt_settings* s);
+kpt_status kpt_set_exposure(kpt_context* ctx, const kpt_exposure* e);
+kpt_status kpt_get_exposure(kpt_context* ctx, kpt_exposure* e);
+
+/* Renderer::resetAccumulation (renderer.cu:336-340). */
+kpt_status kpt_reset_accumulation(kpt_context* ctx);
+
+/* Renderer::executeRendering (renderer.cu:103-195) for `spp` samples per
+ * pixel in one frame: the samples use the reference's frame indices
+ * frame_index .. frame_index+spp-1 and are added to the accumulation in that
+ * order; then the post chain (modulate, histogram + exposure, bloom, AgX)
+ * runs on the device, all captured in one CUDA graph.  Asynchronous. */
+kpt_status kpt_render_frame(kpt_context* ctx, int spp, float delta_ms);
+kpt_status kpt_synchronize(kpt_context* ctx);
+
+/* Headless replacements for getRenderTargetTexture (renderer.cu:197-200):
+ * the display image (AgX, [H][W] RGBA float), the modulated render, the
+ * accumulation sum and the visible-surface albedo.  Synchronous copies to
+ * host memory. */
+kpt_status kpt_read_image(kpt_context* ctx, float* rgba);
+kpt_status kpt_read_render(kpt_context* ctx, float* rgba);
+kpt_status kpt_read_accumulation(kpt_context* ctx, float* rgba);
+kpt_status kpt_read_albedo(kpt_context* ctx, float* rgba);
+kpt_status kpt_read_histogram(kpt_context* ctx, uint64_t* bins256);
+kpt_status kpt_get_stats(kpt_context* ctx, kpt_stats* st);
+
+/* Per-sample radiance of the plain method (the megakernel body,
+ * shaders/kernels.cu:385-413), for parity checks: samples sample0 ..
+ * sample0+n-1 of every pixel, [n][H][W] float4 (rgb, 0) into device memory,
+ * plus (instance, triangle, t bits, 0) of the first hit per pixel.  Does not
+ * touch the accumulation. */
+kpt_status kpt_render_samples_device(kpt_context* ctx, int sample0, int nsamples, float* radiance,
+                                     int32_t* first_hit, float* albedo);
+
+/* Closest hit (TLAS::intersect, shaders/tlas.cu:60-125) and any hit
+ * (TLAS::intersectP, tlas.cu:8-58) for n rays; origins and directions are
+ * 3 floats per ray.  Device pointers. */
+kpt_status kpt_trace_device(kpt_context* ctx, int n, const float* origins, const float* dirs, float tmin,
+                            float tmax, int32_t* instance, int32_t* triangle, float* t, float* uv);
+kpt_status kpt_occluded_device(kpt_context* ctx, int n, const float* origins, const float* dirs, float tmin,
+                               const float* tmax, uint8_t* occluded);
+/* Closest hit plus nbounces diffuse bounces per ray (the traversal
+ * workload); outputs are (nbounces+1) x n. */
+kpt_status kpt_trace_bounces_device(kpt_context* ctx, int n, const float* origins, const float* dirs, int nbounces,
+                                    int32_t* instance, int32_t* triangle, float* t);
+/* Host-memory variant of kpt_trace_bounces_device (copies in and out). */
+kpt_status kpt_trace_bounces(kpt_context* ctx, int n, const float* origins, const float* dirs, int nbounces,
+                             int32_t* instance, int32_t* triangle, float* t);
+
+/* Nishita sky radiance seen from 1 m above the ground for n directions
+ * (NishitaAtmosphereModel::sampleLi, shaders/atmosphere.cuh:132-223). */
+kpt_status kpt_sky_device(kpt_context* ctx, int n, const float* dirs, float* rgb);
+
+/* Device timing of the path kernel inside the frame graph (event-record
+ * nodes around it).  kpt_path_kernel_ms sums the path-kernel time of the
+ * last n frames (n <= 256); it synchronises the stream. */
+kpt_status kpt_enable_timing(kpt_context* ctx, int enable);
+kpt_status kpt_path_kernel_ms(kpt_context* ctx, int nframes, float* total_ms);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time or
+ * order work around the library's launches. */
+kpt_status kpt_get_stream(kpt_context* ctx, void** stream);
+
+/* Kernel-launch counter of the context (every kernel the library enqueues). */
+kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KPT_H */

@@ -1,0 +1,965 @@
+// kpt_api.cu -- the C ABI (include/kpt.h): context, scene commit, frame graph.
+//
+// Host-side counterpart of KittlesPT::Renderer (renderer.cu) and
+// RendererResource (renderer_resource.cuh): the context owns every device
+// buffer; a frame is one CUDA graph (sky constants, path kernel, resolve,
+// histogram, exposure, bloom chain, tonemap) re-captured and updated in place
+// each frame, with no host synchronisation inside it.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kpt.h"
+#include "kpt_internal.h"
+#include "kpt_post.h"
+#include "kpt_scene.h"
+
+using namespace kpt;
+
+namespace {
+
+thread_local std::string g_error;
+
+kpt_status fail(kpt_status code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+#define KPT_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(e_ == cudaErrorMemoryAllocation ? KPT_ERR_NOMEM : KPT_ERR_CUDA,             \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+    } while (0)
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc((void**)&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    cudaError_t upload(const T* src, size_t count, cudaStream_t s) {
+        cudaError_t e = ensure(count);
+        if (e != cudaSuccess || count == 0) return e;
+        return cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+void rows_of(const float* cm, float4* rows, int nrows) {   // column-major Mat4 -> rows
+    for (int r = 0; r < nrows; ++r) rows[r] = make_float4(cm[r], cm[4 + r], cm[8 + r], cm[12 + r]);
+}
+
+}  // namespace
+
+struct kpt_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+
+    // host scene
+    std::vector<kpt_material> materials;
+    std::vector<HostMesh> meshes;
+    std::vector<HostInstance> instances;
+    std::vector<TexRec> textures;
+    std::vector<uint8_t> pixels;
+    bool committed = false, tlas_dirty = true;
+    int nlights = 0;
+
+    // device scene
+    DBuf<BvhNode> d_nodes, d_tlas;
+    DBuf<float4> d_tris;
+    DBuf<TriShade> d_shade;
+    DBuf<MeshRec> d_meshes;
+    DBuf<InstRec> d_inst;
+    DBuf<LightRec> d_lights;
+    DBuf<MatRec> d_materials;
+    DBuf<TexRec> d_textures;
+    DBuf<uint8_t> d_pixels;
+    SceneView view{};
+    std::vector<int> mesh_node_base, mesh_tri_base;
+    std::vector<InstRec> h_inst;
+
+    // camera and settings
+    float inv_proj[16], inv_view[16];
+    bool has_camera = false;
+    kpt_environment env;
+    kpt_settings settings;
+    kpt_exposure exposure;
+
+    // frame buffers
+    int W = 0, H = 0;
+    int frame_index = 0;
+    DBuf<float4> acc, albedo, render, image;
+    DBuf<int4> first_hit;
+    std::vector<DBuf<float4>> mips;
+    std::vector<int2> mip_dims;
+    DBuf<unsigned long long> hist, counters;
+    DBuf<float> thresholds;
+    float thr_black = NAN, thr_white = NAN;
+    DBuf<ExposureState> expo_state;
+    DBuf<float3> sun_radiance;
+    DBuf<int> work_counter;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    // timing of the path kernel inside the frame graph: a ring of event pairs
+    static constexpr int EV_RING = 256;
+    cudaEvent_t ev_start[EV_RING] = {}, ev_stop[EV_RING] = {};
+    bool timing = false;
+    int frames_rendered = 0, last_slot = 0;
+};
+
+extern "C" {
+
+const char* kpt_last_error(void) { return g_error.c_str(); }
+
+void kpt_environment_default(kpt_environment* e) {   // pod_types.hpp:37-44, atmosphere.cuh:292-310
+    e->sun_angular_diameter = 0.0087f;
+    e->sun_phi = 4.18879f;
+    e->sun_theta = 17.0f * 3.14159265358979323846f / 180.0f;
+    e->sun_emission_factor = 1.0f;
+    e->rayleigh[0] = 3.8e-6f;
+    e->rayleigh[1] = 13.5e-6f;
+    e->rayleigh[2] = 33.1e-6f;
+    e->mie = 21e-6f;
+    e->mie_absorption = 21e-6f * 0.1f;
+    e->rayleigh_height = 7994.0f;
+    e->mie_height = 1200.0f;
+    e->pad = 0.0f;
+}
+
+void kpt_settings_default(kpt_settings* s) {   // pod_types.hpp:46-57
+    s->max_depth = 3;
+    s->bloom = 0;
+    s->karis = 0;
+    s->auto_exposure = 0;
+    s->bloom_final_blend = 0.175f;
+    s->bloom_internal_blend = 0.65f;
+    s->frame_delta_ms = 16.0f;
+    s->rng_order = 0;
+}
+
+void kpt_exposure_default(kpt_exposure* e) {   // SampleApp camera_controller.hpp:55-60
+    e->aperture = 11.0f;
+    e->iso = 100.0f;
+    e->shutter = 0.004f;
+    e->ev_comp = 0.0f;
+    e->white_ev = 6.5f;
+    e->black_ev = -10.0f;
+    e->max_iso = 6400.0f;
+    e->min_iso = 100.0f;
+    e->max_shutter = 1.0f / 30.0f;
+    e->min_shutter = 1.0f / 400.0f;
+    e->pad0 = e->pad1 = 0.0f;
+}
+
+kpt_status kpt_create(int device, kpt_context** out) {
+    if (!out) return fail(KPT_ERR_INVALID, "kpt_create: null output");
+    int n = 0;
+    KPT_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(KPT_ERR_INVALID, "kpt_create: no such device");
+    KPT_CUDA(cudaSetDevice(device));
+    kpt_context* c = new kpt_context();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(KPT_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    kpt_environment_default(&c->env);
+    kpt_settings_default(&c->settings);
+    kpt_exposure_default(&c->exposure);
+    if (c->expo_state.ensure(1) != cudaSuccess || c->sun_radiance.ensure(1) != cudaSuccess ||
+        c->work_counter.ensure(1) != cudaSuccess || c->counters.ensure(4) != cudaSuccess ||
+        c->hist.ensure(256) != cudaSuccess || c->thresholds.ensure(256) != cudaSuccess) {
+        kpt_destroy(c);
+        return fail(KPT_ERR_NOMEM, "kpt_create: device allocation failed");
+    }
+    cudaMemsetAsync(c->expo_state.p, 0, sizeof(ExposureState), c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream);
+    *out = c;
+    return KPT_OK;
+}
+
+kpt_status kpt_destroy(kpt_context* c) {
+    if (!c) return KPT_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    for (int i = 0; i < kpt_context::EV_RING; ++i) {
+        if (c->ev_start[i]) cudaEventDestroy(c->ev_start[i]);
+        if (c->ev_stop[i]) cudaEventDestroy(c->ev_stop[i]);
+    }
+    c->d_nodes.release(); c->d_tlas.release(); c->d_tris.release(); c->d_shade.release();
+    c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
+    c->d_textures.release(); c->d_pixels.release();
+    c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
+    for (auto& m : c->mips) m.release();
+    c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
+    c->sun_radiance.release(); c->work_counter.release();
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return KPT_OK;
+}
+
+static kpt_status clear_accumulation(kpt_context* c) {
+    c->frame_index = 0;
+    if (c->acc.p) KPT_CUDA(cudaMemsetAsync(c->acc.p, 0, sizeof(float4) * (size_t)c->W * c->H, c->stream));
+    return KPT_OK;
+}
+
+kpt_status kpt_resize(kpt_context* c, int w, int h) {
+    if (!c || w <= 0 || h <= 0) return fail(KPT_ERR_INVALID, "kpt_resize: bad size");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (w == c->W && h == c->H) return KPT_OK;
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    size_t np = (size_t)w * h;
+    KPT_CUDA(c->acc.ensure(np));
+    KPT_CUDA(c->albedo.ensure(np));
+    KPT_CUDA(c->render.ensure(np));
+    KPT_CUDA(c->image.ensure(np));
+    KPT_CUDA(c->first_hit.ensure(np));
+    // bloom mip chain (mipchain.cuh:17-36): levels below mip 0, at most 6
+    int levels = std::min((int)std::log2((double)w), (int)std::log2((double)h));
+    levels = std::min(levels, 6);
+    for (auto& m : c->mips) m.release();
+    c->mips.assign(levels + 1, DBuf<float4>());
+    c->mip_dims.assign(levels + 1, make_int2(0, 0));
+    for (int l = 0; l <= levels; ++l) {
+        c->mip_dims[l] = make_int2(w >> l, h >> l);
+        KPT_CUDA(c->mips[l].ensure((size_t)(w >> l) * (h >> l)));
+    }
+    c->W = w;
+    c->H = h;
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    return clear_accumulation(c);
+}
+
+kpt_status kpt_set_materials(kpt_context* c, int n, const kpt_material* m) {
+    if (!c || n < 0 || (n > 0 && !m)) return fail(KPT_ERR_INVALID, "kpt_set_materials: bad arguments");
+    c->materials.assign(m, m + n);
+    c->committed = false;
+    return KPT_OK;
+}
+
+kpt_status kpt_set_textures(kpt_context* c, int n, const int32_t* desc, size_t nbytes, const uint8_t* pixels) {
+    if (!c || n < 0 || (n > 0 && !desc) || (nbytes > 0 && !pixels)) return fail(KPT_ERR_INVALID, "kpt_set_textures: bad arguments");
+    c->textures.resize(n);
+    for (int i = 0; i < n; ++i) {
+        c->textures[i].w = desc[4 * i];
+        c->textures[i].h = desc[4 * i + 1];
+        c->textures[i].ch = desc[4 * i + 2];
+        c->textures[i].offset = desc[4 * i + 3];
+        c->textures[i].pad = 0;
+        if (c->textures[i].w <= 0 || c->textures[i].h <= 0 || c->textures[i].ch < 3)
+            return fail(KPT_ERR_INVALID, "kpt_set_textures: bad texture descriptor");
+    }
+    c->pixels.assign(pixels, pixels + nbytes);
+    c->committed = false;
+    return KPT_OK;
+}
+
+kpt_status kpt_upload_mesh(kpt_context* c, int ntris, const float* pos, const float* nrm, const float* uv,
+                           const int32_t* mat, int* mesh_out) {
+    if (!c || ntris <= 0 || !pos || !mat) return fail(KPT_ERR_INVALID, "kpt_upload_mesh: bad arguments");
+    HostMesh m;
+    m.pos.assign(pos, pos + 9 * (size_t)ntris);
+    if (nrm) m.nrm.assign(nrm, nrm + 9 * (size_t)ntris);
+    else m.nrm.assign(9 * (size_t)ntris, 0.0f);
+    if (uv) m.uv.assign(uv, uv + 6 * (size_t)ntris);
+    else m.uv.assign(6 * (size_t)ntris, 0.0f);
+    m.material.assign(mat, mat + ntris);
+    for (int i = 0; i < ntris; ++i)
+        if (mat[i] < 0) return fail(KPT_ERR_INVALID, "kpt_upload_mesh: negative material id");
+    build_blas(m);
+    c->meshes.push_back(std::move(m));
+    if (mesh_out) *mesh_out = (int)c->meshes.size() - 1;
+    c->committed = false;
+    return KPT_OK;
+}
+
+kpt_status kpt_add_instance(kpt_context* c, int mesh, const float* model, int material, int* out) {
+    if (!c || !model || mesh < 0 || mesh >= (int)c->meshes.size())
+        return fail(KPT_ERR_INVALID, "kpt_add_instance: bad mesh or matrix");
+    HostInstance hi;
+    hi.mesh = mesh;
+    std::memcpy(hi.model, model, sizeof hi.model);
+    hi.material = material;
+    c->instances.push_back(hi);
+    if (out) *out = (int)c->instances.size() - 1;
+    c->committed = false;
+    return KPT_OK;
+}
+
+kpt_status kpt_clear_scene(kpt_context* c) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    c->meshes.clear();
+    c->instances.clear();
+    c->materials.clear();
+    c->textures.clear();
+    c->pixels.clear();
+    c->committed = false;
+    return KPT_OK;
+}
+
+static bool emissive(const kpt_material& m) {   // MaterialSceneEntity::isEmissive (pod_types.hpp:118-122)
+    return m.emission[0] * m.emission_scale > 0.0f || m.emission[1] * m.emission_scale > 0.0f ||
+           m.emission[2] * m.emission_scale > 0.0f;
+}
+
+static InstRec make_inst(const kpt_context* c, const HostInstance& hi) {
+    InstRec r{};
+    float inv[16], model[16];
+    inverse4(hi.model, inv);      // BLAS2::setTransform (blas.cuh:338-348)
+    inverse4(inv, model);         // the per-hit inverse of the mesh inverse (interaction.cu:20)
+    rows_of(inv, r.inv, 3);
+    rows_of(model, r.model, 3);
+    r.mesh = hi.mesh;
+    r.material = hi.material;
+    r.light_first = -1;
+    r.light_all = 0;
+    (void)c;
+    return r;
+}
+
+static kpt_status rebuild_tlas(kpt_context* c) {
+    int n = (int)c->instances.size();
+    std::vector<float> lo(3 * (size_t)n), hi(3 * (size_t)n);
+    for (int i = 0; i < n; ++i)
+        instance_bounds(c->meshes[c->instances[i].mesh], c->instances[i].model, &lo[3 * i], &hi[3 * i]);
+    float rlo[3], rhi[3];
+    int root_leaf = 0, depth = 0;
+    std::vector<BvhNode> t = build_tlas(lo, hi, n, rlo, rhi, &root_leaf, &depth);
+    if (depth > TLAS_STACK - 1) return fail(KPT_ERR_STATE, "TLAS deeper than the traversal stack");
+    KPT_CUDA(c->d_tlas.upload(t.data(), t.size(), c->stream));
+    c->view.tlas = c->d_tlas.p;
+    c->view.ntlas = (int)t.size();
+    c->view.tlas_lo = make_float4(rlo[0], rlo[1], rlo[2], 0.0f);
+    c->view.tlas_hi = make_float4(rhi[0], rhi[1], rhi[2], 0.0f);
+    c->view.tlas_root_leaf = root_leaf;
+    for (int i = 0; i < n; ++i) {
+        InstRec r = make_inst(c, c->instances[i]);
+        r.light_first = c->h_inst[i].light_first;
+        r.light_all = c->h_inst[i].light_all;
+        r.prim_base = c->h_inst[i].prim_base;
+        c->h_inst[i] = r;
+    }
+    KPT_CUDA(c->d_inst.upload(c->h_inst.data(), c->h_inst.size(), c->stream));
+    c->view.inst = c->d_inst.p;
+    c->tlas_dirty = false;
+    return KPT_OK;
+}
+
+kpt_status kpt_commit_scene(kpt_context* c) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (c->instances.empty()) return fail(KPT_ERR_STATE, "kpt_commit_scene: no instances");
+    int nm = (int)c->materials.size();
+    for (auto& m : c->meshes)
+        for (int id : m.material)
+            if (id >= nm) return fail(KPT_ERR_INVALID, "kpt_commit_scene: material id out of range");
+    for (auto& i : c->instances)
+        if (i.material >= nm) return fail(KPT_ERR_INVALID, "kpt_commit_scene: material override out of range");
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    // BLAS nodes and triangles, mesh after mesh
+    std::vector<BvhNode> nodes;
+    std::vector<float4> tris;
+    std::vector<TriShade> shade;
+    std::vector<MeshRec> mrec;
+    for (auto& m : c->meshes) {
+        MeshRec r{};
+        int nb = (int)nodes.size(), tb = (int)(tris.size() / 3);
+        for (BvhNode n : m.nodes) {
+            if (n.d.y == 0) n.d.x += nb; else n.d.x += tb;
+            if (n.d.w == 0) n.d.z += nb; else n.d.z += tb;
+            nodes.push_back(n);
+        }
+        r.node_root = m.root >= 0 ? nb + m.root : -1;
+        r.leaf_first = tb + m.leaf_first;
+        r.leaf_count = m.leaf_count;
+        r.ntris = m.ntris();
+        r.tri_base = tb;
+        r.shade_base = (int)shade.size();
+        if (m.max_depth > BLAS_STACK - 1) return fail(KPT_ERR_STATE, "BLAS deeper than the traversal stack");
+        for (int k = 0; k < m.ntris(); ++k) {
+            int t = m.order[k];
+            const float* p = &m.pos[9 * (size_t)t];
+            float lid;
+            std::memcpy(&lid, &t, 4);
+            tris.push_back(make_float4(p[0], p[1], p[2], lid));
+            tris.push_back(make_float4(p[3] - p[0], p[4] - p[1], p[5] - p[2], 0.0f));
+            tris.push_back(make_float4(p[6] - p[0], p[7] - p[1], p[8] - p[2], 0.0f));
+        }
+        int rank = 0;
+        for (int t = 0; t < m.ntris(); ++t) {
+            TriShade s{};
+            const float* u = &m.uv[6 * (size_t)t];
+            s.uv0 = make_float2(u[0], u[1]);
+            s.uv1 = make_float2(u[2], u[3]);
+            s.uv2 = make_float2(u[4], u[5]);
+            float gn[3], area;
+            tri_normal_area(&m.pos[9 * (size_t)t], &m.nrm[9 * (size_t)t], gn, &area);
+            s.gnx = gn[0]; s.gny = gn[1]; s.gnz = gn[2];
+            s.material = m.material[t];
+            s.emissive_rank = emissive(c->materials[m.material[t]]) ? rank++ : -1;
+            shade.push_back(s);
+        }
+        r.n_emissive = rank;
+        mrec.push_back(r);
+    }
+    // instances and lights (renderer.cu:393-401: one light per emissive triangle)
+    std::vector<LightRec> lights;
+    c->h_inst.assign(c->instances.size(), InstRec{});
+    int prim_base = 0;
+    for (size_t i = 0; i < c->instances.size(); ++i) {
+        const HostInstance& hi = c->instances[i];
+        const HostMesh& m = c->meshes[hi.mesh];
+        InstRec r = make_inst(c, hi);
+        r.prim_base = prim_base;
+        prim_base += m.ntris();
+        bool all = hi.material >= 0 && emissive(c->materials[hi.material]);
+        bool own = hi.material < 0 && mrec[hi.mesh].n_emissive > 0;
+        if (all || own) {
+            r.light_first = (int)lights.size();
+            r.light_all = all ? 1 : 0;
+            for (int t = 0; t < m.ntris(); ++t) {
+                int mat = hi.material >= 0 ? hi.material : m.material[t];
+                if (!all && !emissive(c->materials[mat])) continue;
+                LightRec L{};
+                const float* p = &m.pos[9 * (size_t)t];
+                L.p0 = make_float3(p[0], p[1], p[2]);
+                L.p1 = make_float3(p[3], p[4], p[5]);
+                L.p2 = make_float3(p[6], p[7], p[8]);
+                float gn[3], area;
+                tri_normal_area(p, &m.nrm[9 * (size_t)t], gn, &area);
+                L.gn = make_float3(gn[0], gn[1], gn[2]);
+                const float* u = &m.uv[6 * (size_t)t];
+                L.uv0 = make_float2(u[0], u[1]);
+                L.uv1 = make_float2(u[2], u[3]);
+                L.uv2 = make_float2(u[4], u[5]);
+                L.area = area;
+                L.tri_area = area;
+                L.inst = (int)i;
+                L.tri = t;
+                L.material = mat;
+                lights.push_back(L);
+            }
+        }
+        c->h_inst[i] = r;
+    }
+    std::vector<MatRec> mats(c->materials.size());
+    static_assert(sizeof(MatRec) == sizeof(kpt_material), "material layout");
+    std::memcpy(mats.data(), c->materials.data(), sizeof(kpt_material) * mats.size());
+    KPT_CUDA(c->d_nodes.upload(nodes.data(), nodes.size(), c->stream));
+    KPT_CUDA(c->d_tris.upload(tris.data(), tris.size(), c->stream));
+    KPT_CUDA(c->d_shade.upload(shade.data(), shade.size(), c->stream));
+    KPT_CUDA(c->d_meshes.upload(mrec.data(), mrec.size(), c->stream));
+    KPT_CUDA(c->d_lights.upload(lights.data(), lights.size(), c->stream));
+    KPT_CUDA(c->d_materials.upload(mats.data(), mats.size(), c->stream));
+    KPT_CUDA(c->d_textures.upload(c->textures.data(), c->textures.size(), c->stream));
+    KPT_CUDA(c->d_pixels.upload(c->pixels.data(), c->pixels.size(), c->stream));
+    SceneView& v = c->view;
+    v.nodes = c->d_nodes.p;
+    v.tris = c->d_tris.p;
+    v.shade = c->d_shade.p;
+    v.meshes = c->d_meshes.p;
+    v.lights = c->d_lights.p;
+    v.materials = c->d_materials.p;
+    v.textures = c->d_textures.p;
+    v.pixels = c->d_pixels.p;
+    v.npixels = (long long)c->pixels.size();
+    v.nlights = (int)lights.size();
+    v.ninst = (int)c->instances.size();
+    v.ntextures = (int)c->textures.size();
+    c->nlights = (int)lights.size();
+    kpt_status s = rebuild_tlas(c);
+    if (s != KPT_OK) return s;
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    c->committed = true;
+    return clear_accumulation(c);
+}
+
+kpt_status kpt_counts(kpt_context* c, int* materials, int* meshes, int* instances, int* lights) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    if (materials) *materials = (int)c->materials.size();
+    if (meshes) *meshes = (int)c->meshes.size();
+    if (instances) *instances = (int)c->instances.size();
+    if (lights) *lights = c->nlights;
+    return KPT_OK;
+}
+
+kpt_status kpt_set_material(kpt_context* c, int idx, const kpt_material* m) {
+    if (!c || !m) return fail(KPT_ERR_INVALID, "kpt_set_material: null argument");
+    if (idx < 0 || idx >= (int)c->materials.size()) return fail(KPT_ERR_INVALID, "kpt_set_material: index out of range");
+    c->materials[idx] = *m;
+    if (c->committed) {
+        KPT_CUDA(cudaMemcpyAsync(c->d_materials.p + idx, m, sizeof(MatRec), cudaMemcpyHostToDevice, c->stream));
+        KPT_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return clear_accumulation(c);
+}
+
+kpt_status kpt_get_material(kpt_context* c, int idx, kpt_material* m) {
+    if (!c || !m) return fail(KPT_ERR_INVALID, "kpt_get_material: null argument");
+    if (idx < 0 || idx >= (int)c->materials.size()) return fail(KPT_ERR_INVALID, "kpt_get_material: index out of range");
+    *m = c->materials[idx];
+    return KPT_OK;
+}
+
+kpt_status kpt_set_instance_transform(kpt_context* c, int idx, const float* model) {
+    if (!c || !model) return fail(KPT_ERR_INVALID, "kpt_set_instance_transform: null argument");
+    if (idx < 0 || idx >= (int)c->instances.size()) return fail(KPT_ERR_INVALID, "kpt_set_instance_transform: index out of range");
+    for (int i = 0; i < 16; ++i)
+        if (!std::isfinite(model[i])) return fail(KPT_ERR_INVALID, "kpt_set_instance_transform: non-finite matrix");
+    std::memcpy(c->instances[idx].model, model, 16 * sizeof(float));
+    c->tlas_dirty = true;
+    return clear_accumulation(c);
+}
+
+kpt_status kpt_get_instance_transform(kpt_context* c, int idx, float* model) {
+    if (!c || !model) return fail(KPT_ERR_INVALID, "kpt_get_instance_transform: null argument");
+    if (idx < 0 || idx >= (int)c->instances.size()) return fail(KPT_ERR_INVALID, "kpt_get_instance_transform: index out of range");
+    std::memcpy(model, c->instances[idx].model, 16 * sizeof(float));
+    return KPT_OK;
+}
+
+kpt_status kpt_set_camera_inverse(kpt_context* c, const float* ip, const float* iv) {
+    if (!c || !ip || !iv) return fail(KPT_ERR_INVALID, "kpt_set_camera_inverse: null argument");
+    std::memcpy(c->inv_proj, ip, sizeof c->inv_proj);
+    std::memcpy(c->inv_view, iv, sizeof c->inv_view);
+    c->has_camera = true;
+    return clear_accumulation(c);
+}
+
+kpt_status kpt_set_view(kpt_context* c, const float* proj, const float* view) {
+    if (!c || !proj || !view) return fail(KPT_ERR_INVALID, "kpt_set_view: null argument");
+    float ip[16], iv[16];
+    inverse4(proj, ip);
+    inverse4(view, iv);
+    return kpt_set_camera_inverse(c, ip, iv);
+}
+
+kpt_status kpt_set_environment(kpt_context* c, const kpt_environment* e) {
+    if (!c || !e) return fail(KPT_ERR_INVALID, "kpt_set_environment: null argument");
+    if (!(e->rayleigh_height > 0.0f) || !(e->mie_height > 0.0f)) return fail(KPT_ERR_INVALID, "kpt_set_environment: scale heights must be positive");
+    c->env = *e;
+    return clear_accumulation(c);
+}
+kpt_status kpt_get_environment(kpt_context* c, kpt_environment* e) {
+    if (!c || !e) return fail(KPT_ERR_INVALID, "null argument");
+    *e = c->env;
+    return KPT_OK;
+}
+kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
+    if (!c || !s) return fail(KPT_ERR_INVALID, "kpt_set_settings: null argument");
+    if (s->max_depth < 0 || s->max_depth > 64) return fail(KPT_ERR_INVALID, "kpt_set_settings: max_depth out of range");
+    c->settings = *s;
+    return clear_accumulation(c);
+}
+kpt_status kpt_get_settings(kpt_context* c, kpt_settings* s) {
+    if (!c || !s) return fail(KPT_ERR_INVALID, "null argument");
+    *s = c->settings;
+    return KPT_OK;
+}
+kpt_status kpt_set_exposure(kpt_context* c, const kpt_exposure* e) {
+    if (!c || !e) return fail(KPT_ERR_INVALID, "kpt_set_exposure: null argument");
+    if (!(e->aperture > 0.0f) || !(e->iso > 0.0f) || !(e->shutter > 0.0f) || !(e->white_ev > e->black_ev))
+        return fail(KPT_ERR_INVALID, "kpt_set_exposure: invalid camera values");
+    c->exposure = *e;
+    return KPT_OK;
+}
+kpt_status kpt_get_exposure(kpt_context* c, kpt_exposure* e) {
+    if (!c || !e) return fail(KPT_ERR_INVALID, "null argument");
+    *e = c->exposure;
+    return KPT_OK;
+}
+kpt_status kpt_reset_accumulation(kpt_context* c) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    return clear_accumulation(c);
+}
+
+static SkyParams sky_params(const kpt_environment& e) {
+    SkyParams P{};
+    // getSunDirection (integrator.cuh:222-230), single precision as on the device
+    float cp = cosf(e.sun_phi), sp = sinf(e.sun_phi), ct = cosf(e.sun_theta), st = sinf(e.sun_theta);
+    float3 d = make_float3(cp * ct, st, sp * ct);
+    float inv = 1.0f / sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+    P.sun_dir = make_float3(d.x * inv, d.y * inv, d.z * inv);
+    P.sun_emission = e.sun_emission_factor;
+    P.sigma_r = make_float3(e.rayleigh[0], e.rayleigh[1], e.rayleigh[2]);
+    P.sigma_m = e.mie;
+    P.sigma_am = e.mie_absorption;
+    P.h_r = e.rayleigh_height;
+    P.h_m = e.mie_height;
+    P.earth_r = 6378137.0f;
+    P.atm_r = 6438137.0f;
+    P.cos_half_sun = cosf(e.sun_angular_diameter / 2.0f);   // LeSun (integrator.cuh:137)
+    // angularDiameterToPhysicalDiameter / 2 (atmosphere.cuh:79-82)
+    P.sun_radius_m = (2.0f * 149.597e9f * tanf(e.sun_angular_diameter / 2.0f)) / 2.0f;
+    return P;
+}
+
+static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
+    FrameParams F{};
+    F.scene = c->view;
+    F.sky = sky_params(c->env);
+    rows_of(c->inv_proj, F.inv_proj, 4);
+    rows_of(c->inv_view, F.inv_view, 3);
+    F.cam_pos = make_float3(c->inv_view[12], c->inv_view[13], c->inv_view[14]);
+    F.W = c->W;
+    F.H = c->H;
+    F.sample0 = sample0;
+    F.nsamples = nsamples;
+    F.max_depth = c->settings.max_depth;
+    F.rng_order = c->settings.rng_order;
+    F.sun_radiance = c->sun_radiance.p;
+    F.work_counter = c->work_counter.p;
+    F.counters = c->counters.p;
+    return F;
+}
+
+static int path_grid(kpt_context* c) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_path, PATH_BLOCK, 0);
+    return std::max(1, per_sm) * c->sm_count;
+}
+
+static kpt_status ready(kpt_context* c) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    if (!c->committed) return fail(KPT_ERR_STATE, "no committed scene");
+    if (!c->has_camera) return fail(KPT_ERR_STATE, "no camera");
+    if (c->W <= 0) return fail(KPT_ERR_STATE, "no resolution");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (c->tlas_dirty) return rebuild_tlas(c);
+    return KPT_OK;
+}
+
+static void update_thresholds(kpt_context* c) {
+    if (c->thr_black == c->exposure.black_ev && c->thr_white == c->exposure.white_ev) return;
+    // luminanceToBin (histogram.cu:18-33) as thresholds: bin >= k+1 iff
+    // Y >= 2^(black + range*k/254); evaluated in double, rounded up to float
+    float thr[256];
+    double range = (double)c->exposure.white_ev - (double)c->exposure.black_ev;
+    thr[0] = 0.005f;
+    for (int k = 1; k < 255; ++k) {
+        double v = exp2((double)c->exposure.black_ev + range * (double)k / 254.0);
+        float f = (float)v;
+        if ((double)f < v) f = nextafterf(f, INFINITY);
+        thr[k] = f;
+    }
+    thr[255] = INFINITY;
+    cudaMemcpyAsync(c->thresholds.p, thr, sizeof thr, cudaMemcpyHostToDevice, c->stream);
+    c->thr_black = c->exposure.black_ev;
+    c->thr_white = c->exposure.white_ev;
+}
+
+// The frame: enqueued on the context stream (captured into a graph).
+static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
+    cudaStream_t s = c->stream;
+    const int np = c->W * c->H;
+    cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), s);
+    k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
+    int slot = c->frames_rendered % kpt_context::EV_RING;
+    c->last_slot = slot;
+    if (c->timing) cudaEventRecordWithFlags(c->ev_start[slot], s, cudaEventRecordExternal);
+    k_path<<<path_grid(c), PATH_BLOCK, 0, s>>>(F);
+    if (c->timing) cudaEventRecordWithFlags(c->ev_stop[slot], s, cudaEventRecordExternal);
+    k_resolve<<<(np + 255) / 256, 256, 0, s>>>(np, c->acc.p, c->albedo.p, (float)total_samples, c->render.p);
+    c->launches += 3;
+    if (c->settings.auto_exposure) {
+        ExposureIn in{};
+        in.aperture = c->exposure.aperture;
+        in.ev_comp = c->exposure.ev_comp;
+        in.white_ev = c->exposure.white_ev;
+        in.black_ev = c->exposure.black_ev;
+        in.min_iso = c->exposure.min_iso;
+        in.max_iso = c->exposure.max_iso;
+        in.min_shutter = c->exposure.min_shutter;
+        in.max_shutter = c->exposure.max_shutter;
+        in.delta_ms = delta_ms;
+        cudaMemsetAsync(c->hist.p, 0, 256 * sizeof(unsigned long long), s);
+        k_histogram<<<(np + 255) / 256, 256, 0, s>>>(c->W, c->H, c->render.p, c->thresholds.p, c->hist.p);
+        k_exposure<<<1, 32, 0, s>>>(c->hist.p, c->expo_state.p, in);
+        c->launches += 2;
+    }
+    const float4* bloom0 = nullptr;
+    int levels = (int)c->mips.size() - 1;
+    if (c->settings.bloom && levels > 0) {
+        dim3 b(16, 16);
+        for (int l = 0; l < levels; ++l) {
+            int2 sd = c->mip_dims[l], dd = c->mip_dims[l + 1];
+            const float4* src = l == 0 ? c->render.p : c->mips[l].p;
+            k_bloom_down<<<dim3((dd.x + 15) / 16, (dd.y + 15) / 16), b, 0, s>>>(src, sd.x, sd.y, c->mips[l + 1].p, dd.x, dd.y,
+                                                                               c->settings.karis && l == 0);
+        }
+        // mip 0 starts as a copy of the render (renderer.cu:446-451)
+        cudaMemcpyAsync(c->mips[0].p, c->render.p, sizeof(float4) * (size_t)np, cudaMemcpyDeviceToDevice, s);
+        for (int l = levels; l > 0; --l) {
+            int2 sd = c->mip_dims[l], dd = c->mip_dims[l - 1];
+            k_bloom_up<<<dim3((dd.x + 15) / 16, (dd.y + 15) / 16), b, 0, s>>>(c->mips[l].p, sd.x, sd.y, c->mips[l - 1].p,
+                                                                             dd.x, dd.y, c->settings.bloom_internal_blend);
+        }
+        c->launches += 2 * levels;
+        bloom0 = c->mips[0].p;
+    }
+    double N = c->exposure.aperture;
+    double lavg = (10.0 / 0.65) * ((N * N) / ((double)c->exposure.iso * (double)c->exposure.shutter));
+    float fixed_scalar = (float)(0.18 / lavg);
+    k_tonemap<<<dim3((c->W + 15) / 16, (c->H + 15) / 16), dim3(16, 16), 0, s>>>(
+        c->W, c->H, c->render.p, bloom0, bloom0 != nullptr, c->settings.bloom_final_blend, c->expo_state.p, fixed_scalar,
+        c->settings.auto_exposure, c->exposure.white_ev, c->exposure.black_ev, c->image.p);
+    c->launches += 1;
+}
+
+kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
+    kpt_status st = ready(c);
+    if (st != KPT_OK) return st;
+    if (spp <= 0) return fail(KPT_ERR_INVALID, "kpt_render_frame: spp must be positive");
+    update_thresholds(c);
+    FrameParams F = frame_params(c, c->frame_index, spp);
+    F.acc = c->acc.p;
+    F.albedo = c->albedo.p;
+    F.first_hit = c->first_hit.p;
+    int total = c->frame_index + spp;
+    cudaGraph_t g = nullptr;
+    KPT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_frame(c, F, total, delta_ms);
+    KPT_CUDA(cudaStreamEndCapture(c->stream, &g));
+    if (c->graph_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(c->graph_exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+        }
+    }
+    if (!c->graph_exec) {
+        cudaError_t e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return fail(KPT_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaError_t e = cudaGraphLaunch(c->graph_exec, c->stream);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(KPT_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+    c->frame_index = total;
+    c->frames_rendered++;
+    return KPT_OK;
+}
+
+kpt_status kpt_synchronize(kpt_context* c) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    return KPT_OK;
+}
+
+static kpt_status read_buf(kpt_context* c, const void* src, void* dst, size_t bytes) {
+    if (!c || !dst) return fail(KPT_ERR_INVALID, "null argument");
+    if (!src) return fail(KPT_ERR_STATE, "buffer not allocated");
+    KPT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    return KPT_OK;
+}
+kpt_status kpt_read_image(kpt_context* c, float* rgba) { return read_buf(c, c ? c->image.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
+kpt_status kpt_read_render(kpt_context* c, float* rgba) { return read_buf(c, c ? c->render.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
+kpt_status kpt_read_accumulation(kpt_context* c, float* rgba) { return read_buf(c, c ? c->acc.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
+kpt_status kpt_read_albedo(kpt_context* c, float* rgba) { return read_buf(c, c ? c->albedo.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
+kpt_status kpt_read_histogram(kpt_context* c, uint64_t* bins) { return read_buf(c, c ? c->hist.p : nullptr, bins, 256 * sizeof(uint64_t)); }
+
+kpt_status kpt_get_stats(kpt_context* c, kpt_stats* st) {
+    if (!c || !st) return fail(KPT_ERR_INVALID, "null argument");
+    unsigned long long cnt[4];
+    ExposureState es;
+    KPT_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaMemcpyAsync(&es, c->expo_state.p, sizeof es, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    st->box_tests = cnt[0];
+    st->tri_tests = cnt[1];
+    st->inst_xforms = cnt[2];
+    st->overflows = cnt[3];
+    st->avg_luminance = es.avg_lum;
+    st->adapted_luminance = es.adapted_lum;
+    st->exposure_scalar = es.exposure_scalar;
+    st->iso = es.iso;
+    st->shutter = es.shutter;
+    st->avg_bin = es.avg_bin;
+    st->frame_index = c->frame_index;
+    st->pad = 0;
+    return KPT_OK;
+}
+
+kpt_status kpt_render_samples_device(kpt_context* c, int sample0, int nsamples, float* radiance, int32_t* first_hit,
+                                     float* albedo) {
+    kpt_status st = ready(c);
+    if (st != KPT_OK) return st;
+    if (nsamples <= 0 || sample0 < 0) return fail(KPT_ERR_INVALID, "kpt_render_samples_device: bad sample range");
+    FrameParams F = frame_params(c, sample0, nsamples);
+    F.sample_out = reinterpret_cast<float4*>(radiance);
+    F.first_hit = reinterpret_cast<int4*>(first_hit);
+    F.albedo = reinterpret_cast<float4*>(albedo);
+    KPT_CUDA(cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), c->stream));
+    k_sky_constants<<<1, 32, 0, c->stream>>>(F, c->sun_radiance.p);
+    k_path<<<path_grid(c), PATH_BLOCK, 0, c->stream>>>(F);
+    c->launches += 2;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+static int trace_grid(kpt_context* c, const void* kern, int n) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TRACE_BLOCK, 0);
+    int g = std::max(1, per_sm) * c->sm_count;
+    return std::min(g, (n + TRACE_BLOCK - 1) / TRACE_BLOCK);
+}
+
+static kpt_status scene_ready(kpt_context* c) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    if (!c->committed) return fail(KPT_ERR_STATE, "no committed scene");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (c->tlas_dirty) return rebuild_tlas(c);
+    return KPT_OK;
+}
+
+kpt_status kpt_trace_device(kpt_context* c, int n, const float* o, const float* d, float tmin, float tmax, int32_t* inst,
+                            int32_t* tri, float* t, float* uv) {
+    kpt_status st = scene_ready(c);
+    if (st != KPT_OK) return st;
+    if (n < 0 || (n > 0 && (!o || !d || !inst || !tri || !t))) return fail(KPT_ERR_INVALID, "kpt_trace_device: bad arguments");
+    if (n == 0) return KPT_OK;
+    k_trace<<<trace_grid(c, (const void*)k_trace, n), TRACE_BLOCK, 0, c->stream>>>(
+        c->view, n, (const float3*)o, (const float3*)d, tmin, tmax, inst, tri, t, (float2*)uv, c->counters.p);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+kpt_status kpt_occluded_device(kpt_context* c, int n, const float* o, const float* d, float tmin, const float* tmax,
+                               uint8_t* out) {
+    kpt_status st = scene_ready(c);
+    if (st != KPT_OK) return st;
+    if (n < 0 || (n > 0 && (!o || !d || !tmax || !out))) return fail(KPT_ERR_INVALID, "kpt_occluded_device: bad arguments");
+    if (n == 0) return KPT_OK;
+    k_occluded<<<trace_grid(c, (const void*)k_occluded, n), TRACE_BLOCK, 0, c->stream>>>(
+        c->view, n, (const float3*)o, (const float3*)d, tmin, tmax, out, c->counters.p);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+kpt_status kpt_trace_bounces_device(kpt_context* c, int n, const float* o, const float* d, int nb, int32_t* inst,
+                                    int32_t* tri, float* t) {
+    kpt_status st = scene_ready(c);
+    if (st != KPT_OK) return st;
+    if (n < 0 || nb < 0 || (n > 0 && (!o || !d || !inst || !tri || !t)))
+        return fail(KPT_ERR_INVALID, "kpt_trace_bounces_device: bad arguments");
+    if (n == 0) return KPT_OK;
+    k_trace_bounces<<<trace_grid(c, (const void*)k_trace_bounces, n), TRACE_BLOCK, 0, c->stream>>>(
+        c->view, n, (const float3*)o, (const float3*)d, nb, inst, tri, t, c->counters.p);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+kpt_status kpt_trace_bounces(kpt_context* c, int n, const float* o, const float* d, int nb, int32_t* inst, int32_t* tri,
+                             float* t) {
+    kpt_status st = scene_ready(c);
+    if (st != KPT_OK) return st;
+    if (n < 0 || nb < 0 || (n > 0 && (!o || !d || !inst || !tri || !t)))
+        return fail(KPT_ERR_INVALID, "kpt_trace_bounces: bad arguments");
+    if (n == 0) return KPT_OK;
+    size_t nr = (size_t)n, no = nr * (nb + 1);
+    DBuf<float> dev_in;
+    DBuf<int32_t> dev_out;
+    DBuf<float> dev_t;
+    KPT_CUDA(dev_in.ensure(6 * nr));
+    KPT_CUDA(dev_out.ensure(2 * no));
+    KPT_CUDA(dev_t.ensure(no));
+    KPT_CUDA(cudaMemcpyAsync(dev_in.p, o, 12 * nr, cudaMemcpyHostToDevice, c->stream));
+    KPT_CUDA(cudaMemcpyAsync(dev_in.p + 3 * nr, d, 12 * nr, cudaMemcpyHostToDevice, c->stream));
+    st = kpt_trace_bounces_device(c, n, dev_in.p, dev_in.p + 3 * nr, nb, dev_out.p, dev_out.p + no, dev_t.p);
+    if (st == KPT_OK) {
+        KPT_CUDA(cudaMemcpyAsync(inst, dev_out.p, 4 * no, cudaMemcpyDeviceToHost, c->stream));
+        KPT_CUDA(cudaMemcpyAsync(tri, dev_out.p + no, 4 * no, cudaMemcpyDeviceToHost, c->stream));
+        KPT_CUDA(cudaMemcpyAsync(t, dev_t.p, 4 * no, cudaMemcpyDeviceToHost, c->stream));
+        KPT_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    cudaStreamSynchronize(c->stream);
+    dev_in.release();
+    dev_out.release();
+    dev_t.release();
+    return st;
+}
+
+kpt_status kpt_sky_device(kpt_context* c, int n, const float* dirs, float* rgb) {
+    if (!c || n < 0 || (n > 0 && (!dirs || !rgb))) return fail(KPT_ERR_INVALID, "kpt_sky_device: bad arguments");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (n == 0) return KPT_OK;
+    k_sky<<<(n + 127) / 128, 128, 0, c->stream>>>(sky_params(c->env), n, (const float3*)dirs, (float3*)rgb);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+kpt_status kpt_enable_timing(kpt_context* c, int enable) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (enable && !c->ev_start[0]) {
+        for (int i = 0; i < kpt_context::EV_RING; ++i) {
+            KPT_CUDA(cudaEventCreate(&c->ev_start[i]));
+            KPT_CUDA(cudaEventCreate(&c->ev_stop[i]));
+        }
+    }
+    c->timing = enable != 0;
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    return KPT_OK;
+}
+
+kpt_status kpt_path_kernel_ms(kpt_context* c, int nframes, float* total_ms) {
+    if (!c || !total_ms || nframes <= 0 || nframes > kpt_context::EV_RING)
+        return fail(KPT_ERR_INVALID, "kpt_path_kernel_ms: bad arguments");
+    if (!c->timing) return fail(KPT_ERR_STATE, "kpt_path_kernel_ms: timing not enabled");
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    // frames are numbered by frame_index / spp of the frame; walk back from the last one
+    double sum = 0.0;
+    int last = c->last_slot;
+    for (int k = 0; k < nframes; ++k) {
+        int s = ((last - k) % kpt_context::EV_RING + kpt_context::EV_RING) % kpt_context::EV_RING;
+        float ms = 0.0f;
+        KPT_CUDA(cudaEventElapsedTime(&ms, c->ev_start[s], c->ev_stop[s]));
+        sum += ms;
+    }
+    *total_ms = (float)sum;
+    return KPT_OK;
+}
+
+kpt_status kpt_get_stream(kpt_context* c, void** s) {
+    if (!c || !s) return fail(KPT_ERR_INVALID, "null argument");
+    *s = (void*)c->stream;
+    return KPT_OK;
+}
+
+kpt_status kpt_launch_count(kpt_context* c, uint64_t* n) {
+    if (!c || !n) return fail(KPT_ERR_INVALID, "null argument");
+    *n = c->launches;
+    return KPT_OK;
+}
+
+}  // extern "C"

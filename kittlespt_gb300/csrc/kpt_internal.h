@@ -1,0 +1,59 @@
+// kpt_internal.h -- declarations shared by the library's translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "kpt_device.cuh"
+
+namespace kpt {
+
+constexpr int PATH_BLOCK = 128;    // threads per block of the path kernel
+constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
+
+// Everything one launch of the path kernel reads; passed by value.
+struct FrameParams {
+    SceneView scene;
+    SkyParams sky;
+    float4 inv_proj[4];        // rows of the inverse projection
+    float4 inv_view[3];        // rows 0-2 of the inverse view
+    float3 cam_pos;
+    int W, H;
+    int sample0, nsamples;     // reference frame indices sample0 .. sample0+nsamples-1
+    int max_depth, rng_order;
+    const float3* sun_radiance;
+    int* work_counter;         // zeroed before each launch
+    float4* acc;               // [H*W] running sum of samples (rgb), may be null
+    float4* albedo;            // [H*W] visible-surface albedo of the last sample, may be null
+    int4* first_hit;           // [H*W] (instance, triangle, t bits) of the last sample, may be null
+    float4* sample_out;        // [nsamples][H*W] per-sample radiance, may be null
+    unsigned long long* counters;   // [4] box tests, triangle tests, instance transforms, overflows
+};
+
+// Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
+__device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
+    float3 c0, c1;
+    if (n.z < -0.999805696f) {
+        c0 = make_float3(0.0f, -1.0f, 0.0f);
+        c1 = make_float3(-1.0f, 0.0f, 0.0f);
+    } else {
+        float a = __frcp_rn(xa(1.0f, n.z));
+        float b = xm(xm(-n.x, n.y), a);
+        c0 = make_float3(xs(1.0f, xm(xm(n.x, n.x), a)), b, -n.x);
+        c1 = make_float3(b, xs(1.0f, xm(xm(n.y, n.y), a)), -n.y);
+    }
+    return make_float3(xa(xa(xm(c0.x, l.x), xm(c1.x, l.y)), xm(n.x, l.z)),
+                       xa(xa(xm(c0.y, l.x), xm(c1.y, l.y)), xm(n.y, l.z)),
+                       xa(xa(xm(c0.z, l.x), xm(c1.z, l.y)), xm(n.z, l.z)));
+}
+
+// kernels (kpt_path.cu, fast maths)
+__global__ void k_path(FrameParams F);
+__global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
+__global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out);
+__global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, float tmin, float tmax,
+                        int* inst, int* tri, float* t, float2* uv, unsigned long long* counters);
+__global__ void k_occluded(SceneView s, int n, const float3* o, const float3* d, float tmin, const float* tmax,
+                           uint8_t* out, unsigned long long* counters);
+__global__ void k_trace_bounces(SceneView s, int n, const float3* o, const float3* d, int nbounces,
+                                int* inst, int* tri, float* t, unsigned long long* counters);
+
+}  // namespace kpt

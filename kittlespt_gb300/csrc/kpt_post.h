@@ -1,0 +1,29 @@
+// kpt_post.h -- post-chain kernels and their device state.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kpt {
+
+// Exposure state kept on the device between frames.
+struct ExposureState {
+    float avg_bin, avg_lum, adapted_lum, exposure_scalar, iso, shutter, pad0, pad1;
+};
+
+// Camera values read by the exposure program (ExposureValues, pod_types.hpp:9-33).
+struct ExposureIn {
+    float aperture, ev_comp, white_ev, black_ev;
+    float min_iso, max_iso, min_shutter, max_shutter;
+    float delta_ms, pad0, pad1, pad2;
+};
+
+__global__ void k_resolve(int npix, const float4* acc, const float4* albedo, float nsamples, float4* render);
+__global__ void k_histogram(int W, int H, const float4* render, const float* thresholds, unsigned long long* hist);
+__global__ void k_exposure(const unsigned long long* hist, ExposureState* st, ExposureIn in);
+__global__ void k_bloom_down(const float4* src, int sw, int sh, float4* dst, int dw, int dh, int karis_avg);
+__global__ void k_bloom_up(const float4* src, int sw, int sh, float4* dst, int dw, int dh, float blend);
+__global__ void k_tonemap(int W, int H, const float4* render, const float4* bloom, int use_bloom, float final_blend,
+                          const ExposureState* st, float fixed_scalar, int auto_exposure, float white_ev, float black_ev,
+                          float4* image);
+
+}  // namespace kpt

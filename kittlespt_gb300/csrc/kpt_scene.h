@@ -1,0 +1,50 @@
+// kpt_scene.h -- host-side scene build: BLAS and TLAS construction and the
+// packing of the device records (IEEE single precision, no contraction).
+#pragma once
+#include <cstdint>
+#include <vector>
+#include "kpt_device.cuh"
+
+namespace kpt {
+
+struct HostMesh {                    // one uploaded mesh (BLAS geometry)
+    std::vector<float> pos;          // 9 per triangle
+    std::vector<float> nrm;          // 9 per triangle
+    std::vector<float> uv;           // 6 per triangle
+    std::vector<int> material;       // 1 per triangle
+    // built
+    std::vector<BvhNode> nodes;      // interior nodes, local indices
+    std::vector<int> order;          // leaf order -> mesh triangle
+    int root = -1, leaf_first = 0, leaf_count = 0;
+    float lo[3], hi[3];              // object-space bounds (BLAS2::original_bounds)
+    int max_depth = 0;
+    int ntris() const { return (int)material.size(); }
+};
+
+struct HostInstance {
+    int mesh;
+    float model[16];                 // column-major
+    int material;                    // override or -1
+};
+
+// Binned SAH build of the reference (as_builder.cuh:110-261).
+void build_blas(HostMesh& m);
+
+// World bounds of an instance: the 8 transformed corners of the mesh bounds
+// (BLAS2::setTransform, blas.cuh:338-348).
+void instance_bounds(const HostMesh& m, const float* model, float* lo, float* hi);
+
+// Agglomerative TLAS (as_builder.cuh:312-392) converted to the device node
+// format.  Returns the nodes; root_leaf is set for a single instance.
+std::vector<BvhNode> build_tlas(const std::vector<float>& lo, const std::vector<float>& hi, int n,
+                                float* root_lo, float* root_hi, int* root_leaf, int* max_depth);
+
+// Closed-form 4x4 inverse of the reference (matrix_maths.cuh:304-354),
+// identity when |det| < 1e-6.  Column-major in and out.
+void inverse4(const float* m, float* out);
+
+// Local geometric normal of a triangle (Triangle constructor,
+// triangle.cuh:51-64) and its area (pod_types.hpp:143-146).
+void tri_normal_area(const float* p, const float* n, float* gn, float* area);
+
+}  // namespace kpt

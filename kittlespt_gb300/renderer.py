@@ -1,0 +1,283 @@
+"""Python mirror of KittlesPT::Renderer (KittlesPT/src/renderer.hpp:13-58)
+over the C ABI of libkpt.so.
+
+Method names follow the reference (snake_case), with the same argument
+meaning and error behaviour: setters on an index out of range return False
+(the reference's bool), getters raise IndexError (the reference asserts).
+``get_render_target`` replaces getRenderTargetTexture(GLuint): there is no
+graphics stack, so the display image is copied into a numpy array.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as K
+from . import scenes as S
+
+
+def _m16(m) -> np.ndarray:
+    """numpy M[row, col] (4x4) -> 16 floats column-major."""
+    a = np.asarray(m, np.float32)
+    if a.shape == (4, 4):
+        a = a.T
+    return np.ascontiguousarray(a.reshape(16), np.float32)
+
+
+def _mat(rec) -> K.Material:
+    m = K.Material()
+    for name, ctype in K.Material._fields_:
+        v = rec[name]
+        if name in ("albedo", "emission"):
+            getattr(m, name)[:] = [float(x) for x in v]
+        elif ctype is C.c_float:
+            setattr(m, name, float(v))
+        else:
+            setattr(m, name, int(v))
+    return m
+
+
+class Renderer:
+    """One GPU path tracer: scene, camera, settings, accumulation, post chain."""
+
+    def __init__(self, device: int = 0):
+        self._L = K.load()
+        self._ctx = C.c_void_p()
+        self._device = device
+        self._open = False
+
+    # -- lifetime (renderer.cu:22-53) ----------------------------------------
+    def initialize(self):
+        K.check(self._L.kpt_create(self._device, C.byref(self._ctx)))
+        self._open = True
+
+    def shutdown(self):
+        if self._open:
+            K.check(self._L.kpt_destroy(self._ctx))
+            self._open = False
+
+    def __enter__(self):
+        self.initialize()
+        return self
+
+    def __exit__(self, *exc):
+        self.shutdown()
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    # -- resolution (renderer.cu:55-101) -------------------------------------
+    def resize_resolution(self, width: int, height: int):
+        K.check(self._L.kpt_resize(self._ctx, width, height))
+        self.width, self.height = width, height
+
+    # -- scene (renderer.cu:356-436) -----------------------------------------
+    def load_scene(self, scene: S.Scene, commit: bool = True):
+        """Materials, meshes (BLAS built on upload), instances, camera,
+        environment, settings and exposure of a synthetic scene."""
+        L = self._L
+        K.check(L.kpt_clear_scene(self._ctx))
+        mats = (K.Material * len(scene.materials))(*[_mat(m) for m in scene.materials])
+        K.check(L.kpt_set_materials(self._ctx, len(scene.materials), mats))
+        for m in scene.meshes:
+            out = C.c_int()
+            K.check(L.kpt_upload_mesh(self._ctx, m.ntris, K.fptr(m.positions.reshape(-1)),
+                                      K.fptr(m.normals.reshape(-1)), K.fptr(m.uvs.reshape(-1)),
+                                      K.iptr(np.ascontiguousarray(m.material, np.int32)), C.byref(out)))
+        for inst in scene.instances:
+            out = C.c_int()
+            K.check(L.kpt_add_instance(self._ctx, inst.mesh, K.fptr(_m16(inst.model)), inst.material, C.byref(out)))
+        if commit:
+            K.check(L.kpt_commit_scene(self._ctx))
+        self.resize_resolution(scene.width, scene.height)
+        self.set_camera_inverse(scene.camera.inv_proj, scene.camera.inv_view)
+        self.set_procedural_environment_data(scene.env)
+        st = scene.settings
+        self.set_renderer_settings(max_depth=int(st["max_depth"]), bloom=bool(st["bloom"]),
+                                   karis=bool(st["karis"]), auto_exposure=bool(st["auto_exposure"]),
+                                   bloom_final_blend=float(st["bloom_final_blend"]),
+                                   bloom_internal_blend=float(st["bloom_internal_blend"]),
+                                   frame_delta_ms=float(st["frame_delta_ms"]))
+        self.set_exposure(scene.exposure)
+        self.scene = scene
+
+    def get_materials_count(self) -> int:
+        n = C.c_int()
+        K.check(self._L.kpt_counts(self._ctx, C.byref(n), None, None, None))
+        return n.value
+
+    def get_mesh_count(self) -> int:
+        """Instances: the reference's meshes (it copies one mesh per instance)."""
+        n = C.c_int()
+        K.check(self._L.kpt_counts(self._ctx, None, None, C.byref(n), None))
+        return n.value
+
+    def get_light_count(self) -> int:
+        n = C.c_int()
+        K.check(self._L.kpt_counts(self._ctx, None, None, None, C.byref(n)))
+        return n.value
+
+    # -- materials (renderer.cu:207-248) -------------------------------------
+    def set_material(self, index: int, material) -> bool:
+        rec = material if isinstance(material, K.Material) else _mat(material)
+        st = self._L.kpt_set_material(self._ctx, index, C.byref(rec))
+        if st == K.KPT_OK:
+            return True
+        if st == -1:
+            return False
+        K.check(st)
+
+    def get_material(self, index: int) -> np.ndarray:
+        m = K.Material()
+        st = self._L.kpt_get_material(self._ctx, index, C.byref(m))
+        if st == -1:
+            raise IndexError(f"material {index} out of range")
+        K.check(st)
+        out = np.zeros((), S.MATERIAL_DTYPE)
+        for name, _ in K.Material._fields_:
+            v = getattr(m, name)
+            out[name] = list(v) if name in ("albedo", "emission") else v
+        return out
+
+    # -- mesh transforms (renderer.cu:250-278) -------------------------------
+    def set_mesh_transform(self, index: int, model) -> bool:
+        st = self._L.kpt_set_instance_transform(self._ctx, index, K.fptr(_m16(model)))
+        if st == K.KPT_OK:
+            return True
+        if st == -1:
+            return False
+        K.check(st)
+
+    def get_mesh_transform(self, index: int) -> np.ndarray:
+        out = np.zeros(16, np.float32)
+        st = self._L.kpt_get_instance_transform(self._ctx, index, K.fptr(out))
+        if st == -1:
+            raise IndexError(f"mesh {index} out of range")
+        K.check(st)
+        return out.reshape(4, 4).T.copy()
+
+    # -- camera (renderer.cu:342-354) ----------------------------------------
+    def set_view(self, projection, view):
+        K.check(self._L.kpt_set_view(self._ctx, K.fptr(_m16(projection)), K.fptr(_m16(view))))
+
+    def set_camera_inverse(self, inv_projection, inv_view):
+        K.check(self._L.kpt_set_camera_inverse(self._ctx, K.fptr(_m16(inv_projection)), K.fptr(_m16(inv_view))))
+
+    # -- environment, settings, exposure (renderer.cu:290-334) ---------------
+    def set_procedural_environment_data(self, env):
+        e = K.Environment()
+        for name, _ in K.Environment._fields_:
+            if name == "rayleigh":
+                e.rayleigh[:] = [float(x) for x in env["rayleigh"]]
+            else:
+                setattr(e, name, float(env[name]))
+        K.check(self._L.kpt_set_environment(self._ctx, C.byref(e)))
+
+    def get_procedural_environment_data(self) -> K.Environment:
+        e = K.Environment()
+        K.check(self._L.kpt_get_environment(self._ctx, C.byref(e)))
+        return e
+
+    def set_renderer_settings(self, **kw):
+        s = K.Settings()
+        K.check(self._L.kpt_get_settings(self._ctx, C.byref(s)))
+        for k, v in kw.items():
+            setattr(s, k, type(getattr(s, k))(v))
+        K.check(self._L.kpt_set_settings(self._ctx, C.byref(s)))
+
+    def get_renderer_settings(self) -> K.Settings:
+        s = K.Settings()
+        K.check(self._L.kpt_get_settings(self._ctx, C.byref(s)))
+        return s
+
+    def set_exposure(self, exposure):
+        x = K.Exposure()
+        for name, _ in K.Exposure._fields_:
+            setattr(x, name, float(exposure[name]))
+        K.check(self._L.kpt_set_exposure(self._ctx, C.byref(x)))
+
+    def get_exposure(self) -> K.Exposure:
+        x = K.Exposure()
+        K.check(self._L.kpt_get_exposure(self._ctx, C.byref(x)))
+        return x
+
+    def reset_accumulation(self):
+        K.check(self._L.kpt_reset_accumulation(self._ctx))
+
+    # -- rendering (renderer.cu:103-195) -------------------------------------
+    def execute_rendering(self, delta_time_ms: float = 16.0, spp: int = 1):
+        K.check(self._L.kpt_render_frame(self._ctx, spp, delta_time_ms))
+
+    def synchronize(self):
+        K.check(self._L.kpt_synchronize(self._ctx))
+
+    def _read(self, fn, shape=None):
+        out = np.zeros((self.height, self.width, 4) if shape is None else shape, np.float32)
+        K.check(fn(self._ctx, K.fptr(out.reshape(-1))))
+        return out
+
+    def get_render_target(self) -> np.ndarray:
+        """Display image (AgX, non-linear sRGB), [H][W][4] float."""
+        return self._read(self._L.kpt_read_image)
+
+    def read_render(self) -> np.ndarray:
+        return self._read(self._L.kpt_read_render)
+
+    def read_accumulation(self) -> np.ndarray:
+        return self._read(self._L.kpt_read_accumulation)
+
+    def read_albedo(self) -> np.ndarray:
+        return self._read(self._L.kpt_read_albedo)
+
+    def read_histogram(self) -> np.ndarray:
+        out = np.zeros(256, np.uint64)
+        K.check(self._L.kpt_read_histogram(self._ctx, out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out
+
+    def stats(self) -> K.Stats:
+        s = K.Stats()
+        K.check(self._L.kpt_get_stats(self._ctx, C.byref(s)))
+        return s
+
+    def launch_count(self) -> int:
+        n = C.c_uint64()
+        K.check(self._L.kpt_launch_count(self._ctx, C.byref(n)))
+        return n.value
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        K.check(self._L.kpt_get_stream(self._ctx, C.byref(p)))
+        return p.value or 0
+
+    # -- device-pointer entry points (torch tensors or raw pointers) ---------
+    def render_samples_device(self, sample0: int, nsamples: int, radiance_ptr: int, first_hit_ptr: int = 0,
+                              albedo_ptr: int = 0):
+        K.check(self._L.kpt_render_samples_device(self._ctx, sample0, nsamples, radiance_ptr or None,
+                                                  first_hit_ptr or None, albedo_ptr or None))
+
+    def trace_device(self, n, o_ptr, d_ptr, inst_ptr, tri_ptr, t_ptr, uv_ptr=0, tmin=0.0, tmax=float("inf")):
+        K.check(self._L.kpt_trace_device(self._ctx, n, o_ptr, d_ptr, tmin, tmax, inst_ptr, tri_ptr, t_ptr,
+                                         uv_ptr or None))
+
+    def occluded_device(self, n, o_ptr, d_ptr, tmax_ptr, out_ptr, tmin=0.0):
+        K.check(self._L.kpt_occluded_device(self._ctx, n, o_ptr, d_ptr, tmin, tmax_ptr, out_ptr))
+
+    def trace_bounces_device(self, n, o_ptr, d_ptr, nbounces, inst_ptr, tri_ptr, t_ptr):
+        K.check(self._L.kpt_trace_bounces_device(self._ctx, n, o_ptr, d_ptr, nbounces, inst_ptr, tri_ptr, t_ptr))
+
+    def trace_bounces(self, o: np.ndarray, d: np.ndarray, nbounces: int):
+        n = int(o.shape[0])
+        inst = np.zeros((nbounces + 1) * n, np.int32)
+        tri = np.zeros_like(inst)
+        t = np.zeros((nbounces + 1) * n, np.float32)
+        K.check(self._L.kpt_trace_bounces(self._ctx, n, K.fptr(np.ascontiguousarray(o, np.float32).reshape(-1)),
+                                          K.fptr(np.ascontiguousarray(d, np.float32).reshape(-1)), nbounces,
+                                          K.iptr(inst), K.iptr(tri), K.fptr(t)))
+        return (inst.reshape(nbounces + 1, n), tri.reshape(nbounces + 1, n), t.reshape(nbounces + 1, n))
+
+    def sky_device(self, n, dirs_ptr, out_ptr):
+        K.check(self._L.kpt_sky_device(self._ctx, n, dirs_ptr, out_ptr))

@@ -1736,22 +1736,32 @@ void orc_occluded(void* hp, int n, const float* o, const float* d, float tmin, c
 }
 
 // Diffuse bounce chain of the traversal workload: from each closest hit, a
-// cosine-weighted ray about the geometric normal facing the incoming ray
-// (Frisvad basis), origin offset by 1e-3 along it; two draws of the
-// reference PCG sampler seeded with the ray index and the bounce.  Writes
+// cosine-weighted direction about the geometric normal facing the incoming
+// ray (Malley's method: a uniform point on the unit disk, rejection-sampled
+// from pairs of PCG draws, lifted to the hemisphere, then rotated by the
+// Frisvad basis), origin offset by 1e-3 along the normal.  The sampler is
+// seeded with 4 * ray index + bounce.  Only IEEE +, -, *, / and sqrt are
+// used, so every implementation produces the same rays.  Writes
 // (nbounces+1) x n hits.
+static f3 bounce_dir(uint32_t seed, f3 n) {
+    Sampler S; S.order = 0;
+    S.seed = seed;
+    float x = 0.0f, y = 0.0f, r2 = 0.0f;
+    for (int k = 0; k < 64; ++k) {
+        float u0 = S.get1D(), u1 = S.get1D();
+        float a = 2.0f * u0 - 1.0f, b = 2.0f * u1 - 1.0f;
+        float q = a * a + b * b;
+        if (q < 1.0f) { x = a; y = b; r2 = q; break; }
+    }
+    f3 l = {x, y, sqrtf(1.0f - r2)};
+    return mul(onb_frisvad(n), l);
+}
 static void bounce_ray(const Scene& s, const Hit& h, Ray& r, uint32_t idx, int b) {
     const Tri& tr = s.tris[h.prim];
     f3 n = normalize(xyz(mul(s.mesh_model[h.inst], F4(tr.local_gn, 0.0f))));
     if (dot(n, r.d) > 0.0f) n = -n;
     f3 p = point_at(r, h.t);
-    Sampler S; S.order = 0;
-    S.seed = idx * 4u + (uint32_t)b;
-    float u0 = S.get1D(), u1 = S.get1D();
-    float phi = 2.0f * PI * u0;
-    float ct = sqrtf(u1), st = sqrtf(1.0f - u1);
-    f3 l = {st * cosf(phi), st * sinf(phi), ct};
-    f3 w = mul(onb_frisvad(n), l);
+    f3 w = bounce_dir(idx * 4u + (uint32_t)b, n);
     r = make_ray(p + n * HIT_EPS, w);
 }
 void orc_trace_bounces(void* hp, int n, const float* o, const float* d, int nbounces,

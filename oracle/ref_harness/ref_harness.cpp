@@ -247,8 +247,8 @@ void ref_trace(void* hp, int n, const float* o, const float* d, float tmin, floa
 }
 
 // Diffuse bounce chain of the traversal workload (the same rule as the
-// oracle's orc_trace_bounces), built from the reference's own sampler,
-// basis and hemisphere sampling.
+// oracle's orc_trace_bounces: Malley's method with a rejection-sampled disk
+// point), built from the reference's own sampler, basis and traversal.
 void ref_trace_bounces(void* hp, int n, const float* o, const float* d, int nbounces,
                        int* prim, float* t, long long* counters, int nthreads) {
     RefScene& r = *(RefScene*)hp;
@@ -273,9 +273,15 @@ void ref_trace_bounces(void* hp, int n, const float* o, const float* d, int nbou
                 float3 p = ray.getPointAt(h.distance);
                 IndependentSampler S;
                 S.setSeed((uint32_t)i * 4u + (uint32_t)b);
-                float u0 = S.get1D();
-                float u1 = S.get1D();
-                float3 l = sampleCosineWeightedHemisphere(make_float2(u0, u1));
+                float x = 0.0f, y = 0.0f, r2 = 0.0f;
+                for (int q = 0; q < 64; ++q) {
+                    float u0 = S.get1D();
+                    float u1 = S.get1D();
+                    float a = 2.0f * u0 - 1.0f, c = 2.0f * u1 - 1.0f;
+                    float m = a * a + c * c;
+                    if (m < 1.0f) { x = a; y = c; r2 = m; break; }
+                }
+                float3 l = make_float3(x, y, sqrtf(1.0f - r2));
                 float3 w = generateONBFrisvad(nn) * l;
                 ray = Ray(p + nn * Constants::HIT_EPSILON, w);
             }
