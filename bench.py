@@ -201,12 +201,17 @@ def run_gpu(args):
     for _ in range(args.warmup):
         r.execute_rendering(16.0, SPP)
     r.synchronize()
-    st0 = r.stats()
-    l0 = r.launch_count()
-    barrier()
-    torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        # the sampler starts while one more untimed frame runs, so that its
+        # start-up does not overlap the timed region
+        r.execute_rendering(16.0, SPP)
+        time.sleep(1.0)
+        r.synchronize()
+        st0 = r.stats()
+        l0 = r.launch_count()
+        barrier()
+        torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             start.record(stream)
             for k in range(args.steps):
