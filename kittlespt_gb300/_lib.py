@@ -108,6 +108,7 @@ SIGNATURES = {
     "kpt_occluded_device": (_S, [_P, C.c_int, _P, _P, C.c_float, _P, _P]),
     "kpt_trace_bounces_device": (_S, [_P, C.c_int, _P, _P, C.c_int, _P, _P, _P]),
     "kpt_trace_bounces": (_S, [_P, C.c_int, _F, _F, C.c_int, _I, _I, _F]),
+    "kpt_trace_bounces_noalloc": (_S, [_P, C.c_int, _F, _F, C.c_int, _I, _I, _F]),
     "kpt_sky_device": (_S, [_P, C.c_int, _P, _P]),
     "kpt_enable_timing": (_S, [_P, C.c_int]),
     "kpt_path_kernel_ms": (_S, [_P, C.c_int, C.POINTER(C.c_float)]),

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -963,3 +964,87 @@ kpt_status kpt_launch_count(kpt_context* c, uint64_t* n) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Ray bounces without device allocation.
+//
+// kpt_trace_bounces stages the caller's host rays and hits in device buffers
+// it allocates with cudaMalloc on every call.  Some callers cannot do that:
+// a frame loop that must never stall (cudaMalloc and cudaFree can
+// synchronise the whole device), an application that reserves its device
+// memory up front and forbids later growth, or code that runs while another
+// library is capturing a CUDA graph on the device (allocation calls are not
+// allowed during capture).  kpt_trace_bounces_noalloc serves them: the
+// staging lives in one fixed array below, part of the library's device image,
+// so every GPU that loads libkpt.so holds these 8 MiB until the process exits.
+//
+// The array is shared by every call in the process and keeps the last call's
+// contents; nothing in it has to start at zero (the inputs are copied in and
+// the kernel writes every output slot).  Calls that overlap on the GPU --
+// from two threads, or on two contexts of one device at once -- race on it.
+// A call returns only after its results are in host memory, so calls made one
+// after another from one thread never overlap.
+
+namespace {
+
+constexpr size_t NOALLOC_BYTES = size_t(8) << 20;   // KPT_NOALLOC_STAGING_BYTES in kpt.h
+static __device__ __align__(256) unsigned char g_noalloc_staging[NOALLOC_BYTES];
+
+// Device address of the staging array, looked up once per device with that
+// device current (a host-side use of the symbol itself would not be a device
+// address).
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+kpt_status noalloc_staging(int device, unsigned char** out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return fail(KPT_ERR_INVALID, "device index too large");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_staging);
+        if (e != cudaSuccess || !p)
+            return fail(KPT_ERR_CUDA, std::string("cudaGetSymbolAddress(staging): ") + cudaGetErrorString(e));
+        g_noalloc_ptr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_ptr[device]);
+    return KPT_OK;
+}
+
+}  // namespace
+
+extern "C" kpt_status kpt_trace_bounces_noalloc(kpt_context* c, int n, const float* o, const float* d, int nb,
+                                                int32_t* inst, int32_t* tri, float* t) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    if (n < 0 || nb < 0 || (n > 0 && (!o || !d || !inst || !tri || !t)))
+        return fail(KPT_ERR_INVALID, "kpt_trace_bounces_noalloc: bad arguments");
+    if (!c->committed) return fail(KPT_ERR_STATE, "no committed scene");
+    if (c->tlas_dirty)   // rebuilding the TLAS could grow a device buffer
+        return fail(KPT_ERR_STATE, "kpt_trace_bounces_noalloc: instance transforms changed; render or trace once first");
+    const size_t per_ray = 24 + size_t(nb + 1) * 12;   // origin + direction in, (instance, triangle, t) per bounce out
+    if ((size_t)n * per_ray > NOALLOC_BYTES)
+        return fail(KPT_ERR_INVALID, "kpt_trace_bounces_noalloc: n * (24 + 12 * (nbounces + 1)) bytes exceed the "
+                                     "8 MiB staging array (KPT_NOALLOC_STAGING_BYTES)");
+    if (n == 0) return KPT_OK;
+    KPT_CUDA(cudaSetDevice(c->device));
+    unsigned char* base = nullptr;
+    kpt_status st = noalloc_staging(c->device, &base);
+    if (st != KPT_OK) return st;
+    const size_t nr = (size_t)n, no = nr * (nb + 1);
+    float* d_o = reinterpret_cast<float*>(base);          // 12 n bytes
+    float* d_d = d_o + 3 * nr;                              // 12 n bytes
+    int32_t* d_inst = reinterpret_cast<int32_t*>(d_d + 3 * nr);
+    int32_t* d_tri = d_inst + no;
+    float* d_t = reinterpret_cast<float*>(d_tri + no);
+    KPT_CUDA(cudaMemcpyAsync(d_o, o, 12 * nr, cudaMemcpyHostToDevice, c->stream));
+    KPT_CUDA(cudaMemcpyAsync(d_d, d, 12 * nr, cudaMemcpyHostToDevice, c->stream));
+    k_trace_bounces<<<trace_grid(c, (const void*)k_trace_bounces, n), TRACE_BLOCK, 0, c->stream>>>(
+        c->view, n, (const float3*)d_o, (const float3*)d_d, nb, d_inst, d_tri, d_t, c->counters.p);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    KPT_CUDA(cudaMemcpyAsync(inst, d_inst, 4 * no, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaMemcpyAsync(tri, d_tri, 4 * no, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaMemcpyAsync(t, d_t, 4 * no, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    return KPT_OK;
+}
