@@ -241,9 +241,9 @@ def run_gpu(args):
     value = samples_step * args.steps * world / (ms_max / 1e3) / 1e6
 
     # roofline of the path kernel: algorithmic bytes per launch / its time
-    boxes = (st1.box_tests - st0.box_tests) / args.steps
-    tris = (st1.tri_tests - st0.tri_tests) / args.steps
-    insts = (st1.inst_xforms - st0.inst_xforms) / args.steps
+    boxes = (st1.path_box_tests - st0.path_box_tests) / args.steps
+    tris = (st1.path_tri_tests - st0.path_tri_tests) / args.steps
+    insts = (st1.path_inst_xforms - st0.path_inst_xforms) / args.steps
     alg_bytes = 24.0 * boxes + 40.0 * tris + 64.0 * insts
     achieved = alg_bytes / (path_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
@@ -279,7 +279,7 @@ def run_gpu(args):
                "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
                           "instances": len(scene.instances), "triangles_expanded": scene.ntris_expanded,
                           "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "single"},
-               "roofline": {"bound": "hbm", "kernel": "k_path", "achieved": achieved, "peak": peak,
+               "roofline": {"bound": "hbm", "kernel": "k_paths", "achieved": achieved, "peak": peak,
                             "unit": "GB/s", "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                             "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": path_ms,
                             "launch_ms_source": path_src,

@@ -77,9 +77,12 @@ typedef struct kpt_exposure {
     float pad0, pad1;
 } kpt_exposure;
 
-/* Frame statistics of the last render (algorithmic work counted in-kernel). */
+/* Statistics since kpt_create (algorithmic work counted in-kernel: every ray
+ * of the path stage, then the path kernel's own share) and of the last
+ * exposure update. */
 typedef struct kpt_stats {
     uint64_t box_tests, tri_tests, inst_xforms, overflows;
+    uint64_t path_box_tests, path_tri_tests, path_inst_xforms;
     float avg_luminance, adapted_luminance, exposure_scalar, iso, shutter, avg_bin;
     int32_t frame_index, pad;
 } kpt_stats;

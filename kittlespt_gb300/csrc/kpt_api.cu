@@ -118,6 +118,10 @@ struct kpt_context {
     DBuf<float3> sun_radiance;
     DBuf<int> work_counter;
     cudaGraphExec_t graph_exec = nullptr;
+    // work buffers of the path stage
+    DBuf<PrimaryRec> primary;
+    DBuf<int> hit_list, hit_index, miss_list, counts;
+    DBuf<float4> pixel_sky, radiance, sky_queue;
 
     // timing of the path kernel inside the frame graph: a ring of event pairs
     static constexpr int EV_RING = 256;
@@ -188,13 +192,14 @@ kpt_status kpt_create(int device, kpt_context** out) {
     kpt_settings_default(&c->settings);
     kpt_exposure_default(&c->exposure);
     if (c->expo_state.ensure(1) != cudaSuccess || c->sun_radiance.ensure(1) != cudaSuccess ||
-        c->work_counter.ensure(1) != cudaSuccess || c->counters.ensure(4) != cudaSuccess ||
+        c->work_counter.ensure(1) != cudaSuccess || c->counters.ensure(8) != cudaSuccess ||
+        c->counts.ensure(4) != cudaSuccess ||
         c->hist.ensure(256) != cudaSuccess || c->thresholds.ensure(256) != cudaSuccess) {
         kpt_destroy(c);
         return fail(KPT_ERR_NOMEM, "kpt_create: device allocation failed");
     }
     cudaMemsetAsync(c->expo_state.p, 0, sizeof(ExposureState), c->stream);
-    cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
     *out = c;
     return KPT_OK;
 }
@@ -631,15 +636,57 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     F.max_depth = c->settings.max_depth;
     F.rng_order = c->settings.rng_order;
     F.sun_radiance = c->sun_radiance.p;
-    F.work_counter = c->work_counter.p;
     F.counters = c->counters.p;
+    F.primary = c->primary.p;
+    F.hit_list = c->hit_list.p;
+    F.hit_index = c->hit_index.p;
+    F.miss_list = c->miss_list.p;
+    F.counts = c->counts.p;
+    F.pixel_sky = c->pixel_sky.p;
+    F.radiance = c->radiance.p;
+    F.sky_queue = c->sky_queue.p;
     return F;
 }
 
-static int path_grid(kpt_context* c) {
+// Work buffers of the path stage for nsamples samples of every pixel
+// (allocated outside any stream capture).
+static kpt_status ensure_work(kpt_context* c, int nsamples) {
+    size_t np = (size_t)c->W * c->H, ns = np * (size_t)nsamples;
+    KPT_CUDA(c->primary.ensure(np));
+    KPT_CUDA(c->hit_list.ensure(np));
+    KPT_CUDA(c->hit_index.ensure(np));
+    KPT_CUDA(c->miss_list.ensure(np));
+    KPT_CUDA(c->pixel_sky.ensure(np));
+    KPT_CUDA(c->radiance.ensure(ns));
+    KPT_CUDA(c->sky_queue.ensure(2 * ns));
+    return KPT_OK;
+}
+
+static int persistent_grid(kpt_context* c, const void* kern) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_path, PATH_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PATH_BLOCK, 0);
     return std::max(1, per_sm) * c->sm_count;
+}
+
+// The path stage: camera rays, their sky, the paths, the queued sky and the
+// ordered accumulation of every sample.
+static void enqueue_paths(kpt_context* c, const FrameParams& F, bool timed) {
+    cudaStream_t s = c->stream;
+    const int np = c->W * c->H;
+    cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s);
+    k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
+    k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
+    k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky), PATH_BLOCK, 0, s>>>(F);
+    int slot = c->frames_rendered % kpt_context::EV_RING;
+    if (timed) {
+        c->last_slot = slot;
+        cudaEventRecordWithFlags(c->ev_start[slot], s, cudaEventRecordExternal);
+    }
+    k_paths<<<persistent_grid(c, (const void*)k_paths), PATH_BLOCK, 0, s>>>(F);
+    if (timed) cudaEventRecordWithFlags(c->ev_stop[slot], s, cudaEventRecordExternal);
+    k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue), PATH_BLOCK, 0, s>>>(F);
+    k_accumulate<<<(np + 255) / 256, 256, 0, s>>>(F);
+    c->launches += 6;
 }
 
 static kpt_status ready(kpt_context* c) {
@@ -675,15 +722,9 @@ static void update_thresholds(kpt_context* c) {
 static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
-    cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), s);
-    k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
-    int slot = c->frames_rendered % kpt_context::EV_RING;
-    c->last_slot = slot;
-    if (c->timing) cudaEventRecordWithFlags(c->ev_start[slot], s, cudaEventRecordExternal);
-    k_path<<<path_grid(c), PATH_BLOCK, 0, s>>>(F);
-    if (c->timing) cudaEventRecordWithFlags(c->ev_stop[slot], s, cudaEventRecordExternal);
+    enqueue_paths(c, F, c->timing);
     k_resolve<<<(np + 255) / 256, 256, 0, s>>>(np, c->acc.p, c->albedo.p, (float)total_samples, c->render.p);
-    c->launches += 3;
+    c->launches += 1;
     if (c->settings.auto_exposure) {
         ExposureIn in{};
         in.aperture = c->exposure.aperture;
@@ -734,6 +775,8 @@ kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
     if (st != KPT_OK) return st;
     if (spp <= 0) return fail(KPT_ERR_INVALID, "kpt_render_frame: spp must be positive");
     update_thresholds(c);
+    st = ensure_work(c, spp);
+    if (st != KPT_OK) return st;
     FrameParams F = frame_params(c, c->frame_index, spp);
     F.acc = c->acc.p;
     F.albedo = c->albedo.p;
@@ -787,15 +830,18 @@ kpt_status kpt_read_histogram(kpt_context* c, uint64_t* bins) { return read_buf(
 
 kpt_status kpt_get_stats(kpt_context* c, kpt_stats* st) {
     if (!c || !st) return fail(KPT_ERR_INVALID, "null argument");
-    unsigned long long cnt[4];
+    unsigned long long cnt[8];
     ExposureState es;
     KPT_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
     KPT_CUDA(cudaMemcpyAsync(&es, c->expo_state.p, sizeof es, cudaMemcpyDeviceToHost, c->stream));
     KPT_CUDA(cudaStreamSynchronize(c->stream));
-    st->box_tests = cnt[0];
-    st->tri_tests = cnt[1];
-    st->inst_xforms = cnt[2];
-    st->overflows = cnt[3];
+    st->box_tests = cnt[0] + cnt[4];
+    st->tri_tests = cnt[1] + cnt[5];
+    st->inst_xforms = cnt[2] + cnt[6];
+    st->overflows = cnt[3] + cnt[7];
+    st->path_box_tests = cnt[0];
+    st->path_tri_tests = cnt[1];
+    st->path_inst_xforms = cnt[2];
     st->avg_luminance = es.avg_lum;
     st->adapted_luminance = es.adapted_lum;
     st->exposure_scalar = es.exposure_scalar;
@@ -812,14 +858,13 @@ kpt_status kpt_render_samples_device(kpt_context* c, int sample0, int nsamples, 
     kpt_status st = ready(c);
     if (st != KPT_OK) return st;
     if (nsamples <= 0 || sample0 < 0) return fail(KPT_ERR_INVALID, "kpt_render_samples_device: bad sample range");
+    st = ensure_work(c, nsamples);
+    if (st != KPT_OK) return st;
     FrameParams F = frame_params(c, sample0, nsamples);
     F.sample_out = reinterpret_cast<float4*>(radiance);
     F.first_hit = reinterpret_cast<int4*>(first_hit);
     F.albedo = reinterpret_cast<float4*>(albedo);
-    KPT_CUDA(cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), c->stream));
-    k_sky_constants<<<1, 32, 0, c->stream>>>(F, c->sun_radiance.p);
-    k_path<<<path_grid(c), PATH_BLOCK, 0, c->stream>>>(F);
-    c->launches += 2;
+    enqueue_paths(c, F, false);
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;
 }

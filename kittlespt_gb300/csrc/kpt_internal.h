@@ -9,7 +9,14 @@ namespace kpt {
 constexpr int PATH_BLOCK = 128;    // threads per block of the path kernel
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
 
-// Everything one launch of the path kernel reads; passed by value.
+// Closest hit of a pixel's camera ray (the same for every sample: the
+// reference discards its filter jitter, kernels.cu:397-402).
+struct __align__(16) PrimaryRec {
+    float t, u, v;
+    int inst, tri, pad0, pad1, pad2;
+};
+
+// Everything the kernels of one frame read; passed by value.
 struct FrameParams {
     SceneView scene;
     SkyParams sky;
@@ -20,12 +27,21 @@ struct FrameParams {
     int sample0, nsamples;     // reference frame indices sample0 .. sample0+nsamples-1
     int max_depth, rng_order;
     const float3* sun_radiance;
-    int* work_counter;         // zeroed before each launch
     float4* acc;               // [H*W] running sum of samples (rgb), may be null
-    float4* albedo;            // [H*W] visible-surface albedo of the last sample, may be null
-    int4* first_hit;           // [H*W] (instance, triangle, t bits) of the last sample, may be null
-    float4* sample_out;        // [nsamples][H*W] per-sample radiance, may be null
-    unsigned long long* counters;   // [4] box tests, triangle tests, instance transforms, overflows
+    float4* albedo;            // [H*W] visible-surface albedo, may be null
+    int4* first_hit;           // [H*W] (instance, triangle, t bits, 0), may be null
+    float4* sample_out;        // [nsamples][H*W] clamped per-sample radiance, may be null
+    unsigned long long* counters;   // [8] box tests, triangle tests, instance transforms, overflows
+                                    //     of the path kernel, then the same for the primary rays
+    // work buffers of the frame
+    PrimaryRec* primary;       // [H*W]
+    int* hit_list;             // [H*W] pixels whose camera ray hits, compacted
+    int* hit_index;            // [H*W] position in hit_list, -1 for a miss
+    int* miss_list;            // [H*W] pixels whose camera ray misses, compacted
+    int* counts;               // [0] hits, [1] misses, [2] queued sky evaluations (zeroed per frame)
+    float4* pixel_sky;         // [H*W] sky radiance (times LeSun) of a missing camera ray
+    float4* radiance;          // [nsamples][hits] path radiance before clamping
+    float4* sky_queue;         // [2 per entry] (item bits, direction), (throughput, 0)
 };
 
 // Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
@@ -46,8 +62,13 @@ __device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
 }
 
 // kernels (kpt_path.cu, fast maths)
-__global__ void k_path(FrameParams F);
+__global__ void k_primary(FrameParams F);
+__global__ void k_primary_sky(FrameParams F);
+__global__ void k_paths(FrameParams F);
+__global__ void k_sky_queue(FrameParams F);
 __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
+// kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
+__global__ void k_accumulate(FrameParams F);
 __global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out);
 __global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, float tmin, float tmax,
                         int* inst, int* tri, float* t, float2* uv, unsigned long long* counters);

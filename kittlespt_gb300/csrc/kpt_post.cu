@@ -21,9 +21,36 @@
 //                exposure, AgX (film.cuh:79-194).
 // Every kernel but k_tonemap is bit-identical to the CPU oracle; k_tonemap
 // differs only through CUDA's log2f/exp2f/powf.
+#include "kpt_internal.h"
 #include "kpt_post.h"
 
 namespace kpt {
+
+// RGBSpectrum::clampOutput (color.cuh:295-302) of every sample, added to the
+// pixel's accumulation in sample order (integrator.cuh:406-415), as the
+// reference accumulates one frame per sample.  Samples of a pixel whose camera
+// ray misses all equal the pixel's sky radiance.
+__global__ void k_accumulate(FrameParams F) {
+    const int npix = F.W * F.H;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const int nhit = F.counts[0];
+    const int j = F.hit_index[p];
+    float4 acc = F.acc ? F.acc[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < F.nsamples; ++k) {
+        float4 L = j < 0 ? F.pixel_sky[p] : F.radiance[(size_t)k * nhit + j];
+        if (isnan(L.x) || isnan(L.y) || isnan(L.z) || isinf(L.x) || isinf(L.y) || isinf(L.z))
+            L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        else
+            L = make_float4(fmaxf(0.0f, fminf(L.x, 1.0e8f)), fmaxf(0.0f, fminf(L.y, 1.0e8f)),
+                            fmaxf(0.0f, fminf(L.z, 1.0e8f)), 0.0f);
+        acc.x = __fadd_rn(acc.x, L.x);
+        acc.y = __fadd_rn(acc.y, L.y);
+        acc.z = __fadd_rn(acc.z, L.z);
+        if (F.sample_out) F.sample_out[(size_t)k * npix + p] = L;
+    }
+    if (F.acc) F.acc[p] = make_float4(acc.x, acc.y, acc.z, 1.0f);
+}
 
 __device__ __forceinline__ float qbyte(float v) {  // floatToByte then byteToFloat (packing.cuh:10-18)
     v = fmaxf(0.0f, fminf(v, 1.0f));
