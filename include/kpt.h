@@ -80,9 +80,12 @@ typedef struct kpt_exposure {
 /* Statistics since kpt_create (algorithmic work counted in-kernel: every ray
  * of the path stage, then the path kernel's own share) and of the last
  * exposure update. */
+/* Traversal counters (cumulative since kpt_create): every query, then the
+ * path stage's extension rays (closest hit) and shadow rays (any hit). */
 typedef struct kpt_stats {
     uint64_t box_tests, tri_tests, inst_xforms, overflows;
     uint64_t path_box_tests, path_tri_tests, path_inst_xforms;
+    uint64_t shadow_box_tests, shadow_tri_tests, shadow_inst_xforms;
     float avg_luminance, adapted_luminance, exposure_scalar, iso, shutter, avg_bin;
     int32_t frame_index, pad;
 } kpt_stats;
@@ -211,10 +214,23 @@ kpt_status kpt_trace_bounces_noalloc(kpt_context* ctx, int n, const float* origi
  * (NishitaAtmosphereModel::sampleLi, shaders/atmosphere.cuh:132-223). */
 kpt_status kpt_sky_device(kpt_context* ctx, int n, const float* dirs, float* rgb);
 
-/* Device timing of the path kernel inside the frame graph (event-record
- * nodes around it).  kpt_path_kernel_ms sums the path-kernel time of the
- * last n frames (n <= 256); it synchronises the stream. */
+/* Device timing of the frame's stages inside the frame graph (event-record
+ * nodes between its launches).  kpt_stage_ms sums, per stage, the time of
+ * the last n frames rendered with timing on (n <= 32) into
+ * ms[KPT_STAGE_COUNT]; kpt_path_kernel_ms sums the path wave (shade, shadow
+ * and extension kernels).  Both synchronise the stream. */
+enum {
+    KPT_STAGE_CAMERA = 0,     /* sky constants, camera rays, their sky */
+    KPT_STAGE_SHADE = 1,      /* path vertices: emission, light sample, BSDF sample */
+    KPT_STAGE_SHADOW = 2,     /* shadow rays (any hit) */
+    KPT_STAGE_EXTEND = 3,     /* extension rays (closest hit) */
+    KPT_STAGE_SKY = 4,        /* sky of the paths that left the scene */
+    KPT_STAGE_ACCUMULATE = 5, /* clamped samples added in sample order */
+    KPT_STAGE_POST = 6,       /* resolve, histogram, exposure, bloom, tonemap */
+    KPT_STAGE_COUNT = 7
+};
 kpt_status kpt_enable_timing(kpt_context* ctx, int enable);
+kpt_status kpt_stage_ms(kpt_context* ctx, int nframes, float* ms);
 kpt_status kpt_path_kernel_ms(kpt_context* ctx, int nframes, float* total_ms);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time or

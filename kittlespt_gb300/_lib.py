@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libkpt.so")
 
 KPT_OK = 0
+STAGES = ("camera", "shade", "shadow", "extend", "sky", "accumulate", "post")   # KPT_STAGE_* order
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "invalid state", -4: "out of device memory",
           -5: "traversal stack overflow"}
 
@@ -55,7 +56,9 @@ class Exposure(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("box_tests", C.c_uint64), ("tri_tests", C.c_uint64), ("inst_xforms", C.c_uint64),
                 ("overflows", C.c_uint64), ("path_box_tests", C.c_uint64), ("path_tri_tests", C.c_uint64),
-                ("path_inst_xforms", C.c_uint64), ("avg_luminance", C.c_float), ("adapted_luminance", C.c_float),
+                ("path_inst_xforms", C.c_uint64), ("shadow_box_tests", C.c_uint64),
+                ("shadow_tri_tests", C.c_uint64), ("shadow_inst_xforms", C.c_uint64),
+                ("avg_luminance", C.c_float), ("adapted_luminance", C.c_float),
                 ("exposure_scalar", C.c_float), ("iso", C.c_float), ("shutter", C.c_float),
                 ("avg_bin", C.c_float), ("frame_index", C.c_int32), ("pad", C.c_int32)]
 
@@ -112,6 +115,7 @@ SIGNATURES = {
     "kpt_trace_bounces_noalloc": (_S, [_P, C.c_int, _F, _F, C.c_int, _I, _I, _F]),
     "kpt_sky_device": (_S, [_P, C.c_int, _P, _P]),
     "kpt_enable_timing": (_S, [_P, C.c_int]),
+    "kpt_stage_ms": (_S, [_P, C.c_int, C.POINTER(C.c_float)]),
     "kpt_path_kernel_ms": (_S, [_P, C.c_int, C.POINTER(C.c_float)]),
     "kpt_get_stream": (_S, [_P, C.POINTER(_P)]),
     "kpt_launch_count": (_S, [_P, C.POINTER(C.c_uint64)]),

@@ -2,9 +2,10 @@
 //
 // Host-side counterpart of KittlesPT::Renderer (renderer.cu) and
 // RendererResource (renderer_resource.cuh): the context owns every device
-// buffer; a frame is one CUDA graph (sky constants, path kernel, resolve,
-// histogram, exposure, bloom chain, tonemap) re-captured and updated in place
-// each frame, with no host synchronisation inside it.
+// buffer; a frame is one CUDA graph (sky constants, camera rays, the path
+// wave level by level, sky queue, accumulation, resolve, histogram, exposure,
+// bloom chain, tonemap) re-captured and updated in place each frame, with no
+// host synchronisation inside it.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -116,19 +117,32 @@ struct kpt_context {
     float thr_black = NAN, thr_white = NAN;
     DBuf<ExposureState> expo_state;
     DBuf<float3> sun_radiance;
-    DBuf<int> work_counter;
     cudaGraphExec_t graph_exec = nullptr;
     // work buffers of the path stage
-    DBuf<PrimaryRec> primary;
-    DBuf<int> hit_list, hit_index, miss_list, counts;
+    DBuf<PrimaryRec> primary, hits;
+    DBuf<int> hit_list, hit_index, miss_list, counts, level_counts;
     DBuf<float4> pixel_sky, radiance, sky_queue;
+    DBuf<PathRec> paths[2];
+    DBuf<ShadowRec> shadow;
+    int wave_cap = 0;
 
-    // timing of the path kernel inside the frame graph: a ring of event pairs
-    static constexpr int EV_RING = 256;
-    cudaEvent_t ev_start[EV_RING] = {}, ev_stop[EV_RING] = {};
+    // stage timing inside the frame graph: per frame, event-record nodes
+    // between the launches and the stage each interval belongs to
+    static constexpr int EV_FRAMES = 32, EV_PER_FRAME = 96;
+    struct TimedFrame {
+        cudaEvent_t ev[EV_PER_FRAME] = {};
+        unsigned char stage[EV_PER_FRAME] = {};
+        int n = 0;
+    };
+    TimedFrame tframes[EV_FRAMES];
     bool timing = false;
     int frames_rendered = 0, last_slot = 0;
+    TimedFrame* tf = nullptr;   // frame being captured with timing, else null
 };
+
+// Wave capacity: paths advanced together, level by level (208 B of work
+// buffers each; 2^25 paths hold a 1080p frame of 16 samples in one wave).
+static constexpr long long WAVE_CAP = 1LL << 25;
 
 extern "C" {
 
@@ -192,14 +206,14 @@ kpt_status kpt_create(int device, kpt_context** out) {
     kpt_settings_default(&c->settings);
     kpt_exposure_default(&c->exposure);
     if (c->expo_state.ensure(1) != cudaSuccess || c->sun_radiance.ensure(1) != cudaSuccess ||
-        c->work_counter.ensure(1) != cudaSuccess || c->counters.ensure(8) != cudaSuccess ||
+        c->counters.ensure(12) != cudaSuccess ||
         c->counts.ensure(4) != cudaSuccess ||
         c->hist.ensure(256) != cudaSuccess || c->thresholds.ensure(256) != cudaSuccess) {
         kpt_destroy(c);
         return fail(KPT_ERR_NOMEM, "kpt_create: device allocation failed");
     }
     cudaMemsetAsync(c->expo_state.p, 0, sizeof(ExposureState), c->stream);
-    cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 12 * sizeof(unsigned long long), c->stream);
     *out = c;
     return KPT_OK;
 }
@@ -209,17 +223,20 @@ kpt_status kpt_destroy(kpt_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-    for (int i = 0; i < kpt_context::EV_RING; ++i) {
-        if (c->ev_start[i]) cudaEventDestroy(c->ev_start[i]);
-        if (c->ev_stop[i]) cudaEventDestroy(c->ev_stop[i]);
-    }
+    for (auto& f : c->tframes)
+        for (cudaEvent_t e : f.ev)
+            if (e) cudaEventDestroy(e);
     c->d_nodes.release(); c->d_tlas.release(); c->d_tris.release(); c->d_shade.release();
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
     for (auto& m : c->mips) m.release();
     c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
-    c->sun_radiance.release(); c->work_counter.release();
+    c->sun_radiance.release();
+    c->primary.release(); c->hits.release(); c->hit_list.release(); c->hit_index.release();
+    c->miss_list.release(); c->counts.release(); c->level_counts.release(); c->pixel_sky.release();
+    c->radiance.release(); c->sky_queue.release(); c->paths[0].release(); c->paths[1].release();
+    c->shadow.release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return KPT_OK;
@@ -637,6 +654,12 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     F.rng_order = c->settings.rng_order;
     F.sun_radiance = c->sun_radiance.p;
     F.counters = c->counters.p;
+    F.paths[0] = c->paths[0].p;
+    F.paths[1] = c->paths[1].p;
+    F.hits = c->hits.p;
+    F.shadow = c->shadow.p;
+    F.level_counts = c->level_counts.p;
+    F.cap = c->wave_cap;
     F.primary = c->primary.p;
     F.hit_list = c->hit_list.p;
     F.hit_index = c->hit_index.p;
@@ -652,6 +675,14 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
 // (allocated outside any stream capture).
 static kpt_status ensure_work(kpt_context* c, int nsamples) {
     size_t np = (size_t)c->W * c->H, ns = np * (size_t)nsamples;
+    if (ns > (size_t)INT32_MAX) return fail(KPT_ERR_INVALID, "more than 2^31 - 1 samples in one call");
+    const int cap = (int)std::min<long long>((long long)ns, WAVE_CAP);
+    KPT_CUDA(c->paths[0].ensure(cap));
+    KPT_CUDA(c->paths[1].ensure(cap));
+    KPT_CUDA(c->hits.ensure(cap));
+    KPT_CUDA(c->shadow.ensure(cap));
+    KPT_CUDA(c->level_counts.ensure((size_t)LEVEL_WORDS * (c->settings.max_depth + 2)));
+    c->wave_cap = cap;
     KPT_CUDA(c->primary.ensure(np));
     KPT_CUDA(c->hit_list.ensure(np));
     KPT_CUDA(c->hit_index.ensure(np));
@@ -662,31 +693,58 @@ static kpt_status ensure_work(kpt_context* c, int nsamples) {
     return KPT_OK;
 }
 
-static int persistent_grid(kpt_context* c, const void* kern) {
+static int persistent_grid(kpt_context* c, const void* kern, int block) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PATH_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
     return std::max(1, per_sm) * c->sm_count;
 }
 
-// The path stage: camera rays, their sky, the paths, the queued sky and the
-// ordered accumulation of every sample.
-static void enqueue_paths(kpt_context* c, const FrameParams& F, bool timed) {
+// Closes the current timed interval of the frame being captured (if any) and
+// opens the next one for `stage`.
+static void stage_mark(kpt_context* c, int stage) {
+    kpt_context::TimedFrame* f = c->tf;
+    if (!f || f->n >= kpt_context::EV_PER_FRAME) return;
+    cudaEventRecordWithFlags(f->ev[f->n], c->stream, cudaEventRecordExternal);
+    f->stage[f->n] = (unsigned char)stage;
+    f->n++;
+}
+
+// The path stage: camera rays and their sky, then the wave(s) of paths level
+// by level, the queued sky and the ordered accumulation of every sample.
+static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
+    const int D = F.max_depth;
     cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s);
+    stage_mark(c, KPT_STAGE_CAMERA);
     k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
     k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
-    k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky), PATH_BLOCK, 0, s>>>(F);
-    int slot = c->frames_rendered % kpt_context::EV_RING;
-    if (timed) {
-        c->last_slot = slot;
-        cudaEventRecordWithFlags(c->ev_start[slot], s, cudaEventRecordExternal);
+    k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
+    c->launches += 3;
+    const int g_shade = persistent_grid(c, (const void*)k_shade, PATH_BLOCK);
+    const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
+    const int g_shd = persistent_grid(c, (const void*)k_shadow, TRACE_BLOCK);
+    // every pixel may hit: the last waves find no work when fewer do
+    const long long items = (long long)np * F.nsamples;
+    for (long long w0 = 0; w0 < items; w0 += F.cap) {
+        cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
+        for (int l = 0; l <= D; ++l) {
+            if (l > 0) {
+                stage_mark(c, KPT_STAGE_EXTEND);
+                k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
+            }
+            stage_mark(c, KPT_STAGE_SHADE);
+            k_shade<<<g_shade, PATH_BLOCK, 0, s>>>(F, l, w0);
+            stage_mark(c, KPT_STAGE_SHADOW);
+            k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
+            c->launches += l > 0 ? 3 : 2;
+        }
     }
-    k_paths<<<persistent_grid(c, (const void*)k_paths), PATH_BLOCK, 0, s>>>(F);
-    if (timed) cudaEventRecordWithFlags(c->ev_stop[slot], s, cudaEventRecordExternal);
-    k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue), PATH_BLOCK, 0, s>>>(F);
+    stage_mark(c, KPT_STAGE_SKY);
+    k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
+    stage_mark(c, KPT_STAGE_ACCUMULATE);
     k_accumulate<<<(np + 255) / 256, 256, 0, s>>>(F);
-    c->launches += 6;
+    c->launches += 2;
 }
 
 static kpt_status ready(kpt_context* c) {
@@ -722,7 +780,8 @@ static void update_thresholds(kpt_context* c) {
 static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
-    enqueue_paths(c, F, c->timing);
+    enqueue_paths(c, F);
+    stage_mark(c, KPT_STAGE_POST);
     k_resolve<<<(np + 255) / 256, 256, 0, s>>>(np, c->acc.p, c->albedo.p, (float)total_samples, c->render.p);
     c->launches += 1;
     if (c->settings.auto_exposure) {
@@ -768,6 +827,7 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
         c->W, c->H, c->render.p, bloom0, bloom0 != nullptr, c->settings.bloom_final_blend, c->expo_state.p, fixed_scalar,
         c->settings.auto_exposure, c->exposure.white_ev, c->exposure.black_ev, c->image.p);
     c->launches += 1;
+    stage_mark(c, KPT_STAGE_COUNT);   // end of the last interval
 }
 
 kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
@@ -783,9 +843,18 @@ kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
     F.first_hit = c->first_hit.p;
     int total = c->frame_index + spp;
     cudaGraph_t g = nullptr;
-    KPT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_frame(c, F, total, delta_ms);
-    KPT_CUDA(cudaStreamEndCapture(c->stream, &g));
+    if (c->timing) {
+        c->last_slot = c->frames_rendered % kpt_context::EV_FRAMES;
+        c->tf = &c->tframes[c->last_slot];
+        c->tf->n = 0;
+    }
+    cudaError_t ce = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        enqueue_frame(c, F, total, delta_ms);
+        ce = cudaStreamEndCapture(c->stream, &g);
+    }
+    c->tf = nullptr;
+    KPT_CUDA(ce);
     if (c->graph_exec) {
         cudaGraphExecUpdateResultInfo info;
         if (cudaGraphExecUpdate(c->graph_exec, g, &info) != cudaSuccess) {
@@ -830,18 +899,21 @@ kpt_status kpt_read_histogram(kpt_context* c, uint64_t* bins) { return read_buf(
 
 kpt_status kpt_get_stats(kpt_context* c, kpt_stats* st) {
     if (!c || !st) return fail(KPT_ERR_INVALID, "null argument");
-    unsigned long long cnt[8];
+    unsigned long long cnt[12];
     ExposureState es;
     KPT_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
     KPT_CUDA(cudaMemcpyAsync(&es, c->expo_state.p, sizeof es, cudaMemcpyDeviceToHost, c->stream));
     KPT_CUDA(cudaStreamSynchronize(c->stream));
-    st->box_tests = cnt[0] + cnt[4];
-    st->tri_tests = cnt[1] + cnt[5];
-    st->inst_xforms = cnt[2] + cnt[6];
-    st->overflows = cnt[3] + cnt[7];
+    st->box_tests = cnt[0] + cnt[4] + cnt[8];
+    st->tri_tests = cnt[1] + cnt[5] + cnt[9];
+    st->inst_xforms = cnt[2] + cnt[6] + cnt[10];
+    st->overflows = cnt[3] + cnt[7] + cnt[11];
     st->path_box_tests = cnt[0];
     st->path_tri_tests = cnt[1];
     st->path_inst_xforms = cnt[2];
+    st->shadow_box_tests = cnt[8];
+    st->shadow_tri_tests = cnt[9];
+    st->shadow_inst_xforms = cnt[10];
     st->avg_luminance = es.avg_lum;
     st->adapted_luminance = es.adapted_lum;
     st->exposure_scalar = es.exposure_scalar;
@@ -864,7 +936,7 @@ kpt_status kpt_render_samples_device(kpt_context* c, int sample0, int nsamples, 
     F.sample_out = reinterpret_cast<float4*>(radiance);
     F.first_hit = reinterpret_cast<int4*>(first_hit);
     F.albedo = reinterpret_cast<float4*>(albedo);
-    enqueue_paths(c, F, false);
+    enqueue_paths(c, F);
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;
 }
@@ -967,32 +1039,42 @@ kpt_status kpt_sky_device(kpt_context* c, int n, const float* dirs, float* rgb) 
 kpt_status kpt_enable_timing(kpt_context* c, int enable) {
     if (!c) return fail(KPT_ERR_INVALID, "null context");
     KPT_CUDA(cudaSetDevice(c->device));
-    if (enable && !c->ev_start[0]) {
-        for (int i = 0; i < kpt_context::EV_RING; ++i) {
-            KPT_CUDA(cudaEventCreate(&c->ev_start[i]));
-            KPT_CUDA(cudaEventCreate(&c->ev_stop[i]));
-        }
+    if (enable && !c->tframes[0].ev[0]) {
+        for (auto& f : c->tframes)
+            for (cudaEvent_t& e : f.ev) KPT_CUDA(cudaEventCreate(&e));
     }
     c->timing = enable != 0;
+    for (auto& f : c->tframes) f.n = 0;
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
     return KPT_OK;
 }
 
-kpt_status kpt_path_kernel_ms(kpt_context* c, int nframes, float* total_ms) {
-    if (!c || !total_ms || nframes <= 0 || nframes > kpt_context::EV_RING)
-        return fail(KPT_ERR_INVALID, "kpt_path_kernel_ms: bad arguments");
-    if (!c->timing) return fail(KPT_ERR_STATE, "kpt_path_kernel_ms: timing not enabled");
+kpt_status kpt_stage_ms(kpt_context* c, int nframes, float* ms) {
+    if (!c || !ms || nframes <= 0 || nframes > kpt_context::EV_FRAMES || nframes > c->frames_rendered)
+        return fail(KPT_ERR_INVALID, "kpt_stage_ms: bad arguments");
+    if (!c->timing) return fail(KPT_ERR_STATE, "kpt_stage_ms: timing not enabled");
     KPT_CUDA(cudaStreamSynchronize(c->stream));
-    // frames are numbered by frame_index / spp of the frame; walk back from the last one
-    double sum = 0.0;
-    int last = c->last_slot;
+    double sum[KPT_STAGE_COUNT] = {};
     for (int k = 0; k < nframes; ++k) {
-        int s = ((last - k) % kpt_context::EV_RING + kpt_context::EV_RING) % kpt_context::EV_RING;
-        float ms = 0.0f;
-        KPT_CUDA(cudaEventElapsedTime(&ms, c->ev_start[s], c->ev_stop[s]));
-        sum += ms;
+        int slot = ((c->last_slot - k) % kpt_context::EV_FRAMES + kpt_context::EV_FRAMES) % kpt_context::EV_FRAMES;
+        const kpt_context::TimedFrame& f = c->tframes[slot];
+        if (f.n == 0) return fail(KPT_ERR_STATE, "kpt_stage_ms: a frame was rendered without timing");
+        for (int i = 0; i + 1 < f.n; ++i) {
+            float t = 0.0f;
+            KPT_CUDA(cudaEventElapsedTime(&t, f.ev[i], f.ev[i + 1]));
+            if (f.stage[i] < KPT_STAGE_COUNT) sum[f.stage[i]] += t;
+        }
     }
-    *total_ms = (float)sum;
+    for (int i = 0; i < KPT_STAGE_COUNT; ++i) ms[i] = (float)sum[i];
+    return KPT_OK;
+}
+
+kpt_status kpt_path_kernel_ms(kpt_context* c, int nframes, float* total_ms) {
+    if (!total_ms) return fail(KPT_ERR_INVALID, "kpt_path_kernel_ms: bad arguments");
+    float ms[KPT_STAGE_COUNT];
+    kpt_status st = kpt_stage_ms(c, nframes, ms);
+    if (st != KPT_OK) return st;
+    *total_ms = ms[KPT_STAGE_SHADE] + ms[KPT_STAGE_SHADOW] + ms[KPT_STAGE_EXTEND];
     return KPT_OK;
 }
 

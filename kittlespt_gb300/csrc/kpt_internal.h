@@ -6,8 +6,9 @@
 
 namespace kpt {
 
-constexpr int PATH_BLOCK = 128;    // threads per block of the path kernel
+constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
+constexpr int TRACE_MIN_BLOCKS = 8;   // ray kernels: at most 64 registers, 32 warps per SM
 
 // Closest hit of a pixel's camera ray (the same for every sample: the
 // reference discards its filter jitter, kernels.cu:397-402).
@@ -15,6 +16,25 @@ struct __align__(16) PrimaryRec {
     float t, u, v;
     int inst, tri, pad0, pad1, pad2;
 };
+
+// A path between two levels of the wave (64 B): the ray of its next segment,
+// its throughput, the vertex it leaves and the sampler state.
+struct __align__(16) PathRec {
+    float4 o_pb;        // ray origin, BSDF pdf of the sampled direction (MIS at a light hit)
+    float4 d_seed;      // ray direction, sampler seed (bits)
+    float4 beta_item;   // throughput, work item (bits)
+    float4 prev;        // previous vertex, unused
+};
+
+// A shadow ray and the radiance it carries if nothing blocks it (48 B).
+struct __align__(16) ShadowRec {
+    float4 o_tmax;      // origin, tmax
+    float4 d_item;      // direction, work item (bits)
+    float4 contrib;     // radiance added to the item when unoccluded
+};
+
+// per-level counters of a wave, LEVEL_WORDS ints per level
+constexpr int LEVEL_WORDS = 4;   // paths entering the level, sun shadow rays, light shadow rays, unused
 
 // Everything the kernels of one frame read; passed by value.
 struct FrameParams {
@@ -31,8 +51,8 @@ struct FrameParams {
     float4* albedo;            // [H*W] visible-surface albedo, may be null
     int4* first_hit;           // [H*W] (instance, triangle, t bits, 0), may be null
     float4* sample_out;        // [nsamples][H*W] clamped per-sample radiance, may be null
-    unsigned long long* counters;   // [8] box tests, triangle tests, instance transforms, overflows
-                                    //     of the path kernel, then the same for the primary rays
+    unsigned long long* counters;   // [12] box tests, triangle tests, instance transforms, overflows
+                                    //      of the extension rays, the camera rays, the shadow rays
     // work buffers of the frame
     PrimaryRec* primary;       // [H*W]
     int* hit_list;             // [H*W] pixels whose camera ray hits, compacted
@@ -42,6 +62,12 @@ struct FrameParams {
     float4* pixel_sky;         // [H*W] sky radiance (times LeSun) of a missing camera ray
     float4* radiance;          // [nsamples][hits] path radiance before clamping
     float4* sky_queue;         // [2 per entry] (item bits, direction), (throughput, 0)
+    // the wave: up to `cap` paths advanced one level per launch triple
+    PathRec* paths[2];         // [cap] paths entering even / odd levels
+    PrimaryRec* hits;          // [cap] closest hits of the paths entering a level
+    ShadowRec* shadow;         // [cap] shadow rays of a level: sun rays from the front, light rays from the back
+    int* level_counts;         // [LEVEL_WORDS * (max_depth + 2)] zeroed per wave
+    int cap;
 };
 
 // Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
@@ -64,7 +90,9 @@ __device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
 // kernels (kpt_path.cu, fast maths)
 __global__ void k_primary(FrameParams F);
 __global__ void k_primary_sky(FrameParams F);
-__global__ void k_paths(FrameParams F);
+__global__ void k_shade(FrameParams F, int level, long long wave0);
+__global__ void k_extend(FrameParams F, int level);
+__global__ void k_shadow(FrameParams F, int level);
 __global__ void k_sky_queue(FrameParams F);
 __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order

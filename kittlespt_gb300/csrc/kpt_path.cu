@@ -5,7 +5,7 @@
 // One frame of the plain method follows the megakernel
 // computePathTraceSamplesMegaKernel (shaders/kernels.cu:385-451) and
 // Integrator::Li (shaders/integrator.cuh:241-402), reorganised for the GPU
-// without changing any sample:
+// as a wavefront without changing any sample:
 //   * k_primary traces each pixel's camera ray once per frame.  The camera
 //     ray is the same for every sample (the reference computes a filter
 //     jitter and then discards it, kernels.cu:397-402), so its closest hit,
@@ -13,10 +13,12 @@
 //     per-pixel quantities;
 //   * k_primary_sky evaluates the sky once per missing pixel, over a
 //     compacted list (every lane runs the same 16x8-step march);
-//   * k_paths is persistent: each thread walks work items (sample, hit
-//     pixel) round-robin and advances one bounce per loop iteration, taking a
-//     new item as soon as its path ends, so lanes stay busy while paths of
-//     different lengths finish;
+//   * the work items (sample, hit pixel) then advance as a wave, one path
+//     vertex per level: k_shade shades every path entering the level and
+//     writes its light sample's shadow ray and its continuation to compacted
+//     queues, k_shadow traces the shadow rays, k_extend the continuations.
+//     The ray kernels hold no shading state, so they run at full occupancy,
+//     and every lane of a warp runs the same kind of query;
 //   * a path whose ray leaves the scene does not march the sky inline: it
 //     queues (item, direction, throughput) and k_sky_queue evaluates the queue
 //     coherently, adding sky * throughput to the sample -- a miss is always the
@@ -228,196 +230,260 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary_sky(FrameParams F) {
 }
 
 // ---------------------------------------------------------------------------
-// paths
+// paths: one wave of work items advanced level by level
 
-struct PathState {
-    float3 o, d, beta, L, prev_pos;
-    float p_b;
-    uint32_t seed;
-    int depth, item, pixel;
-    bool any_ns;
-};
+// Appends the lanes of a (possibly divergent) warp that reach this call to a
+// list with one atomic; returns each lane's slot.
+__device__ __forceinline__ int group_append(int* counter) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+    return g.shfl(base, 0) + (int)g.thread_rank();
+}
 
-// One bounce of Integrator::Li (integrator.cuh:266-399) with LeSun, sampleLdSun
-// (:147-186), sampleLd (:188-220) and russianRoulette (maths/sampling.cuh:19-31).
-// Returns false when the path has ended.
-__device__ __forceinline__ bool bounce(const FrameParams& F, PathState& ps, TraceStats& st, int* stack) {
+// Shadow ray of Integrator::unoccluded (integrator.cuh:124-131): from the
+// offset surface point towards `target`, stopping 0.11 short of it.
+__device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si, float3 target, float3 contrib,
+                                            int item, int* counter, bool from_back) {
+    float3 o = si.backface ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+    float3 d = normalize(target - o);
+    float tmax = length(target - o) - 0.11f;
+    int j = group_append(counter);
+    if (from_back) j = F.cap - 1 - j;
+    ShadowRec r;
+    r.o_tmax = make_float4(o.x, o.y, o.z, tmax);
+    r.d_item = make_float4(d.x, d.y, d.z, __int_as_float(item));
+    r.contrib = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
+    F.shadow[j] = r;
+}
+
+// One vertex of Integrator::Li (integrator.cuh:266-399) for every path of the
+// wave entering `level`: emission with its MIS weight, one light sample --
+// LeSun / sampleLdSun (:135-186) or sampleLd (:188-220) -- whose shadow ray
+// goes to k_shadow with the radiance it would add, the BSDF sample and
+// russianRoulette (maths/sampling.cuh:19-31).  A path whose ray left the
+// scene goes to the sky queue.  The radiance of each item is kept in
+// `radiance` and receives its terms in the reference's order: this vertex's
+// emission here, its light sample in k_shadow, the next vertex's terms at the
+// next level, the sky last.  Level 0 starts the paths of items
+// wave0 .. wave0+cap-1 from the camera-ray hits of k_primary.
+__global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, long long wave0) {
     const SceneView& s = F.scene;
     const SkyParams& P = F.sky;
     const int order = F.rng_order;
     const int nl = s.nlights;
-    Sampler S;
-    S.seed = ps.seed + (uint32_t)ps.depth;
-    const bool first = ps.depth == 0;
-    int inst, tri;
-    float t, u, v;
+    const bool first = level == 0;
+    int n;
     if (first) {
-        const PrimaryRec pr = F.primary[ps.pixel];
-        inst = pr.inst; tri = pr.tri; t = pr.t; u = pr.u; v = pr.v;
+        const long long left = (long long)F.counts[0] * F.nsamples - wave0;
+        n = (int)(left < 0 ? 0 : (left < F.cap ? left : F.cap));
     } else {
-        Hit h = trace_closest(s, make_xray(ps.o, ps.d), 0.0f, __int_as_float(0x7f800000), st, stack);
-        inst = h.inst; tri = h.tri; t = h.t; u = h.u; v = h.v;
+        n = F.level_counts[LEVEL_WORDS * level];
     }
-    if (inst < 0) {
-        // the sky is evaluated by k_sky_queue; the path ends here.  The lanes
-        // that missed together take consecutive queue slots with one atomic.
-        cg::coalesced_group g = cg::coalesced_threads();
-        int q0 = 0;
-        if (g.thread_rank() == 0) q0 = atomicAdd(F.counts + 2, (int)g.size());
-        int q = g.shfl(q0, 0) + (int)g.thread_rank();
-        F.sky_queue[2 * (size_t)q] = make_float4(__int_as_float(ps.item), ps.d.x, ps.d.y, ps.d.z);
-        F.sky_queue[2 * (size_t)q + 1] = make_float4(ps.beta.x, ps.beta.y, ps.beta.z, 0.0f);
-        return false;
-    }
-    Surf si = surface_at(s, inst, tri, t, u, v, ps.o, ps.d);
-    float3 Le = make_float3(0.0f, 0.0f, 0.0f);
-    if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
-    if (nonzero(Le)) {
-        float w_l = 1.0f;
-        if (si.light >= 0 && !first) {
-            const LightRec& lt = s.lights[si.light];
-            float pmf = 1.0f / (float)nl;
-            float dist = length(si.pos - ps.prev_pos);
-            float cosl = AbsDot(normalize(si.pos - ps.prev_pos), si.ng);
-            float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
-            w_l = Sqr(ps.p_b) / (Sqr(ps.p_b) + Sqr(lpdf));
-        }
-        ps.L = ps.L + Le * w_l * ps.beta;
-    }
-    Bsdf bsdf = bsdf_at(s, si);
-    if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);   // demodulate (bsdf.cuh:286-288)
-    if (ps.any_ns && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
-    const float3 wo = -ps.d;
-    if (!(bsdf.alpha < 0.001f)) {
-        if (S.get1D() < 0.5f) {
-            // sampleLdSun: jittered point on the sun disc at 1 AU
-            float3 Ld = make_float3(0.0f, 0.0f, 0.0f);
-            const float dsun = 149.597e9f;
-            float3 sun_pos = P.sun_dir * dsun;
-            float3 off;
-            if (order == 0) {
-                float2 a = S.get2D(0);
-                float b = S.get1D();
-                off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
-            } else {
-                float b = S.get1D();
-                float2 a = S.get2D(1);
-                off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
-            }
-            float3 target = sun_pos + (off * P.sun_radius_m);
-            float3 fcos = bsdf.f(wo, P.sun_dir) * fmaxf(0.0f, dot(P.sun_dir, (si.backface ? -1.0f : 1.0f) * si.ng));
-            const float3 sun_rad = *F.sun_radiance;
-            if (nonzero(fcos) && nonzero(sun_rad) && unoccluded(F, si, target, st, stack)) {
-                float area = PI_F * Sqr(P.sun_radius_m);
-                float3 sn = normalize(target - sun_pos), wi = normalize(target - si.pos);
-                float th = AbsDot(sn, -wi);
-                float pdf = (1.0f / area) / (th / Sqr(dsun));
-                Ld = (fcos * sun_rad * 6.0e5f) / pdf;
-            }
-            ps.L = ps.L + Ld * ps.beta / 0.5f;
-        } else {
-            // sampleLd: uniform light pick, uniform point on the triangle
-            float3 Ld = make_float3(0.0f, 0.0f, 0.0f);
-            float X = S.get1D();
-            if (nl >= 1) {
-                int li = min((int)(X * (float)nl), nl - 1);
-                const LightRec& lt = s.lights[li];
-                float prob = 1.0f / (float)nl;
-                float2 uu = S.get2D(order);
-                const InstRec& lir = s.inst[lt.inst];
-                float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
-                float bx, by;
-                if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
-                else { by = uu.y / 2.0f; bx = uu.x - by; }
-                float bz = 1.0f - bx - by;
-                float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
-                                         bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
-                float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
-                p = row3(model, p, 1.0f);
-                float3 gn = row3(model, lt.gn, 0.0f);
-                float pdf = 1.0f / lt.tri_area;
-                pdf *= Sqr(length(p - si.pos));
-                pdf /= AbsDot(normalize(p - si.pos), gn);
-                float3 wi = normalize(p - si.pos);
-                float3 Lem = emission_of(s, lt.material, luv);
-                if (!(pdf <= 0.0f || !nonzero(Lem))) {
-                    float3 fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
-                    if (nonzero(fcos) && unoccluded(F, si, p, st, stack)) {
-                        float p_l = prob * pdf;
-                        float pb = bsdf.pdf(wo, wi);
-                        float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
-                        Ld = (Lem * fcos * w_l) / p_l;
-                    }
-                }
-            }
-            ps.L = ps.L + Ld * ps.beta / (1.0f - 0.5f);
-        }
-    }
-    if (ps.depth++ == F.max_depth) return false;
-    float2 uu, X;
-    if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
-    else { X = S.get2D(1); uu = S.get2D(1); }
-    BsdfSample bs = bsdf.sample(wo, uu, X);
-    if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) return false;
-    ps.beta = ps.beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
-    ps.p_b = bsdf.pdf(wo, bs.wi);
-    ps.any_ns = true;
-    ps.prev_pos = si.pos;
-    ps.o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
-    ps.d = bs.wi;
-    float mx = fmaxf(ps.beta.x, fmaxf(ps.beta.y, ps.beta.z));
-    if (mx < 1.0f && ps.depth > 1) {
-        float q = fmaxf(0.0f, 1.0f - mx);
-        if (S.get1D() < q) {
-            ps.seed = S.seed;
-            return false;
-        }
-        ps.beta = ps.beta / (1.0f - q);
-    }
-    ps.seed = S.seed;
-    return nonzero(ps.beta);   // while (throughput) (integrator.cuh:266)
-}
-
-__global__ void __launch_bounds__(PATH_BLOCK) k_paths(FrameParams F) {
-    int stack[STACK_WORDS];
-    TraceStats st = {0, 0, 0, 0};
-    const int nhit = F.counts[0];
-    const long long total = (long long)nhit * F.nsamples;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    long long next = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    PathState ps;
-    ps.item = -1;
-    for (;;) {
-        if (ps.item < 0) {
-            if (next >= total) break;
-            const int item = (int)next;
-            next += stride;
+    const PathRec* in = F.paths[level & 1];
+    PathRec* out = F.paths[(level + 1) & 1];
+    int* here = F.level_counts + LEVEL_WORDS * level;
+    int* next = F.level_counts + LEVEL_WORDS * (level + 1);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float3 o, d, beta, prev, L;
+        float p_b;
+        uint32_t seed;
+        int item;
+        PrimaryRec h;
+        if (first) {
+            const int nhit = F.counts[0];
+            item = (int)(wave0 + i);
             const int k = item / nhit;
             const int p = F.hit_list[item - k * nhit];
             const int x = p % F.W, y = p / F.W;
-            Sampler S;
-            S.init(x, y, F.W, F.sample0 + k);
-            S.get1D();   // BoxFilter::sample, result discarded (kernels.cu:397-402)
-            S.get1D();
+            Sampler S0;
+            S0.init(x, y, F.W, F.sample0 + k);
+            S0.get1D();   // BoxFilter::sample, result discarded (kernels.cu:397-402)
+            S0.get1D();
             XRay r = camera_ray(F, x, y);
-            ps.o = r.o;
-            ps.d = r.d;
-            ps.beta = make_float3(1.0f, 1.0f, 1.0f);
-            ps.L = make_float3(0.0f, 0.0f, 0.0f);
-            ps.prev_pos = make_float3(0.0f, 0.0f, 0.0f);
-            ps.p_b = 1.0f;
-            ps.seed = S.seed;
-            ps.depth = 0;
-            ps.item = item;
-            ps.pixel = p;
-            ps.any_ns = false;
+            o = r.o;
+            d = r.d;
+            beta = make_float3(1.0f, 1.0f, 1.0f);
+            prev = make_float3(0.0f, 0.0f, 0.0f);
+            L = make_float3(0.0f, 0.0f, 0.0f);
+            p_b = 1.0f;
+            seed = S0.seed;
+            h = F.primary[p];
+        } else {
+            const PathRec pr = in[i];
+            o = make_float3(pr.o_pb.x, pr.o_pb.y, pr.o_pb.z);
+            p_b = pr.o_pb.w;
+            d = make_float3(pr.d_seed.x, pr.d_seed.y, pr.d_seed.z);
+            seed = __float_as_uint(pr.d_seed.w);
+            beta = make_float3(pr.beta_item.x, pr.beta_item.y, pr.beta_item.z);
+            item = __float_as_int(pr.beta_item.w);
+            prev = make_float3(pr.prev.x, pr.prev.y, pr.prev.z);
+            h = F.hits[i];
+            const float4 l4 = F.radiance[item];
+            L = make_float3(l4.x, l4.y, l4.z);
         }
-        if (!bounce(F, ps, st, stack)) {
-            F.radiance[ps.item] = make_float4(ps.L.x, ps.L.y, ps.L.z, 0.0f);
-            ps.item = -1;
+        if (h.inst < 0) {
+            // the sky is evaluated by k_sky_queue; the path ends here
+            const int q = group_append(F.counts + 2);
+            F.sky_queue[2 * (size_t)q] = make_float4(__int_as_float(item), d.x, d.y, d.z);
+            F.sky_queue[2 * (size_t)q + 1] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+            continue;
         }
+        Sampler S;
+        S.seed = seed + (uint32_t)level;
+        Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
+        float3 Le = make_float3(0.0f, 0.0f, 0.0f);
+        if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
+        if (nonzero(Le)) {
+            float w_l = 1.0f;
+            if (si.light >= 0 && !first) {
+                const LightRec& lt = s.lights[si.light];
+                float pmf = 1.0f / (float)nl;
+                float dist = length(si.pos - prev);
+                float cosl = AbsDot(normalize(si.pos - prev), si.ng);
+                float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
+                w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
+            }
+            L = L + Le * w_l * beta;
+        }
+        Bsdf bsdf = bsdf_at(s, si);
+        if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);   // demodulate (bsdf.cuh:286-288)
+        if (!first && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
+        const float3 wo = -d;
+        if (!(bsdf.alpha < 0.001f)) {
+            if (S.get1D() < 0.5f) {
+                // sampleLdSun: jittered point on the sun disc at 1 AU
+                const float dsun = 149.597e9f;
+                float3 sun_pos = P.sun_dir * dsun;
+                float3 off;
+                if (order == 0) {
+                    float2 a = S.get2D(0);
+                    float b = S.get1D();
+                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                } else {
+                    float b = S.get1D();
+                    float2 a = S.get2D(1);
+                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                }
+                float3 target = sun_pos + (off * P.sun_radius_m);
+                float3 fcos = bsdf.f(wo, P.sun_dir) * fmaxf(0.0f, dot(P.sun_dir, (si.backface ? -1.0f : 1.0f) * si.ng));
+                const float3 sun_rad = *F.sun_radiance;
+                if (nonzero(fcos) && nonzero(sun_rad)) {
+                    float area = PI_F * Sqr(P.sun_radius_m);
+                    float3 sn = normalize(target - sun_pos), wi = normalize(target - si.pos);
+                    float th = AbsDot(sn, -wi);
+                    float pdf = (1.0f / area) / (th / Sqr(dsun));
+                    float3 Ld = (fcos * sun_rad * 6.0e5f) / pdf;
+                    float3 c = Ld * beta / 0.5f;
+                    if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                        emit_shadow(F, si, target, c, item, here + 1, false);
+                }
+            } else {
+                // sampleLd: uniform light pick, uniform point on the triangle
+                float X = S.get1D();
+                if (nl >= 1) {
+                    int li = min((int)(X * (float)nl), nl - 1);
+                    const LightRec& lt = s.lights[li];
+                    float prob = 1.0f / (float)nl;
+                    float2 uu = S.get2D(order);
+                    const InstRec& lir = s.inst[lt.inst];
+                    float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
+                    float bx, by;
+                    if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
+                    else { by = uu.y / 2.0f; bx = uu.x - by; }
+                    float bz = 1.0f - bx - by;
+                    float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
+                                             bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
+                    float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
+                    p = row3(model, p, 1.0f);
+                    float3 gn = row3(model, lt.gn, 0.0f);
+                    float pdf = 1.0f / lt.tri_area;
+                    pdf *= Sqr(length(p - si.pos));
+                    pdf /= AbsDot(normalize(p - si.pos), gn);
+                    float3 wi = normalize(p - si.pos);
+                    float3 Lem = emission_of(s, lt.material, luv);
+                    if (!(pdf <= 0.0f || !nonzero(Lem))) {
+                        float3 fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
+                        if (nonzero(fcos)) {
+                            float p_l = prob * pdf;
+                            float pb = bsdf.pdf(wo, wi);
+                            float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
+                            float3 Ld = (Lem * fcos * w_l) / p_l;
+                            float3 c = Ld * beta / (1.0f - 0.5f);
+                            if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                                emit_shadow(F, si, p, c, item, here + 2, true);
+                        }
+                    }
+                }
+            }
+        }
+        F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
+        if (level == F.max_depth) continue;
+        float2 uu, X;
+        if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
+        else { X = S.get2D(1); uu = S.get2D(1); }
+        BsdfSample bs = bsdf.sample(wo, uu, X);
+        if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) continue;
+        beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
+        p_b = bsdf.pdf(wo, bs.wi);
+        o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+        float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
+        if (mx < 1.0f && level >= 1) {
+            float q = fmaxf(0.0f, 1.0f - mx);
+            if (S.get1D() < q) continue;
+            beta = beta / (1.0f - q);
+        }
+        if (!nonzero(beta)) continue;   // while (throughput) (integrator.cuh:266)
+        const int j = group_append(next);
+        PathRec pr;
+        pr.o_pb = make_float4(o.x, o.y, o.z, p_b);
+        pr.d_seed = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, __uint_as_float(S.seed));
+        pr.beta_item = make_float4(beta.x, beta.y, beta.z, __int_as_float(item));
+        pr.prev = make_float4(si.pos.x, si.pos.y, si.pos.z, 0.0f);
+        out[j] = pr;
+    }
+}
+
+// Closest hits of the paths entering `level` (1 .. max_depth).
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_extend(FrameParams F, int level) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    const int n = F.level_counts[LEVEL_WORDS * level];
+    const PathRec* in = F.paths[level & 1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = in[i].o_pb, b = in[i].d_seed;
+        Hit h = trace_closest(F.scene, make_xray(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)), 0.0f,
+                              __int_as_float(0x7f800000), st, stack);
+        PrimaryRec r;
+        r.t = h.t;
+        r.u = h.u;
+        r.v = h.v;
+        r.inst = h.inst;
+        r.tri = h.tri;
+        r.pad0 = r.pad1 = r.pad2 = 0;
+        F.hits[i] = r;
     }
     flush_stats(st, F.counters);
+}
+
+// Shadow rays of `level`: an unoccluded ray adds its radiance to its item.
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameParams F, int level) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    const int* lc = F.level_counts + LEVEL_WORDS * level;
+    const int nsun = lc[1], n = nsun + lc[2];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int j = i < nsun ? i : F.cap - 1 - (i - nsun);
+        const float4 a = F.shadow[j].o_tmax, b = F.shadow[j].d_item;
+        if (!trace_any(F.scene, make_xray(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)), 0.0f, a.w, st,
+                       stack)) {
+            const int item = __float_as_int(b.w);
+            const float4 c = F.shadow[j].contrib;
+            const float4 L = F.radiance[item];
+            F.radiance[item] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+        }
+    }
+    flush_stats(st, F.counters + 8);
 }
 
 // sky * throughput of every path that left the scene, added to its sample
