@@ -121,6 +121,7 @@ struct kpt_context {
     // work buffers of the path stage
     DBuf<PrimaryRec> primary, hits;
     DBuf<int> hit_list, hit_index, miss_list, counts, level_counts;
+    DBuf<int> fetch;   // queue counter of the ray-batch entry points
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2];
     DBuf<ShadowRec> shadow;
@@ -207,7 +208,7 @@ kpt_status kpt_create(int device, kpt_context** out) {
     kpt_exposure_default(&c->exposure);
     if (c->expo_state.ensure(1) != cudaSuccess || c->sun_radiance.ensure(1) != cudaSuccess ||
         c->counters.ensure(12) != cudaSuccess ||
-        c->counts.ensure(4) != cudaSuccess ||
+        c->counts.ensure(4) != cudaSuccess || c->fetch.ensure(1) != cudaSuccess ||
         c->hist.ensure(256) != cudaSuccess || c->thresholds.ensure(256) != cudaSuccess) {
         kpt_destroy(c);
         return fail(KPT_ERR_NOMEM, "kpt_create: device allocation failed");
@@ -236,7 +237,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->primary.release(); c->hits.release(); c->hit_list.release(); c->hit_index.release();
     c->miss_list.release(); c->counts.release(); c->level_counts.release(); c->pixel_sky.release();
     c->radiance.release(); c->sky_queue.release(); c->paths[0].release(); c->paths[1].release();
-    c->shadow.release();
+    c->shadow.release(); c->fetch.release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return KPT_OK;
@@ -962,8 +963,10 @@ kpt_status kpt_trace_device(kpt_context* c, int n, const float* o, const float* 
     if (st != KPT_OK) return st;
     if (n < 0 || (n > 0 && (!o || !d || !inst || !tri || !t))) return fail(KPT_ERR_INVALID, "kpt_trace_device: bad arguments");
     if (n == 0) return KPT_OK;
+    KPT_CUDA(cudaMemsetAsync(c->fetch.p, 0, sizeof(int), c->stream));
     k_trace<<<trace_grid(c, (const void*)k_trace, n), TRACE_BLOCK, 0, c->stream>>>(
-        c->view, n, (const float3*)o, (const float3*)d, tmin, tmax, inst, tri, t, (float2*)uv, c->counters.p);
+        c->view, n, (const float3*)o, (const float3*)d, tmin, tmax, inst, tri, t, (float2*)uv, c->fetch.p,
+        c->counters.p);
     c->launches += 1;
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;
@@ -975,8 +978,9 @@ kpt_status kpt_occluded_device(kpt_context* c, int n, const float* o, const floa
     if (st != KPT_OK) return st;
     if (n < 0 || (n > 0 && (!o || !d || !tmax || !out))) return fail(KPT_ERR_INVALID, "kpt_occluded_device: bad arguments");
     if (n == 0) return KPT_OK;
+    KPT_CUDA(cudaMemsetAsync(c->fetch.p, 0, sizeof(int), c->stream));
     k_occluded<<<trace_grid(c, (const void*)k_occluded, n), TRACE_BLOCK, 0, c->stream>>>(
-        c->view, n, (const float3*)o, (const float3*)d, tmin, tmax, out, c->counters.p);
+        c->view, n, (const float3*)o, (const float3*)d, tmin, tmax, out, c->fetch.p, c->counters.p);
     c->launches += 1;
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;

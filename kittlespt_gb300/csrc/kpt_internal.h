@@ -33,8 +33,10 @@ struct __align__(16) ShadowRec {
     float4 contrib;     // radiance added to the item when unoccluded
 };
 
-// per-level counters of a wave, LEVEL_WORDS ints per level
-constexpr int LEVEL_WORDS = 4;   // paths entering the level, sun shadow rays, light shadow rays, unused
+// per-level counters of a wave, LEVEL_WORDS ints per level: paths entering
+// the level, sun shadow rays, light shadow rays, then the fetch counters of
+// the extension and shadow ray queues
+constexpr int LEVEL_WORDS = 8;
 
 // Everything the kernels of one frame read; passed by value.
 struct FrameParams {
@@ -99,9 +101,9 @@ __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
 __global__ void k_accumulate(FrameParams F);
 __global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out);
 __global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, float tmin, float tmax,
-                        int* inst, int* tri, float* t, float2* uv, unsigned long long* counters);
+                        int* inst, int* tri, float* t, float2* uv, int* next, unsigned long long* counters);
 __global__ void k_occluded(SceneView s, int n, const float3* o, const float3* d, float tmin, const float* tmax,
-                           uint8_t* out, unsigned long long* counters);
+                           uint8_t* out, int* next, unsigned long long* counters);
 __global__ void k_trace_bounces(SceneView s, int n, const float3* o, const float3* d, int nbounces,
                                 int* inst, int* tri, float* t, unsigned long long* counters);
 

@@ -29,13 +29,9 @@
 //     recomputes per hit and per light sample (interaction.cu:20, light.cu:36).
 // k_accumulate (kpt_post.cu) then clamps each sample and adds them per pixel
 // in sample order, as the reference's frame-by-frame accumulation does.
-#include <cooperative_groups.h>
-
 #include "kpt_internal.h"
 #include "kpt_shade.cuh"
 #include "kpt_trace.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace kpt {
 
@@ -445,15 +441,17 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, 
 }
 
 // Closest hits of the paths entering `level` (1 .. max_depth).
-__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_extend(FrameParams F, int level) {
-    int stack[STACK_WORDS];
-    TraceStats st = {0, 0, 0, 0};
-    const int n = F.level_counts[LEVEL_WORDS * level];
-    const PathRec* in = F.paths[level & 1];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+struct ExtendQueue {
+    const PathRec* in;
+    PrimaryRec* out;
+    __device__ __forceinline__ void ray(int i, float3& o, float3& d, float& tmin, float& tmax) const {
         const float4 a = in[i].o_pb, b = in[i].d_seed;
-        Hit h = trace_closest(F.scene, make_xray(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)), 0.0f,
-                              __int_as_float(0x7f800000), st, stack);
+        o = make_float3(a.x, a.y, a.z);
+        d = make_float3(b.x, b.y, b.z);
+        tmin = 0.0f;
+        tmax = __int_as_float(0x7f800000);
+    }
+    __device__ __forceinline__ void closest(int i, const Hit& h) const {
         PrimaryRec r;
         r.t = h.t;
         r.u = h.u;
@@ -461,28 +459,52 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_extend(FrameP
         r.inst = h.inst;
         r.tri = h.tri;
         r.pad0 = r.pad1 = r.pad2 = 0;
-        F.hits[i] = r;
+        out[i] = r;
     }
+    __device__ __forceinline__ void any(int, bool) const {}
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_extend(FrameParams F, int level) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    int* lc = F.level_counts + LEVEL_WORDS * level;
+    ExtendQueue q{F.paths[level & 1], F.hits};
+    trace_queue<false>(F.scene, lc[0], lc + 3, q, st, stack);
     flush_stats(st, F.counters);
 }
 
-// Shadow rays of `level`: an unoccluded ray adds its radiance to its item.
+// Shadow rays of `level` (sun rays from the front of the buffer, light rays
+// from the back): an unoccluded ray adds its radiance to its item.
+struct ShadowQueue {
+    const ShadowRec* rec;
+    float4* radiance;
+    int nsun, cap;
+    __device__ __forceinline__ int slot(int i) const { return i < nsun ? i : cap - 1 - (i - nsun); }
+    __device__ __forceinline__ void ray(int i, float3& o, float3& d, float& tmin, float& tmax) const {
+        const int j = slot(i);
+        const float4 a = rec[j].o_tmax, b = rec[j].d_item;
+        o = make_float3(a.x, a.y, a.z);
+        d = make_float3(b.x, b.y, b.z);
+        tmin = 0.0f;
+        tmax = a.w;
+    }
+    __device__ __forceinline__ void closest(int, const Hit&) const {}
+    __device__ __forceinline__ void any(int i, bool occluded) const {
+        if (occluded) return;
+        const int j = slot(i);
+        const int item = __float_as_int(rec[j].d_item.w);
+        const float4 c = rec[j].contrib;
+        const float4 L = radiance[item];
+        radiance[item] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+    }
+};
+
 __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameParams F, int level) {
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
-    const int* lc = F.level_counts + LEVEL_WORDS * level;
-    const int nsun = lc[1], n = nsun + lc[2];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int j = i < nsun ? i : F.cap - 1 - (i - nsun);
-        const float4 a = F.shadow[j].o_tmax, b = F.shadow[j].d_item;
-        if (!trace_any(F.scene, make_xray(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z)), 0.0f, a.w, st,
-                       stack)) {
-            const int item = __float_as_int(b.w);
-            const float4 c = F.shadow[j].contrib;
-            const float4 L = F.radiance[item];
-            F.radiance[item] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
-        }
-    }
+    int* lc = F.level_counts + LEVEL_WORDS * level;
+    ShadowQueue q{F.shadow, F.radiance, lc[1], F.cap};
+    trace_queue<true>(F.scene, lc[1] + lc[2], lc + 4, q, st, stack);
     flush_stats(st, F.counters + 8);
 }
 
@@ -517,30 +539,49 @@ __global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out) {
 // ---------------------------------------------------------------------------
 // ray queries
 
-// Closest hit for a batch of rays, one ray per thread per step.
-__global__ void __launch_bounds__(TRACE_BLOCK) k_trace(SceneView s, int n, const float3* o, const float3* d,
-                                                       float tmin, float tmax, int* inst, int* tri, float* t,
-                                                       float2* uv, unsigned long long* counters) {
-    int stack[STACK_WORDS];
-    TraceStats st = {0, 0, 0, 0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        XRay r = make_xray(o[i], d[i]);
-        Hit h = trace_closest(s, r, tmin, tmax, st, stack);
+// Closest hit / occlusion for a batch of rays.
+struct RayBatch {
+    const float3 *o, *d;
+    float tmin, tmax;
+    const float* tmax_each;
+    int *inst, *tri;
+    float* t;
+    float2* uv;
+    uint8_t* occ;
+    __device__ __forceinline__ void ray(int i, float3& ro, float3& rd, float& t0, float& t1) const {
+        ro = o[i];
+        rd = d[i];
+        t0 = tmin;
+        t1 = tmax_each ? tmax_each[i] : tmax;
+    }
+    __device__ __forceinline__ void closest(int i, const Hit& h) const {
         inst[i] = h.inst;
         tri[i] = h.tri;
         t[i] = h.t;
         if (uv) uv[i] = make_float2(h.u, h.v);
     }
+    __device__ __forceinline__ void any(int i, bool occluded) const { occ[i] = occluded ? 1 : 0; }
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_trace(SceneView s, int n, const float3* o,
+                                                                       const float3* d, float tmin, float tmax,
+                                                                       int* inst, int* tri, float* t, float2* uv,
+                                                                       int* next, unsigned long long* counters) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    RayBatch q{o, d, tmin, tmax, nullptr, inst, tri, t, uv, nullptr};
+    trace_queue<false>(s, n, next, q, st, stack);
     flush_stats(st, counters);
 }
 
-__global__ void __launch_bounds__(TRACE_BLOCK) k_occluded(SceneView s, int n, const float3* o, const float3* d,
-                                                          float tmin, const float* tmax, uint8_t* out,
-                                                          unsigned long long* counters) {
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_occluded(SceneView s, int n, const float3* o,
+                                                                          const float3* d, float tmin,
+                                                                          const float* tmax, uint8_t* out, int* next,
+                                                                          unsigned long long* counters) {
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        out[i] = trace_any(s, make_xray(o[i], d[i]), tmin, tmax[i], st, stack) ? 1 : 0;
+    RayBatch q{o, d, tmin, 0.0f, tmax, nullptr, nullptr, nullptr, nullptr, out};
+    trace_queue<true>(s, n, next, q, st, stack);
     flush_stats(st, counters);
 }
 

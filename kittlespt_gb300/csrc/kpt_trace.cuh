@@ -14,9 +14,13 @@
 //     undefined behaviour); a ray that would overflow stops and is counted
 //     in `overflow`.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "kpt_device.cuh"
 
 namespace kpt {
+
+namespace cg = cooperative_groups;
 
 struct XRay { float3 o, d, inv; };
 
@@ -312,6 +316,145 @@ __device__ __forceinline__ bool trace_any(const SceneView& s, const XRay& r, flo
         }
     }
     return false;
+}
+
+// ---------------------------------------------------------------------------
+// Queue traversal: a persistent warp walks a queue of rays.  Each lane runs
+// its own ray and, when the ray is done, fetches the next queue entry (one
+// atomic per group of lanes fetching together), so no lane waits for the
+// longest ray of its warp.  One loop iteration is one step of a lane's ray --
+// a node (TLAS and BLAS share the node format), one triangle, entering or
+// leaving an instance -- so lanes at different depths of the two levels keep
+// issuing together.  The visiting order and culling are those of
+// trace_closest / trace_any above (the BLAS keeps its local closest hit and
+// culls against it, and is merged into the ray's closest hit when left), so
+// every result is identical to theirs.
+//
+// Src supplies the queue:  void ray(int i, float3& o, float3& d, float& tmin, float& tmax);
+//                          void closest(int i, const Hit& h);   (ANY == false)
+//                          void any(int i, bool occluded);      (ANY == true)
+template <bool ANY, class Src>
+__device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next, Src& src, TraceStats& st,
+                                            int* stack) {
+    const float INF = __int_as_float(0x7f800000);
+    XRay w, r;               // world ray; current ray (object space inside an instance)
+    float tmin = 0.0f, tmax0 = INF;
+    Hit best, loc;           // closest hit of the ray; of the instance being traversed
+    int ray = -1;            // queue entry, -1: fetch the next one
+    int inst = -1;           // instance being traversed, -1: in the TLAS
+    int base = 0;            // stack height when the instance was entered
+    int sp = 0;
+    int first = 0, count = 0;   // triangles of the leaf being tested
+    best.t = loc.t = INF;
+    best.inst = best.tri = loc.inst = loc.tri = -1;
+    best.u = best.v = loc.u = loc.v = 0.0f;
+    for (;;) {
+        if (ray < 0) {
+            cg::coalesced_group g = cg::coalesced_threads();
+            int b = 0;
+            if (g.thread_rank() == 0) b = atomicAdd(next, (int)g.size());
+            ray = g.shfl(b, 0) + (int)g.thread_rank();
+            if (ray >= n) break;
+            float3 o, d;
+            src.ray(ray, o, d, tmin, tmax0);
+            w = make_xray(o, d);
+            r = w;
+            best.t = INF;
+            best.inst = best.tri = -1;
+            best.u = best.v = 0.0f;
+            inst = -1;
+            sp = 0;
+            count = 0;
+            float te;
+            st.box_tests++;
+            if (s.ninst > 0 &&
+                slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
+                stack[sp++] = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
+        } else if (count > 0) {
+            // one triangle of the leaf (BLAS2::intersect / intersectP leaf loop)
+            float u, v;
+            int lid;
+            const float tmx = ANY ? tmax0 : fminf(tmax0, loc.t);
+            float t = tri_test(s.tris + 3 * (size_t)first, r, tmin, tmx, &u, &v, &lid);
+            st.tri_tests++;
+            ++first;
+            --count;
+            if (ANY) {
+                if (t < INF) {
+                    src.any(ray, true);
+                    ray = -1;
+                }
+            } else if (t < loc.t) {
+                loc.t = t;
+                loc.tri = lid;
+                loc.u = u;
+                loc.v = v;
+            }
+        } else if (inst >= 0 && sp == base) {
+            // leaving the instance: merge its closest hit (tlas.cu:116-121)
+            if (!ANY && loc.t < best.t) {
+                best = loc;
+                best.inst = inst;
+            }
+            inst = -1;
+            r = w;
+        } else if (sp == 0) {
+            if (ANY) src.any(ray, false);
+            else src.closest(ray, best);
+            ray = -1;
+        } else {
+            const int e = stack[--sp];
+            if (e >= 0) {
+                // interior node of the TLAS or of the instance's BLAS
+                const bool in_blas = inst >= 0;
+                const BvhNode nd = load_node((in_blas ? s.nodes : s.tlas) + e);
+                const float cull = ANY ? INF : (in_blas ? loc.t : best.t);
+                const float tmx = (ANY || !in_blas) ? tmax0 : fminf(tmax0, loc.t);
+                bool h1, h2;
+                float t1, t2;
+                node_slabs(nd, r, tmin, tmx, &h1, &t1, &h2, &t2);
+                st.box_tests += 2;
+                const bool p1 = h1 && t1 < cull, p2 = h2 && t2 < cull;
+                if (in_blas ? (sp - base + 2 > BLAS_STACK) : (sp + 2 > TLAS_STACK)) {
+                    st.overflow++;
+                    sp = in_blas ? base : 0;   // the reference's stack would overflow: end this level
+                } else {
+                    const int c1 = nd.d.y ? (in_blas ? leaf_code(e, 0) : -nd.d.x - 1) : nd.d.x;
+                    const int c2 = nd.d.w ? (in_blas ? leaf_code(e, 1) : -nd.d.z - 1) : nd.d.z;
+                    // near child pushed last, popped first
+                    const bool far1 = t1 > t2;
+                    const int ca = far1 ? c1 : c2, cb = far1 ? c2 : c1;
+                    const bool pa = far1 ? p1 : p2, pb = far1 ? p2 : p1;
+                    if (pa) stack[sp++] = ca;
+                    if (pb) stack[sp++] = cb;
+                }
+            } else if (inst < 0) {
+                // entering an instance (TLAS leaf): object-space ray (Ray::transform)
+                inst = -e - 1;
+                const InstRec& ir = s.inst[inst];
+                const MeshRec m = s.meshes[ir.mesh];
+                const float4 inv[3] = {__ldg(&ir.inv[0]), __ldg(&ir.inv[1]), __ldg(&ir.inv[2])};
+                r = transform_xray(w, inv);
+                st.inst_xforms++;
+                base = sp;
+                loc.t = INF;
+                loc.tri = -1;
+                loc.u = loc.v = 0.0f;
+                if (m.node_root < 0) {
+                    first = m.leaf_first;
+                    count = m.leaf_count;
+                } else {
+                    stack[sp++] = m.node_root;
+                }
+            } else {
+                // BLAS leaf: its triangle range is read back from the parent node
+                const int c = -e - 1;
+                const int4 d = __ldg(reinterpret_cast<const int4*>(s.nodes + (c >> 1)) + 3);
+                first = (c & 1) ? d.z : d.x;
+                count = (c & 1) ? d.w : d.y;
+            }
+        }
+    }
 }
 
 }  // namespace kpt
