@@ -304,6 +304,22 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile_case(spec):
+    """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
+    small case that ncu captures of single kernels run on."""
+    from kittlespt_gb300 import scenes as S
+    from kittlespt_gb300.renderer import Renderer
+    w, h, spp = (int(v) for v in spec.lower().split("x"))
+    r = Renderer(0)
+    r.initialize()
+    r.load_scene(S.scene_full(w, h, spp, DEPTH))
+    for _ in range(2):
+        r.execute_rendering(16.0, spp)
+    r.synchronize()
+    print(f"profile case {w}x{h}x{spp}: {r.stats().box_tests} box tests", file=sys.stderr)
+    r.shutdown()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,7 +327,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
+                    help="render two frames of the full scene at this size and exit (small case for ncu)")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -8,7 +8,12 @@ namespace kpt {
 
 constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
-constexpr int TRACE_MIN_BLOCKS = 8;   // ray kernels: at most 64 registers, 32 warps per SM
+#ifndef KPT_TRACE_MIN_BLOCKS
+#define KPT_TRACE_MIN_BLOCKS 8
+#endif
+// ray kernels: resident blocks of TRACE_BLOCK threads per SM the register
+// budget must allow (8: at most 64 registers, 32 warps per SM)
+constexpr int TRACE_MIN_BLOCKS = KPT_TRACE_MIN_BLOCKS;
 
 // Closest hit of a pixel's camera ray (the same for every sample: the
 // reference discards its filter jitter, kernels.cu:397-402).
