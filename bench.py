@@ -248,6 +248,10 @@ def run_gpu(args):
     def delta(field):
         return (getattr(st1, field) - getattr(st0, field)) / args.steps
     kern = {"extend": ("k_extend", "path"), "shadow": ("k_shadow", "shadow")}
+    # DRAM bytes per frame of each ray kernel from one ncu capture of the
+    # 960x540x8 case (profiles/wave_kernels_960x540x8.md), scaled by samples
+    # (x8) to this workload
+    traffic = {"extend": (246.9e6 + 20.9e6) * 8.0, "shadow": (131.3e6 + 1.6e6) * 8.0}
     dom = max(kern, key=lambda k: stage_ms[k])
     kname, pre = kern[dom]
     boxes, tris, insts = delta(pre + "_box_tests"), delta(pre + "_tri_tests"), delta(pre + "_inst_xforms")
@@ -288,7 +292,10 @@ def run_gpu(args):
                           "instances": len(scene.instances), "triangles_expanded": scene.ntris_expanded,
                           "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "single"},
                "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
-                            "unit": "GB/s", "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic[dom],
+                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per frame, "
+                                              "960x540x8 capture scaled x8 by samples",
+                            "peak_kind": peak_kind,
                             "algorithmic_bytes_per_frame": alg_bytes, "kernel_ms_per_frame": launch_ms,
                             "launches_per_frame": DEPTH + (1 if dom == "shadow" else 0),
                             "kernel_ms_source": "event-record nodes around each launch in the frame graph",
