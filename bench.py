@@ -33,6 +33,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -175,7 +177,6 @@ def run_reference(args):
 
 
 def run_gpu(args):
-    import numpy as np
     import torch
 
     rank, world, local = env_rank()
@@ -311,6 +312,105 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+BATCH_JOBS = 32
+BATCH_RES = [(128, 128), (256, 256), (512, 288), (1024, 1024), (1920, 1080)]
+
+
+def batch_jobs(seed=4):
+    """The mixed-job workload: 32 jobs in a seeded arrival order, resolution
+    from BATCH_RES, spp U{1..16}, depth U{3..8}, scene from the small (sphere)
+    or the full-frame (icosphere grid) family with U{1..64} object instances."""
+    import dataclasses
+    from kittlespt_gb300 import scenes as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = S.scene_full(W, H, SPP, DEPTH)
+    objects, lights = base.instances[:64], base.instances[64:]
+    jobs = []
+    for _ in range(BATCH_JOBS):
+        w, h = BATCH_RES[int(rng.integers(0, len(BATCH_RES)))]
+        spp, depth = int(rng.integers(1, 17)), int(rng.integers(3, 9))
+        n_inst = int(rng.integers(1, 65))
+        if rng.integers(0, 2) == 0:
+            sc = S.scene_small_n(w, h, spp, depth, n_inst, seed=int(rng.integers(0, 1 << 30)))
+        else:
+            sc = dataclasses.replace(base, instances=objects[:n_inst] + lights,
+                                     camera=S.Camera.look_at((0.0, 4.0, 22.0), (0.0, 1.0, 0.0), 45.0, w, h),
+                                     settings=S.settings(max_depth=depth, bloom=True, auto_exposure=True),
+                                     width=w, height=h, spp=spp, name=f"icosphere_grid_{n_inst}")
+        jobs.append(sc)
+    return jobs
+
+
+def run_batch(args):
+    """Batched requests against the same jobs launched one by one: total
+    Msamples/s and p50/p99 job latency (all jobs arrive at once; a job's
+    latency is the wall time from the start of the round to the end of its
+    frame, host submission included)."""
+    import torch
+    from kittlespt_gb300 import build as B
+    B.build()
+    from kittlespt_gb300.renderer import Batch, Renderer
+    jobs = batch_jobs()
+    rs = []
+    for sc in jobs:
+        r = Renderer(0)
+        r.initialize()
+        r.load_scene(sc)
+        rs.append(r)
+    spp = [sc.spp for sc in jobs]
+    samples = sum(sc.width * sc.height * sc.spp for sc in jobs)
+
+    def one_by_one():
+        lat, t0 = [], time.perf_counter()
+        for r, s in zip(rs, spp):
+            r.execute_rendering(16.0, s)
+            r.synchronize()
+            lat.append((time.perf_counter() - t0) * 1e3)
+        return (time.perf_counter() - t0) * 1e3, np.array(lat)
+
+    with Batch(0) as b:
+        def batched(lanes):
+            t0 = time.perf_counter()
+            b.submit(rs, spp, lanes=lanes)
+            t_sub = (time.perf_counter() - t0) * 1e3
+            job_ms, _ = b.wait()
+            return (time.perf_counter() - t0) * 1e3, job_ms + t_sub
+
+        for _ in range(args.warmup):
+            one_by_one()
+            batched(0)
+        t_tune = time.perf_counter()
+        tuning, lanes, tuned_ms = b.autotune(rs, spp, reps=2)
+        t_tune = time.perf_counter() - t_tune
+        batched(lanes)   # instantiate the tuned graph outside the timed rounds
+        seq = [one_by_one() for _ in range(args.steps)]
+        bat = [batched(lanes) for _ in range(args.steps)]
+    for r in rs:
+        r.shutdown()
+    torch.cuda.synchronize()
+    seq_ms = float(np.mean([t for t, _ in seq]))
+    bat_ms = float(np.mean([t for t, _ in bat]))
+    seq_lat = np.concatenate([l for _, l in seq])
+    bat_lat = np.concatenate([l for _, l in bat])
+    out = {"metric": "total Msamples/s, 32 mixed jobs (batched requests)", "value": samples / bat_ms / 1e3,
+           "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": bat_ms, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded mixed jobs of the small and full-frame scene families)",
+           "config": {"workload": "batch_32_mixed_jobs", "jobs": BATCH_JOBS, "samples_per_round": samples,
+                      "resolutions": [f"{sc.width}x{sc.height}" for sc in jobs], "spp": spp,
+                      "depths": [int(sc.settings["max_depth"]) for sc in jobs],
+                      "instances": [len(sc.instances) for sc in jobs]},
+           "batched": {"Msamples_per_s": samples / bat_ms / 1e3, "round_ms": bat_ms,
+                       "p50_latency_ms": float(np.percentile(bat_lat, 50)),
+                       "p99_latency_ms": float(np.percentile(bat_lat, 99))},
+           "one_by_one": {"Msamples_per_s": samples / seq_ms / 1e3, "round_ms": seq_ms,
+                          "p50_latency_ms": float(np.percentile(seq_lat, 50)),
+                          "p99_latency_ms": float(np.percentile(seq_lat, 99))},
+           "speedup": seq_ms / bat_ms,
+           "autotune": {"tuning": tuning, "lanes": lanes, "device_ms": tuned_ms, "tuning_seconds": t_tune}}
+    print(json.dumps(out))
+
+
 def run_profile_case(spec):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
     small case that ncu captures of single kernels run on."""
@@ -334,6 +434,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
+                    help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
     args = ap.parse_args()
@@ -342,6 +444,8 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

@@ -240,6 +240,49 @@ kpt_status kpt_get_stream(kpt_context* ctx, void** stream);
 /* Kernel-launch counter of the context (every kernel the library enqueues). */
 kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
 
+/* ---- Batched requests.  No counterpart in the reference, which renders one
+ * frame of one scene per Renderer::executeRendering call (renderer.cu:103-195)
+ * and synchronises after every launch. ---- */
+
+/* Launch parameters of a context's path stage.  grid_scale: fraction of the
+ * persistent grid (resident blocks x SMs) its wave kernels launch with, so
+ * that jobs of one batch share the SMs; wave_cap: paths advanced together per
+ * wave (queue capacity), 0 = 2^25; shade_block: threads per block of the
+ * shading kernel (64, 128 or 256, 0 = 128). */
+typedef struct kpt_tuning {
+    float grid_scale;
+    int32_t wave_cap;
+    int32_t shade_block;
+    int32_t pad;
+} kpt_tuning;
+void kpt_tuning_default(kpt_tuning* t);
+kpt_status kpt_set_tuning(kpt_context* ctx, const kpt_tuning* t);
+kpt_status kpt_get_tuning(kpt_context* ctx, kpt_tuning* t);
+
+/* A batch renders one frame (spp samples, then the post chain) of each of n
+ * jobs -- contexts of the batch's device, each with its own scene, camera,
+ * resolution and settings, none twice -- as branches of one CUDA graph on the
+ * batch's stream: `lanes` chains of jobs run concurrently (jobs are dealt to
+ * the lanes longest first by W*H*spp*max_depth; lanes <= 0 or >= n: one lane
+ * per job).  kpt_submit_batch returns after the launch; kpt_wait_batch waits
+ * and returns each job's device latency from the start of the batch to the
+ * end of its frame (job_ms[n], may be null) and the batch's device time. */
+typedef struct kpt_batch kpt_batch;
+kpt_status kpt_batch_create(int device, kpt_batch** out);
+kpt_status kpt_batch_destroy(kpt_batch* b);
+kpt_status kpt_submit_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp, int lanes);
+kpt_status kpt_wait_batch(kpt_batch* b, float* job_ms, float* total_ms);
+
+/* The batch autotuner: renders the batch under each candidate (grid_scale,
+ * wave_cap, shade_block, lanes) -- one untimed and `reps` timed submissions
+ * each -- keeps the fastest total device time, applies its tuning to every
+ * job and returns it with its lane count and time.  The result is cached per
+ * batch signature (the jobs' sizes, spp and depths): a second call with the
+ * same signature applies the cached choice without rendering.  Frames
+ * rendered while tuning are discarded: every job's accumulation is reset. */
+kpt_status kpt_autotune_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp, int reps,
+                              kpt_tuning* best, int32_t* best_lanes, float* best_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,10 @@ class Stats(C.Structure):
                 ("avg_bin", C.c_float), ("frame_index", C.c_int32), ("pad", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("grid_scale", C.c_float), ("wave_cap", C.c_int32), ("shade_block", C.c_int32), ("pad", C.c_int32)]
+
+
 assert C.sizeof(Material) == 72 and C.sizeof(Environment) == 48
 assert C.sizeof(Settings) == 32 and C.sizeof(Exposure) == 48
 
@@ -119,6 +123,14 @@ SIGNATURES = {
     "kpt_path_kernel_ms": (_S, [_P, C.c_int, C.POINTER(C.c_float)]),
     "kpt_get_stream": (_S, [_P, C.POINTER(_P)]),
     "kpt_launch_count": (_S, [_P, C.POINTER(C.c_uint64)]),
+    "kpt_tuning_default": (None, [C.POINTER(Tuning)]),
+    "kpt_set_tuning": (_S, [_P, C.POINTER(Tuning)]),
+    "kpt_get_tuning": (_S, [_P, C.POINTER(Tuning)]),
+    "kpt_batch_create": (_S, [C.c_int, C.POINTER(_P)]),
+    "kpt_batch_destroy": (_S, [_P]),
+    "kpt_submit_batch": (_S, [_P, C.c_int, C.POINTER(_P), _I, C.c_int]),
+    "kpt_wait_batch": (_S, [_P, _F, _F]),
+    "kpt_autotune_batch": (_S, [_P, C.c_int, C.POINTER(_P), _I, C.c_int, C.POINTER(Tuning), _I, _F]),
 }
 
 _lib = None

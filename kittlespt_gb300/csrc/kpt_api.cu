@@ -10,7 +10,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -126,6 +128,7 @@ struct kpt_context {
     DBuf<PathRec> paths[2];
     DBuf<ShadowRec> shadow;
     int wave_cap = 0;
+    kpt_tuning tuning{};   // launch parameters of the path stage (kpt_set_tuning)
 
     // stage timing inside the frame graph: per frame, event-record nodes
     // between the launches and the stage each interval belongs to
@@ -206,6 +209,7 @@ kpt_status kpt_create(int device, kpt_context** out) {
     kpt_environment_default(&c->env);
     kpt_settings_default(&c->settings);
     kpt_exposure_default(&c->exposure);
+    kpt_tuning_default(&c->tuning);
     if (c->expo_state.ensure(1) != cudaSuccess || c->sun_radiance.ensure(1) != cudaSuccess ||
         c->counters.ensure(12) != cudaSuccess ||
         c->counts.ensure(4) != cudaSuccess || c->fetch.ensure(1) != cudaSuccess ||
@@ -677,7 +681,8 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
 static kpt_status ensure_work(kpt_context* c, int nsamples) {
     size_t np = (size_t)c->W * c->H, ns = np * (size_t)nsamples;
     if (ns > (size_t)INT32_MAX) return fail(KPT_ERR_INVALID, "more than 2^31 - 1 samples in one call");
-    const int cap = (int)std::min<long long>((long long)ns, WAVE_CAP);
+    const long long wcap = c->tuning.wave_cap > 0 ? (long long)c->tuning.wave_cap : WAVE_CAP;
+    const int cap = (int)std::min<long long>((long long)ns, wcap);
     KPT_CUDA(c->paths[0].ensure(cap));
     KPT_CUDA(c->paths[1].ensure(cap));
     KPT_CUDA(c->hits.ensure(cap));
@@ -694,10 +699,13 @@ static kpt_status ensure_work(kpt_context* c, int nsamples) {
     return KPT_OK;
 }
 
+// Resident blocks x SMs, scaled by the context's grid_scale (a job of a batch
+// shares the SMs with the others).
 static int persistent_grid(kpt_context* c, const void* kern, int block) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
-    return std::max(1, per_sm) * c->sm_count;
+    const int full = std::max(1, per_sm) * c->sm_count;
+    return std::max(1, (int)std::lround((double)full * c->tuning.grid_scale));
 }
 
 // Closes the current timed interval of the frame being captured (if any) and
@@ -722,7 +730,8 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
     k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
     c->launches += 3;
-    const int g_shade = persistent_grid(c, (const void*)k_shade, PATH_BLOCK);
+    const int shade_block = c->tuning.shade_block > 0 ? c->tuning.shade_block : PATH_BLOCK;
+    const int g_shade = persistent_grid(c, (const void*)k_shade, shade_block);
     const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
     const int g_shd = persistent_grid(c, (const void*)k_shadow, TRACE_BLOCK);
     // every pixel may hit: the last waves find no work when fewer do
@@ -735,7 +744,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
             }
             stage_mark(c, KPT_STAGE_SHADE);
-            k_shade<<<g_shade, PATH_BLOCK, 0, s>>>(F, l, w0);
+            k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
             stage_mark(c, KPT_STAGE_SHADOW);
             k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
             c->launches += l > 0 ? 3 : 2;
@@ -831,17 +840,53 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
     stage_mark(c, KPT_STAGE_COUNT);   // end of the last interval
 }
 
-kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
+// Host-side work of a frame, outside any capture: TLAS rebuild, exposure
+// thresholds, work buffers, the frame's parameters.
+static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     kpt_status st = ready(c);
     if (st != KPT_OK) return st;
-    if (spp <= 0) return fail(KPT_ERR_INVALID, "kpt_render_frame: spp must be positive");
+    if (spp <= 0) return fail(KPT_ERR_INVALID, "spp must be positive");
     update_thresholds(c);
     st = ensure_work(c, spp);
     if (st != KPT_OK) return st;
-    FrameParams F = frame_params(c, c->frame_index, spp);
-    F.acc = c->acc.p;
-    F.albedo = c->albedo.p;
-    F.first_hit = c->first_hit.p;
+    *F = frame_params(c, c->frame_index, spp);
+    F->acc = c->acc.p;
+    F->albedo = c->albedo.p;
+    F->first_hit = c->first_hit.p;
+    return KPT_OK;
+}
+
+static void finish_frame(kpt_context* c, int spp) {
+    c->frame_index += spp;
+    c->frames_rendered++;
+}
+
+// Instantiates `g` into *exec, updating the previous executable in place when
+// the topology is unchanged.  Consumes g.
+static kpt_status instantiate(cudaGraph_t g, cudaGraphExec_t* exec) {
+    if (*exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(*exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(*exec);
+            *exec = nullptr;
+        }
+    }
+    if (!*exec) {
+        cudaError_t e = cudaGraphInstantiate(exec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return fail(KPT_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaGraphDestroy(g);
+    return KPT_OK;
+}
+
+kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
+    FrameParams F;
+    kpt_status st = prepare_frame(c, spp, &F);
+    if (st != KPT_OK) return st;
     int total = c->frame_index + spp;
     cudaGraph_t g = nullptr;
     if (c->timing) {
@@ -856,26 +901,11 @@ kpt_status kpt_render_frame(kpt_context* c, int spp, float delta_ms) {
     }
     c->tf = nullptr;
     KPT_CUDA(ce);
-    if (c->graph_exec) {
-        cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(c->graph_exec, g, &info) != cudaSuccess) {
-            cudaGetLastError();
-            cudaGraphExecDestroy(c->graph_exec);
-            c->graph_exec = nullptr;
-        }
-    }
-    if (!c->graph_exec) {
-        cudaError_t e = cudaGraphInstantiate(&c->graph_exec, g, 0);
-        if (e != cudaSuccess) {
-            cudaGraphDestroy(g);
-            return fail(KPT_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-        }
-    }
+    st = instantiate(g, &c->graph_exec);
+    if (st != KPT_OK) return st;
     cudaError_t e = cudaGraphLaunch(c->graph_exec, c->stream);
-    cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(KPT_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
-    c->frame_index = total;
-    c->frames_rendered++;
+    finish_frame(c, spp);
     return KPT_OK;
 }
 
@@ -1091,6 +1121,290 @@ kpt_status kpt_get_stream(kpt_context* c, void** s) {
 kpt_status kpt_launch_count(kpt_context* c, uint64_t* n) {
     if (!c || !n) return fail(KPT_ERR_INVALID, "null argument");
     *n = c->launches;
+    return KPT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch parameters and batched requests
+
+void kpt_tuning_default(kpt_tuning* t) {
+    t->grid_scale = 1.0f;
+    t->wave_cap = 0;
+    t->shade_block = PATH_BLOCK;
+    t->pad = 0;
+}
+
+kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
+    if (!c || !t) return fail(KPT_ERR_INVALID, "kpt_set_tuning: null argument");
+    if (!(t->grid_scale > 0.0f && t->grid_scale <= 1.0f))
+        return fail(KPT_ERR_INVALID, "kpt_set_tuning: grid_scale must be in (0, 1]");
+    if (t->wave_cap != 0 && (t->wave_cap < 1024 || t->wave_cap > WAVE_CAP))
+        return fail(KPT_ERR_INVALID, "kpt_set_tuning: wave_cap must be 0 or in [1024, 2^25]");
+    if (t->shade_block != 0 && t->shade_block != 64 && t->shade_block != 128 && t->shade_block != 256)
+        return fail(KPT_ERR_INVALID, "kpt_set_tuning: shade_block must be 0, 64, 128 or 256");
+    c->tuning = *t;
+    if (c->tuning.shade_block == 0) c->tuning.shade_block = PATH_BLOCK;
+    return KPT_OK;
+}
+
+kpt_status kpt_get_tuning(kpt_context* c, kpt_tuning* t) {
+    if (!c || !t) return fail(KPT_ERR_INVALID, "kpt_get_tuning: null argument");
+    *t = c->tuning;
+    return KPT_OK;
+}
+
+}  // extern "C"
+
+struct kpt_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_fork = nullptr, ev_done = nullptr;
+    std::vector<cudaEvent_t> ev_end, ev_dep, ev_pre;   // per job
+    int n = 0;
+    bool pending = false;
+    struct Choice {
+        kpt_tuning tuning;
+        int lanes;
+        float ms;
+    };
+    std::map<std::string, Choice> cache;   // batch signature -> autotuned choice
+};
+
+namespace {
+
+kpt_status batch_events(kpt_batch* b, int n) {
+    while ((int)b->ev_end.size() < n) {
+        cudaEvent_t e = nullptr, d = nullptr, p = nullptr;
+        KPT_CUDA(cudaEventCreate(&e));
+        KPT_CUDA(cudaEventCreateWithFlags(&d, cudaEventDisableTiming));
+        KPT_CUDA(cudaEventCreateWithFlags(&p, cudaEventDisableTiming));
+        b->ev_end.push_back(e);
+        b->ev_dep.push_back(d);
+        b->ev_pre.push_back(p);
+    }
+    return KPT_OK;
+}
+
+double job_cost(const kpt_context* c, int spp) {
+    return (double)c->W * c->H * spp * (c->settings.max_depth + 1);
+}
+
+std::string batch_signature(int n, kpt_context* const* jobs, const int32_t* spp) {
+    std::string sig;
+    for (int j = 0; j < n; ++j) {
+        const kpt_context* c = jobs[j];
+        sig += std::to_string(c->W) + "x" + std::to_string(c->H) + "x" + std::to_string(spp[j]) + "d" +
+               std::to_string(c->settings.max_depth) + "i" + std::to_string(c->instances.size()) + ";";
+    }
+    return sig;
+}
+
+}  // namespace
+
+extern "C" {
+
+kpt_status kpt_batch_create(int device, kpt_batch** out) {
+    if (!out) return fail(KPT_ERR_INVALID, "kpt_batch_create: null output");
+    int nd = 0;
+    KPT_CUDA(cudaGetDeviceCount(&nd));
+    if (device < 0 || device >= nd) return fail(KPT_ERR_INVALID, "kpt_batch_create: no such device");
+    KPT_CUDA(cudaSetDevice(device));
+    kpt_batch* b = new kpt_batch();
+    b->device = device;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev_start) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming) != cudaSuccess) {
+        kpt_batch_destroy(b);
+        return fail(KPT_ERR_CUDA, "kpt_batch_create: stream or event creation failed");
+    }
+    *out = b;
+    return KPT_OK;
+}
+
+kpt_status kpt_batch_destroy(kpt_batch* b) {
+    if (!b) return KPT_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (cudaEvent_t e : {b->ev_start, b->ev_fork, b->ev_done})
+        if (e) cudaEventDestroy(e);
+    for (auto* v : {&b->ev_end, &b->ev_dep, &b->ev_pre})
+        for (cudaEvent_t e : *v) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return KPT_OK;
+}
+
+kpt_status kpt_submit_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp, int lanes) {
+    if (!b || n <= 0 || !jobs || !spp) return fail(KPT_ERR_INVALID, "kpt_submit_batch: bad arguments");
+    if (b->pending) return fail(KPT_ERR_STATE, "kpt_submit_batch: the previous batch was not waited for");
+    for (int j = 0; j < n; ++j) {
+        if (!jobs[j]) return fail(KPT_ERR_INVALID, "kpt_submit_batch: null job");
+        if (jobs[j]->device != b->device) return fail(KPT_ERR_INVALID, "kpt_submit_batch: job on another device");
+        if (spp[j] <= 0) return fail(KPT_ERR_INVALID, "kpt_submit_batch: spp must be positive");
+        for (int k = 0; k < j; ++k)
+            if (jobs[k] == jobs[j]) return fail(KPT_ERR_INVALID, "kpt_submit_batch: a context appears twice");
+    }
+    KPT_CUDA(cudaSetDevice(b->device));
+    kpt_status st = batch_events(b, n);
+    if (st != KPT_OK) return st;
+    // host work of every frame, then the batch stream waits for what it enqueued
+    std::vector<FrameParams> F(n);
+    for (int j = 0; j < n; ++j) {
+        st = prepare_frame(jobs[j], spp[j], &F[j]);
+        if (st != KPT_OK) return st;
+        KPT_CUDA(cudaEventRecord(b->ev_pre[j], jobs[j]->stream));
+        KPT_CUDA(cudaStreamWaitEvent(b->stream, b->ev_pre[j], 0));
+    }
+    // jobs dealt longest first to the least-loaded lane
+    const int L = (lanes <= 0 || lanes >= n) ? n : lanes;
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int c) { return job_cost(jobs[a], spp[a]) > job_cost(jobs[c], spp[c]); });
+    std::vector<double> load(L, 0.0);
+    std::vector<int> last(L, -1), prev(n, -1);
+    for (int j : order) {
+        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        prev[j] = last[l];
+        last[l] = j;
+        load[l] += job_cost(jobs[j], spp[j]);
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        cudaEventRecordWithFlags(b->ev_start, b->stream, cudaEventRecordExternal);
+        cudaEventRecord(b->ev_fork, b->stream);
+        for (int j : order) {
+            kpt_context* c = jobs[j];
+            cudaStreamWaitEvent(c->stream, prev[j] < 0 ? b->ev_fork : b->ev_dep[prev[j]], 0);
+            enqueue_frame(c, F[j], c->frame_index + spp[j], c->settings.frame_delta_ms);
+            cudaEventRecordWithFlags(b->ev_end[j], c->stream, cudaEventRecordExternal);
+            cudaEventRecord(b->ev_dep[j], c->stream);
+        }
+        for (int l = 0; l < L; ++l)
+            if (last[l] >= 0) cudaStreamWaitEvent(b->stream, b->ev_dep[last[l]], 0);
+        ce = cudaStreamEndCapture(b->stream, &g);
+    }
+    KPT_CUDA(ce);
+    st = instantiate(g, &b->exec);
+    if (st != KPT_OK) return st;
+    KPT_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    // later work on a job's own stream (reads, its next frame) follows the batch
+    KPT_CUDA(cudaEventRecord(b->ev_done, b->stream));
+    for (int j = 0; j < n; ++j) {
+        KPT_CUDA(cudaStreamWaitEvent(jobs[j]->stream, b->ev_done, 0));
+        finish_frame(jobs[j], spp[j]);
+    }
+    b->n = n;
+    b->pending = true;
+    return KPT_OK;
+}
+
+kpt_status kpt_wait_batch(kpt_batch* b, float* job_ms, float* total_ms) {
+    if (!b) return fail(KPT_ERR_INVALID, "kpt_wait_batch: null batch");
+    if (!b->pending) return fail(KPT_ERR_STATE, "kpt_wait_batch: no batch submitted");
+    KPT_CUDA(cudaSetDevice(b->device));
+    b->pending = false;
+    KPT_CUDA(cudaStreamSynchronize(b->stream));
+    float total = 0.0f;
+    for (int j = 0; j < b->n; ++j) {
+        float ms = 0.0f;
+        KPT_CUDA(cudaEventElapsedTime(&ms, b->ev_start, b->ev_end[j]));
+        if (job_ms) job_ms[j] = ms;
+        total = std::max(total, ms);
+    }
+    if (total_ms) *total_ms = total;
+    return KPT_OK;
+}
+
+// Device time of one batch under (tuning, lanes): one untimed submission, then
+// the mean of `reps` timed ones.
+static kpt_status time_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp,
+                             const kpt_tuning& t, int lanes, int reps, float* ms) {
+    for (int j = 0; j < n; ++j) {
+        kpt_status st = kpt_set_tuning(jobs[j], &t);
+        if (st != KPT_OK) return st;
+    }
+    double sum = 0.0;
+    for (int r = 0; r <= reps; ++r) {
+        kpt_status st = kpt_submit_batch(b, n, jobs, spp, lanes);
+        if (st != KPT_OK) return st;
+        float total = 0.0f;
+        st = kpt_wait_batch(b, nullptr, &total);
+        if (st != KPT_OK) return st;
+        if (r > 0) sum += total;
+    }
+    *ms = (float)(sum / reps);
+    return KPT_OK;
+}
+
+kpt_status kpt_autotune_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp, int reps,
+                              kpt_tuning* best, int32_t* best_lanes, float* best_ms) {
+    if (!b || n <= 0 || !jobs || !spp || reps <= 0) return fail(KPT_ERR_INVALID, "kpt_autotune_batch: bad arguments");
+    for (int j = 0; j < n; ++j)
+        if (!jobs[j]) return fail(KPT_ERR_INVALID, "kpt_autotune_batch: null job");
+    const std::string sig = batch_signature(n, jobs, spp);
+    auto hit = b->cache.find(sig);
+    kpt_batch::Choice choice;
+    if (hit != b->cache.end()) {
+        choice = hit->second;
+    } else {
+        // coordinate descent from the single-frame defaults: lanes, then the
+        // grid share, the wave capacity and the shading block, each value
+        // tried with the others at their best so far
+        kpt_tuning cur;
+        kpt_tuning_default(&cur);
+        int lanes = n;
+        float cur_ms = 0.0f;
+        kpt_status st = time_batch(b, n, jobs, spp, cur, lanes, reps, &cur_ms);
+        if (st != KPT_OK) return st;
+        std::vector<int> lane_opts;
+        for (int l = n / 2; l >= 1 && (int)lane_opts.size() < 3; l /= 2) lane_opts.push_back(l);
+        for (int l : lane_opts) {
+            float ms = 0.0f;
+            st = time_batch(b, n, jobs, spp, cur, l, reps, &ms);
+            if (st != KPT_OK) return st;
+            if (ms < cur_ms) { cur_ms = ms; lanes = l; }
+        }
+        for (float g : {0.5f, 0.25f, 0.125f}) {
+            kpt_tuning t = cur;
+            t.grid_scale = g;
+            float ms = 0.0f;
+            st = time_batch(b, n, jobs, spp, t, lanes, reps, &ms);
+            if (st != KPT_OK) return st;
+            if (ms < cur_ms) { cur_ms = ms; cur = t; }
+        }
+        for (int w : {1 << 23, 1 << 21}) {
+            kpt_tuning t = cur;
+            t.wave_cap = w;
+            float ms = 0.0f;
+            st = time_batch(b, n, jobs, spp, t, lanes, reps, &ms);
+            if (st != KPT_OK) return st;
+            if (ms < cur_ms) { cur_ms = ms; cur = t; }
+        }
+        for (int blk : {64, 256}) {
+            kpt_tuning t = cur;
+            t.shade_block = blk;
+            float ms = 0.0f;
+            st = time_batch(b, n, jobs, spp, t, lanes, reps, &ms);
+            if (st != KPT_OK) return st;
+            if (ms < cur_ms) { cur_ms = ms; cur = t; }
+        }
+        choice = {cur, lanes, cur_ms};
+        b->cache[sig] = choice;
+    }
+    for (int j = 0; j < n; ++j) {
+        kpt_status st = kpt_set_tuning(jobs[j], &choice.tuning);
+        if (st != KPT_OK) return st;
+        st = clear_accumulation(jobs[j]);
+        if (st != KPT_OK) return st;
+    }
+    if (best) *best = choice.tuning;
+    if (best_lanes) *best_lanes = choice.lanes;
+    if (best_ms) *best_ms = choice.ms;
     return KPT_OK;
 }
 

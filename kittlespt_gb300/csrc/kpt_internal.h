@@ -7,6 +7,7 @@
 namespace kpt {
 
 constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
+constexpr int SHADE_MAX_BLOCK = 256;   // largest block k_shade is launched with (kpt_tuning.shade_block)
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
 #ifndef KPT_TRACE_MIN_BLOCKS
 #define KPT_TRACE_MIN_BLOCKS 8

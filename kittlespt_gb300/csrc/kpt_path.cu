@@ -263,7 +263,7 @@ __device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si
 // emission here, its light sample in k_shadow, the next vertex's terms at the
 // next level, the sky last.  Level 0 starts the paths of items
 // wave0 .. wave0+cap-1 from the camera-ray hits of k_primary.
-__global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, long long wave0) {
+__global__ void __launch_bounds__(SHADE_MAX_BLOCK) k_shade(FrameParams F, int level, long long wave0) {
     const SceneView& s = F.scene;
     const SkyParams& P = F.sky;
     const int order = F.rng_order;

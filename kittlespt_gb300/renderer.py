@@ -281,3 +281,65 @@ class Renderer:
 
     def sky_device(self, n, dirs_ptr, out_ptr):
         K.check(self._L.kpt_sky_device(self._ctx, n, dirs_ptr, out_ptr))
+
+    # -- launch parameters (no reference counterpart) -------------------------
+    def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0):
+        t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block)
+        K.check(self._L.kpt_set_tuning(self._ctx, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = K.Tuning()
+        K.check(self._L.kpt_get_tuning(self._ctx, C.byref(t)))
+        return {"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block}
+
+
+class Batch:
+    """Batched requests (no reference counterpart): one frame of each of many
+    renderers -- each its own scene, camera, resolution and settings -- as
+    concurrent branches of one CUDA graph (kpt_submit_batch), and the
+    autotuner that picks their launch parameters (kpt_autotune_batch)."""
+
+    def __init__(self, device: int = 0):
+        self._L = K.load()
+        self._b = C.c_void_p()
+        K.check(self._L.kpt_batch_create(device, C.byref(self._b)))
+        self._n = 0
+
+    def close(self):
+        if self._b:
+            K.check(self._L.kpt_batch_destroy(self._b))
+            self._b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _args(self, renderers, spp):
+        n = len(renderers)
+        jobs = (C.c_void_p * n)(*[r._ctx.value for r in renderers])
+        s = np.ascontiguousarray(np.broadcast_to(np.asarray(spp, np.int32), (n,)))
+        return n, jobs, s
+
+    def submit(self, renderers, spp, lanes: int = 0):
+        n, jobs, s = self._args(renderers, spp)
+        K.check(self._L.kpt_submit_batch(self._b, n, jobs, K.iptr(s), lanes))
+        self._n = n
+
+    def wait(self):
+        """Per-job device latency from the batch start (ms) and the batch's device time."""
+        job = np.zeros(max(self._n, 1), np.float32)
+        total = np.zeros(1, np.float32)
+        K.check(self._L.kpt_wait_batch(self._b, K.fptr(job), K.fptr(total)))
+        return job[:self._n], float(total[0])
+
+    def autotune(self, renderers, spp, reps: int = 2):
+        n, jobs, s = self._args(renderers, spp)
+        t = K.Tuning()
+        lanes = np.zeros(1, np.int32)
+        ms = np.zeros(1, np.float32)
+        K.check(self._L.kpt_autotune_batch(self._b, n, jobs, K.iptr(s), reps, C.byref(t), K.iptr(lanes),
+                                           K.fptr(ms)))
+        return ({"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block},
+                int(lanes[0]), float(ms[0]))

@@ -1,0 +1,158 @@
+"""Batched requests (kpt_submit_batch / kpt_wait_batch / kpt_autotune_batch).
+
+A batch renders one frame of each job as a branch of one CUDA graph; every
+job's samples are computed exactly as by kpt_render_frame, so images and
+accumulations must be bit-identical to rendering the jobs one by one, under
+any lane count and any launch tuning (grid share, wave capacity -- a small one
+forces many waves -- and shading block size)."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from kittlespt_gb300 import _lib as K
+
+
+def test_tuning_defaults_and_errors():
+    L = K.load()
+    t = K.Tuning()
+    L.kpt_tuning_default(C.byref(t))
+    assert (t.grid_scale, t.wave_cap, t.shade_block) == (1.0, 0, 128)
+    assert L.kpt_set_tuning(None, C.byref(t)) == -1
+    assert L.kpt_get_tuning(None, C.byref(t)) == -1
+    assert L.kpt_submit_batch(None, 1, None, None, 0) == -1
+    assert L.kpt_wait_batch(None, None, None) == -1
+    assert L.kpt_autotune_batch(None, 1, None, None, 1, None, None, None) == -1
+    assert L.kpt_batch_destroy(None) == 0
+
+
+def _jobs():
+    from kittlespt_gb300 import scenes as S
+    return [
+        (S.scene_small_n(96, 64, 2, 4, 3), 2),
+        (S.scene_small(128, 72, 3, 3), 3),
+        (S.scene_full(160, 90, 1, 5), 1),
+        (S.scene_small_n(64, 64, 4, 6, 8, seed=5), 4),
+    ]
+
+
+def _renderers(jobs):
+    from kittlespt_gb300.renderer import Renderer
+    rs = []
+    for sc, _ in jobs:
+        r = Renderer(0)
+        r.initialize()
+        r.load_scene(sc)
+        rs.append(r)
+    return rs
+
+
+def _outputs(rs):
+    for r in rs:
+        r.synchronize()
+    return [(r.get_render_target(), r.read_accumulation()) for r in rs]
+
+
+def _same(a, b, images=True):
+    for (ia, aa), (ib, ab) in zip(a, b):
+        if images:
+            np.testing.assert_array_equal(ia.view(np.uint32), ib.view(np.uint32))
+        np.testing.assert_array_equal(aa.view(np.uint32), ab.view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def reference_frames():
+    """Two frames of every job, rendered one by one."""
+    jobs = _jobs()
+    rs = _renderers(jobs)
+    for _ in range(2):
+        for r, (_, spp) in zip(rs, jobs):
+            r.execute_rendering(16.0, spp)
+    out = _outputs(rs)
+    for r in rs:
+        r.shutdown()
+    return jobs, out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lanes,tuning", [
+    (0, None),
+    (2, None),
+    (1, dict(grid_scale=0.25, wave_cap=1024, shade_block=64)),
+    (3, dict(grid_scale=0.5, wave_cap=4096, shade_block=256)),
+])
+def test_batch_matches_one_by_one(reference_frames, lanes, tuning):
+    from kittlespt_gb300.renderer import Batch
+    jobs, ref = reference_frames
+    rs = _renderers(jobs)
+    spp = [s for _, s in jobs]
+    try:
+        if tuning:
+            for r in rs:
+                r.set_tuning(**tuning)
+        with Batch(0) as b:
+            for _ in range(2):
+                b.submit(rs, spp, lanes=lanes)
+                job_ms, total = b.wait()
+                assert job_ms.shape == (len(rs),) and np.all(job_ms > 0)
+                assert total == pytest.approx(float(job_ms.max()))
+        _same(_outputs(rs), ref)
+        assert all(r.stats().frame_index == 2 * s for r, s in zip(rs, spp))
+    finally:
+        for r in rs:
+            r.shutdown()
+
+
+@pytest.mark.gpu
+def test_batch_errors():
+    from kittlespt_gb300.renderer import Batch
+    from kittlespt_gb300 import scenes as S
+    rs = _renderers([(S.scene_small(32, 32, 1, 2), 1)])
+    try:
+        with Batch(0) as b:
+            with pytest.raises(K.KptError):
+                b.submit(rs + rs, [1, 1])       # one context twice
+            with pytest.raises(K.KptError):
+                b.submit(rs, [0])               # no samples
+            with pytest.raises(K.KptError):
+                b.wait()                        # nothing submitted
+            b.submit(rs, [1])
+            with pytest.raises(K.KptError):
+                b.submit(rs, [1])               # previous batch not waited for
+            b.wait()
+        with pytest.raises(K.KptError):
+            rs[0].set_tuning(grid_scale=0.0)
+        with pytest.raises(K.KptError):
+            rs[0].set_tuning(wave_cap=100)
+        with pytest.raises(K.KptError):
+            rs[0].set_tuning(shade_block=96)
+    finally:
+        for r in rs:
+            r.shutdown()
+
+
+@pytest.mark.gpu
+def test_autotune_applies_and_caches(reference_frames):
+    from kittlespt_gb300.renderer import Batch
+    jobs, ref = reference_frames
+    rs = _renderers(jobs)
+    spp = [s for _, s in jobs]
+    try:
+        with Batch(0) as b:
+            t1, lanes1, ms1 = b.autotune(rs, spp, reps=1)
+            assert 0.0 < t1["grid_scale"] <= 1.0 and t1["shade_block"] in (64, 128, 256)
+            assert 1 <= lanes1 <= len(rs) and ms1 > 0.0
+            assert all(r.tuning() == t1 for r in rs)
+            assert all(r.stats().frame_index == 0 for r in rs)   # tuning frames discarded
+            t2, lanes2, ms2 = b.autotune(rs, spp, reps=1)          # cached: same choice, no rendering
+            assert (t2, lanes2, ms2) == (t1, lanes1, ms1)
+            for _ in range(2):
+                b.submit(rs, spp, lanes=lanes1)
+                b.wait()
+        # the eye adaptation of the discarded frames persists (resetAccumulation
+        # keeps it, renderer.cu:336-340): only the accumulation is compared
+        _same(_outputs(rs), ref, images=False)
+    finally:
+        for r in rs:
+            r.shutdown()
