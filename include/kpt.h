@@ -77,11 +77,9 @@ typedef struct kpt_exposure {
     float pad0, pad1;
 } kpt_exposure;
 
-/* Statistics since kpt_create (algorithmic work counted in-kernel: every ray
- * of the path stage, then the path kernel's own share) and of the last
- * exposure update. */
-/* Traversal counters (cumulative since kpt_create): every query, then the
- * path stage's extension rays (closest hit) and shadow rays (any hit). */
+/* Traversal counters (cumulative since kpt_create, counted in-kernel): every
+ * query, then the path stage's extension rays (closest hit) and shadow rays
+ * (any hit); and the state of the last exposure update. */
 typedef struct kpt_stats {
     uint64_t box_tests, tri_tests, inst_xforms, overflows;
     uint64_t path_box_tests, path_tri_tests, path_inst_xforms;
@@ -282,6 +280,41 @@ kpt_status kpt_wait_batch(kpt_batch* b, float* job_ms, float* total_ms);
  * rendered while tuning are discarded: every job's accumulation is reset. */
 kpt_status kpt_autotune_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp, int reps,
                               kpt_tuning* best, int32_t* best_lanes, float* best_ms);
+
+/* ---- Path-replay adjoint.  No counterpart in the reference. ----
+ *
+ * The differentiated image is, per pixel, the mean over the samples sample0 ..
+ * sample0+nsamples-1 of the clamped path radiance (the quantity the
+ * accumulation receives per frame, before modulation and the post chain).
+ * Given adjoint = dLoss/dimage ([H][W] RGBA float, alpha ignored), the adjoint
+ * replays every sample's path from its random-number stream and returns
+ * dLoss/dtheta for theta = per material m (albedo r, g, b, roughness) in
+ * material order, then the sky (Rayleigh r, g, b, Mie, Rayleigh scale height,
+ * Mie scale height): kpt_adjoint_param_count() values.  Sampled directions,
+ * lobe, light and sun choices, Russian roulette, pdfs and MIS weights are held
+ * fixed (detached sampling): the gradient is that of the estimator with
+ * respect to the BSDF values and the sky radiance.  image (may be null)
+ * receives the image itself.  Requires max_depth <= 16.
+ * kpt_adjoint_device takes device pointers (grad: doubles) and does not
+ * synchronise; kpt_adjoint takes host arrays. */
+kpt_status kpt_adjoint_param_count(kpt_context* ctx, int* n);
+kpt_status kpt_adjoint_device(kpt_context* ctx, int sample0, int nsamples, const float* adjoint, double* grad,
+                              float* image);
+kpt_status kpt_adjoint(kpt_context* ctx, int sample0, int nsamples, const float* adjoint, double* grad, float* image);
+
+/* Test support for the adjoint's FP64 oracle: as kpt_adjoint_device, and
+ * also writes every path vertex the replay visited -- all its fixed quantities
+ * (local directions, pdfs, roulette factors, light-sample factors, emission,
+ * the sample's adjoint weight, the escape direction) -- as 192-byte records
+ * (kpt_adjoint_record_size) to records (device), at most max_records; *count
+ * (host) receives the number of vertices visited.  Synchronises. */
+int kpt_adjoint_record_size(void);
+/* The sky radiance (as kpt_sky_device) and its derivatives with respect to
+ * the six sky parameters above, for n directions (device): rgb[7 i] is the
+ * radiance, rgb[7 i + 1 + k] its derivative for parameter k (3 floats each). */
+kpt_status kpt_sky_grad_device(kpt_context* ctx, int n, const float* dirs, float* rgb);
+kpt_status kpt_adjoint_records_device(kpt_context* ctx, int sample0, int nsamples, const float* adjoint, double* grad,
+                                      void* records, int max_records, int* count);
 
 #ifdef __cplusplus
 }

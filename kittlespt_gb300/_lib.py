@@ -131,6 +131,12 @@ SIGNATURES = {
     "kpt_submit_batch": (_S, [_P, C.c_int, C.POINTER(_P), _I, C.c_int]),
     "kpt_wait_batch": (_S, [_P, _F, _F]),
     "kpt_autotune_batch": (_S, [_P, C.c_int, C.POINTER(_P), _I, C.c_int, C.POINTER(Tuning), _I, _F]),
+    "kpt_adjoint_param_count": (_S, [_P, C.POINTER(C.c_int)]),
+    "kpt_adjoint_device": (_S, [_P, C.c_int, C.c_int, _P, _P, _P]),
+    "kpt_adjoint": (_S, [_P, C.c_int, C.c_int, _F, C.POINTER(C.c_double), _F]),
+    "kpt_adjoint_record_size": (C.c_int, []),
+    "kpt_sky_grad_device": (_S, [_P, C.c_int, _P, _P]),
+    "kpt_adjoint_records_device": (_S, [_P, C.c_int, C.c_int, _P, _P, _P, C.c_int, C.POINTER(C.c_int)]),
 }
 
 _lib = None

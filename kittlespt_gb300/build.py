@@ -1,9 +1,10 @@
 """Builds libkpt.so (the CUDA path tracer behind include/kpt.h) in-tree.
 
-Four translation units, compiled in parallel with nvcc for sm_103a only:
+Five translation units, compiled in parallel with nvcc for sm_103a only:
 kpt_path.cu (path and ray kernels, fast maths like the reference's GPU
-build), kpt_post.cu (post chain, IEEE), kpt_api.cu (C ABI) and kpt_scene.cpp
-(host acceleration-structure build).  Host code is compiled without
+build), kpt_adjoint.cu (path-replay adjoint, fast maths), kpt_post.cu (post
+chain, IEEE), kpt_api.cu (C ABI) and kpt_scene.cpp (host
+acceleration-structure build).  Host code is compiled without
 floating-point contraction so x86-64 and aarch64 builds agree.
 """
 
@@ -27,6 +28,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 
 UNITS = {
     "kpt_path.cu": ["-use_fast_math"],
+    "kpt_adjoint.cu": ["-use_fast_math"],
     "kpt_post.cu": [],
     "kpt_api.cu": [],
     "kpt_scene.cpp": [],

@@ -1,0 +1,450 @@
+// kpt_adjoint.cu -- path-replay adjoint of the plain method (no counterpart in
+// the reference).
+//
+// The differentiated image is, per pixel, the mean over samples of the
+// clamped path radiance (what the accumulation adds per frame, before the
+// post chain).  For dLoss/dimage given per pixel, k_adjoint replays every
+// sample's path with the forward's random numbers -- the same camera ray,
+// traversal, light sample and BSDF sample as k_shade, in one thread -- and
+// keeps, per vertex, the throughput beta_k, the radiance the vertex adds c_k,
+// the weight to the next vertex w_k and their derivatives.  With
+// R_k = c_k + w_k R_{k+1} (R after the last vertex: the sky if the path
+// escaped), the gradient is sum_k beta_k (dc_k + dw_k R_{k+1}) plus the sky
+// terms.  Sampled directions, lobe / light / sun choices, Russian roulette,
+// pdfs and MIS weights are held fixed (detached sampling), so the result is
+// the derivative of the estimator with respect to the BSDF values (per
+// material albedo and roughness) and the sky radiance (Rayleigh r, g, b, Mie,
+// both scale heights).  Nothing is stored between passes: each sample is
+// recomputed from its RNG stream.
+#include "kpt_adjoint.cuh"
+#include "kpt_pathfn.cuh"
+
+namespace kpt {
+
+// Gradient slots: material m -> 4 m + (albedo r, g, b, roughness); then the
+// sky parameters.  Accumulated per block in shared memory (double), then
+// added to the output.
+struct GradAcc {
+    double* s;
+    __device__ __forceinline__ void add(int i, float v) {
+        if (v != 0.0f) atomicAdd(s + i, (double)v);
+    }
+};
+
+__device__ __forceinline__ void grad_begin(double* sg, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sg[i] = 0.0;
+    __syncthreads();
+}
+__device__ __forceinline__ void grad_end(const double* sg, int n, double* out) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (sg[i] != 0.0) atomicAdd(out + i, sg[i]);
+}
+
+// g * x per channel, 0 where the weight g is 0 (a clamped channel: its
+// derivative terms may be infinite)
+__device__ __forceinline__ float3 wmul(float3 g, float3 x) {
+    return make_float3(g.x != 0.0f ? g.x * x.x : 0.0f, g.y != 0.0f ? g.y * x.y : 0.0f, g.z != 0.0f ? g.z * x.z : 0.0f);
+}
+__device__ __forceinline__ float wdot(float3 g, float3 x) {
+    const float3 p = wmul(g, x);
+    return p.x + p.y + p.z;
+}
+
+// clampOutput (color.cuh:295-302) per channel and its derivative mask
+__device__ __forceinline__ float clamp_out(float v, float* mask) {
+    bool ok = !(isnan(v) || isinf(v));
+    *mask = (ok && v >= 0.0f && v <= 1.0e8f) ? 1.0f : 0.0f;
+    return ok ? fminf(fmaxf(v, 0.0f), 1.0e8f) : 0.0f;
+}
+
+// Texture factors of the material at a hit: albedo (sRGB-decoded texel) and
+// roughness (ORM green), 1 without a texture (material.cu:17-70).
+struct MatFactors {
+    float3 alb_tex;
+    float rough_tex, rough_eff;
+};
+__device__ __forceinline__ MatFactors mat_factors(const SceneView& s, const Surf& si) {
+    const MatRec& m = s.materials[si.material];
+    MatFactors f;
+    f.alb_tex = make_float3(1.0f, 1.0f, 1.0f);
+    f.rough_tex = 1.0f;
+    if (m.albedo_tex >= 0) {
+        float3 t = texture_eval(s, m.albedo_tex, si.uv);
+        f.alb_tex = make_float3(srgb_decode(t.x), srgb_decode(t.y), srgb_decode(t.z));
+    }
+    if (m.orm_tex >= 0) f.rough_tex = texture_eval(s, m.orm_tex, si.uv).y;
+    f.rough_eff = m.roughness * f.rough_tex;
+    return f;
+}
+
+// d(sun radiance)/d(sky parameters): the Nishita radiance towards the sun is
+// a per-frame constant (k_sky_constants), so is its Jacobian (in double
+// precision, see nishita_jacobian_d).
+__global__ void k_adjoint_constants(FrameParams F, AdjParams A) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const SkyParams& P = F.sky;
+        float3 J[SKY_PARAMS];
+        nishita_jacobian_d(P, make_float3(0.0f, P.earth_r + 1.0f, 0.0f), P.sun_dir, J);
+        for (int i = 0; i < SKY_PARAMS; ++i) A.sun_J[i] = J[i];
+    }
+}
+
+// Sky radiance and its Jacobian for a list of directions (tests and tools):
+// out[7 i] = L, out[7 i + 1 + k] = dL/d(sky parameter k).
+__global__ void k_sky_grad(SkyParams P, int n, const float3* dirs, float3* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 J[SKY_PARAMS];
+    out[7 * (size_t)i] = nishita_grad(P, make_float3(0.0f, P.earth_r + 1.0f, 0.0f), dirs[i], J);
+    for (int k = 0; k < SKY_PARAMS; ++k) out[7 * (size_t)i + 1 + k] = J[k];
+}
+
+// Pixels whose camera ray misses: every sample is sky(d) * LeSun(d).
+__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjParams A) {
+    extern __shared__ double sg[];
+    const int ng = 4 * A.nmat + ADJ_SKY_PARAMS;
+    grad_begin(sg, ng);
+    GradAcc acc{sg};
+    const SkyParams& P = F.sky;
+    const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
+    const int n = F.counts[1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = F.miss_list[i];
+        XRay r = camera_ray(F, p % F.W, p / F.W);
+        float3 J[SKY_PARAMS];
+        const float ls = le_sun(P, r.d);
+        float3 L = nishita_grad(P, obs, r.d, J) * ls;
+        float3 m;
+        float3 Lc = make_float3(clamp_out(L.x, &m.x), clamp_out(L.y, &m.y), clamp_out(L.z, &m.z));
+        const float4 a = A.adjoint[p];
+        const float3 g = make_float3(a.x, a.y, a.z) * m * ls;   // mean over identical samples
+        for (int k = 0; k < SKY_PARAMS; ++k) acc.add(4 * A.nmat + k, wdot(g, J[k]));
+        if (A.image) A.image[p] = make_float4(Lc.x, Lc.y, Lc.z, 0.0f);
+    }
+    grad_end(sg, ng, A.grad);
+}
+
+// Replay of every (sample, hit pixel) item; REC also writes each vertex's
+// frozen quantities to A.rec.
+template <bool REC>
+__device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjParams& A, GradAcc& acc, int* stack,
+                                              double* gsky) {
+    constexpr int MV = ADJ_MAX_VERTICES;
+    const SceneView& s = F.scene;
+    const SkyParams& P = F.sky;
+    const int order = F.rng_order;
+    const int nl = s.nlights;
+    const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
+    const int nhit = F.counts[0];
+    const long long total = (long long)nhit * F.nsamples;
+    const float3 sun_rad = *F.sun_radiance;
+    TraceStats st = {0, 0, 0, 0};
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int item = (int)it;
+        const int ks = item / nhit;
+        const int p = F.hit_list[item - ks * nhit];
+        const int x = p % F.W, y = p / F.W;
+        Sampler S0;
+        S0.init(x, y, F.W, F.sample0 + ks);
+        S0.get1D();   // BoxFilter::sample, result discarded (kernels.cu:397-402)
+        S0.get1D();
+        XRay cam = camera_ray(F, x, y);
+        float3 o = cam.o, d = cam.d, beta = make_float3(1.0f, 1.0f, 1.0f), prev = make_float3(0.0f, 0.0f, 0.0f);
+        float p_b = 1.0f;
+        uint32_t seed = S0.seed;
+        PrimaryRec h = F.primary[p];
+        // per vertex: throughput, added radiance, weight to the next vertex and
+        // derivatives (albedo per channel, roughness), radiance per unit sun radiance
+        float3 vb[MV], vc[MV], vw[MV], vdca[MV], vdcr[MV], vdwa[MV], vdwr[MV], vcs[MV];
+        int vm[MV];
+        AdjRec lrec[REC ? MV : 1];
+        int nv = 0;
+        bool escaped = false;
+        float3 s_end = make_float3(0.0f, 0.0f, 0.0f), b_end = s_end, d_end = s_end;
+        float3 J_end[SKY_PARAMS];
+        for (int level = 0;; ++level) {
+            if (level > 0) {
+                Hit hh = trace_closest(s, make_xray(o, d), 0.0f, __int_as_float(0x7f800000), st, stack);
+                h.t = hh.t; h.u = hh.u; h.v = hh.v; h.inst = hh.inst; h.tri = hh.tri;
+            }
+            if (h.inst < 0) {
+                escaped = true;
+                s_end = nishita_grad(P, obs, d, J_end);
+                b_end = beta;
+                d_end = d;
+                break;
+            }
+            const bool first = level == 0;
+            Sampler S;
+            S.seed = seed + (uint32_t)level;
+            Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
+            float3 c = make_float3(0.0f, 0.0f, 0.0f);
+            float3 Le = make_float3(0.0f, 0.0f, 0.0f);
+            if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
+            if (nonzero(Le)) {
+                float w_l = 1.0f;
+                if (si.light >= 0 && !first) {
+                    const LightRec& lt = s.lights[si.light];
+                    float pmf = 1.0f / (float)nl;
+                    float dist = length(si.pos - prev);
+                    float cosl = AbsDot(normalize(si.pos - prev), si.ng);
+                    float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
+                    w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
+                }
+                c = Le * w_l;
+            }
+            const float3 emit = c;
+            Bsdf bsdf = bsdf_at(s, si);
+            const MatFactors mf = mat_factors(s, si);
+            // d albedo / d parameter (0 at the demodulated first vertex, bsdf.cuh:286-288)
+            const float3 dalb = first ? make_float3(0.0f, 0.0f, 0.0f) : mf.alb_tex;
+            if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);
+            // d alpha / d roughness: alpha = (roughness * texel)^2, then regularised
+            float dal = 2.0f * mf.rough_eff * mf.rough_tex;
+            if (!first && bsdf.alpha < 0.3f) {
+                float a2 = 2.0f * bsdf.alpha;
+                dal *= (a2 > 0.1f && a2 < 0.3f) ? 2.0f : 0.0f;
+                bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
+            }
+            const float3 wo = -d;
+            float3 dca = make_float3(0.0f, 0.0f, 0.0f), dcr = dca, cs = dca;
+            int nee = 0;
+            bool nee_vis = false;
+            float3 nwi = dca, nfac = dca;
+            float ncos = 0.0f;
+            if (!(bsdf.alpha < 0.001f)) {
+                if (S.get1D() < 0.5f) {
+                    // sampleLdSun
+                    const float dsun = 149.597e9f;
+                    float3 sun_pos = P.sun_dir * dsun;
+                    float3 off;
+                    if (order == 0) {
+                        float2 a = S.get2D(0);
+                        float b = S.get1D();
+                        off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                    } else {
+                        float b = S.get1D();
+                        float2 a = S.get2D(1);
+                        off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                    }
+                    float3 target = sun_pos + (off * P.sun_radius_m);
+                    const float cf = fmaxf(0.0f, dot(P.sun_dir, (si.backface ? -1.0f : 1.0f) * si.ng));
+                    FGrad fg;
+                    float3 fcos = bsdf_f_grad(bsdf, wo, P.sun_dir, fg) * cf;
+                    nee = 1;
+                    if (nonzero(fcos) && nonzero(sun_rad) && unoccluded(F, si, target, st, stack)) {
+                        float area = PI_F * Sqr(P.sun_radius_m);
+                        float3 sn = normalize(target - sun_pos), wi = normalize(target - si.pos);
+                        float th = AbsDot(sn, -wi);
+                        float pdf = (1.0f / area) / (th / Sqr(dsun));
+                        const float k = 6.0e5f / pdf / 0.5f;
+                        c = c + fcos * sun_rad * k;
+                        cs = fcos * k;
+                        dca = fg.da * dalb * cf * sun_rad * k;
+                        dcr = fg.dal * dal * cf * sun_rad * k;
+                        nee_vis = true;
+                        nfac = make_float3(k, k, k);
+                    }
+                    nwi = mul_t(bsdf.basis, P.sun_dir);
+                    ncos = cf;
+                } else {
+                    // sampleLd
+                    float X = S.get1D();
+                    if (nl >= 1) {
+                        int li = min((int)(X * (float)nl), nl - 1);
+                        const LightRec& lt = s.lights[li];
+                        float prob = 1.0f / (float)nl;
+                        float2 uu = S.get2D(order);
+                        const InstRec& lir = s.inst[lt.inst];
+                        float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
+                        float bx, by;
+                        if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
+                        else { by = uu.y / 2.0f; bx = uu.x - by; }
+                        float bz = 1.0f - bx - by;
+                        float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
+                                                 bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
+                        float3 lp = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
+                        lp = row3(model, lp, 1.0f);
+                        float3 gn = row3(model, lt.gn, 0.0f);
+                        float pdf = 1.0f / lt.tri_area;
+                        pdf *= Sqr(length(lp - si.pos));
+                        pdf /= AbsDot(normalize(lp - si.pos), gn);
+                        float3 wi = normalize(lp - si.pos);
+                        float3 Lem = emission_of(s, lt.material, luv);
+                        nee = 2;
+                        if (!(pdf <= 0.0f || !nonzero(Lem))) {
+                            const float cf = fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
+                            FGrad fg;
+                            float3 fcos = bsdf_f_grad(bsdf, wo, wi, fg) * cf;
+                            nwi = mul_t(bsdf.basis, wi);
+                            ncos = cf;
+                            if (nonzero(fcos) && unoccluded(F, si, lp, st, stack)) {
+                                float p_l = prob * pdf;
+                                float pb = bsdf.pdf(wo, wi);
+                                float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
+                                const float3 k = Lem * (w_l / p_l / (1.0f - 0.5f));
+                                c = c + fcos * k;
+                                dca = fg.da * dalb * cf * k;
+                                dcr = fg.dal * dal * cf * k;
+                                nee_vis = true;
+                                nfac = k;
+                            }
+                        }
+                    }
+                }
+            }
+            vb[nv] = beta;
+            vc[nv] = c;
+            vdca[nv] = dca;
+            vdcr[nv] = dcr;
+            vcs[nv] = cs;
+            vm[nv] = si.material;
+            vw[nv] = vdwa[nv] = vdwr[nv] = make_float3(0.0f, 0.0f, 0.0f);
+            if (REC) {
+                AdjRec& r = lrec[nv];
+                r.item = item;
+                r.vertex = nv;
+                r.material = si.material;
+                r.flags = (first ? ADJ_FIRST : 0) | (si.backface ? ADJ_BACKFACE : 0) | (nee_vis ? ADJ_NEE_UNOCCLUDED : 0);
+                r.lobe = LOBE_NONE;
+                r.nee = nee;
+                r.pixel = p;
+                r.alb_tex[0] = mf.alb_tex.x; r.alb_tex[1] = mf.alb_tex.y; r.alb_tex[2] = mf.alb_tex.z;
+                r.rough_tex = mf.rough_tex;
+                r.metallic = bsdf.metallic;
+                r.transmission = bsdf.transmission;
+                r.ior = bsdf.ior;
+                r.eta = 1.0f;
+                float3 lwo = mul_t(bsdf.basis, wo);
+                r.wo[0] = lwo.x; r.wo[1] = lwo.y; r.wo[2] = lwo.z;
+                r.cosw = 0.0f; r.pdf = 0.0f; r.rr = 1.0f;
+                r.wi[0] = r.wi[1] = r.wi[2] = r.wm[0] = r.wm[1] = r.wm[2] = 0.0f;
+                r.nwi[0] = nwi.x; r.nwi[1] = nwi.y; r.nwi[2] = nwi.z;
+                r.ncos = ncos;
+                r.nfac[0] = nfac.x; r.nfac[1] = nfac.y; r.nfac[2] = nfac.z;
+                r.emit[0] = emit.x; r.emit[1] = emit.y; r.emit[2] = emit.z;
+                r.miss[0] = r.miss[1] = r.miss[2] = 0.0f;
+                r.pad0 = 0;
+                r.pad1 = r.pad2 = r.pad3 = r.pad4 = 0.0f;
+            }
+            const int vi = nv++;
+            if (level == F.max_depth || nv == MV) break;
+            float2 uu, X;
+            if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
+            else { X = S.get2D(1); uu = S.get2D(1); }
+            FGrad sg;
+            SampleInfo sinfo;
+            BsdfSample bs = bsdf_sample_grad(bsdf, wo, uu, X, sg, sinfo);
+            if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) break;
+            const float cw = AbsDot(si.ng, bs.wi);
+            float3 w = bs.f * cw / bs.pdf;
+            float3 dwa = sg.da * dalb * cw / bs.pdf, dwr = sg.dal * dal * cw / bs.pdf;
+            beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
+            p_b = bsdf.pdf(wo, bs.wi);
+            o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+            float rr = 1.0f;
+            bool killed = false;
+            float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
+            if (mx < 1.0f && level >= 1) {
+                float q = fmaxf(0.0f, 1.0f - mx);
+                if (S.get1D() < q) killed = true;
+                else {
+                    beta = beta / (1.0f - q);
+                    rr = 1.0f / (1.0f - q);
+                }
+            }
+            vw[vi] = w * rr;
+            vdwa[vi] = dwa * rr;
+            vdwr[vi] = dwr * rr;
+            if (REC) {
+                AdjRec& r = lrec[vi];
+                r.lobe = sinfo.lobe;
+                r.eta = sinfo.eta;
+                r.wi[0] = sinfo.wi.x; r.wi[1] = sinfo.wi.y; r.wi[2] = sinfo.wi.z;
+                r.wm[0] = sinfo.wm.x; r.wm[1] = sinfo.wm.y; r.wm[2] = sinfo.wm.z;
+                r.cosw = cw;
+                r.pdf = bs.pdf;
+                r.rr = killed ? 0.0f : rr;
+                r.pad0 = sinfo.tir | (sinfo.inside << 1);
+            }
+            if (killed || !nonzero(beta)) break;
+            prev = si.pos;
+            d = bs.wi;
+            seed = S.seed;
+        }
+        // the sample's radiance (the forward's sum), its clamp and the weight
+        // dLoss/d(sample) = dLoss/dimage / nsamples on unclamped channels
+        float3 L = make_float3(0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < nv; ++k) L = L + vb[k] * vc[k];
+        if (escaped) L = L + b_end * s_end;
+        float3 msk;
+        const float3 Lc = make_float3(clamp_out(L.x, &msk.x), clamp_out(L.y, &msk.y), clamp_out(L.z, &msk.z));
+        const float inv_n = 1.0f / (float)F.nsamples;
+        const float4 a = A.adjoint[p];
+        const float3 g = make_float3(a.x, a.y, a.z) * msk * inv_n;
+        if (A.image) {
+            atomicAdd(&A.image[p].x, Lc.x * inv_n);
+            atomicAdd(&A.image[p].y, Lc.y * inv_n);
+            atomicAdd(&A.image[p].z, Lc.z * inv_n);
+        }
+        // reverse sweep: R = radiance from vertex k on, per unit throughput at k
+        float3 R = escaped ? s_end : make_float3(0.0f, 0.0f, 0.0f);
+        if (nonzero(g)) {
+            if (escaped) {
+                const float3 gb = wmul(g, b_end);
+                for (int i = 0; i < SKY_PARAMS; ++i) gsky[i] += wdot(gb, J_end[i]);
+            }
+            for (int k = nv - 1; k >= 0; --k) {
+                const float3 gb = wmul(g, vb[k]);
+                const float3 ta = wmul(gb, vdca[k] + wmul(vdwa[k], R));
+                const int m4 = 4 * vm[k];
+                acc.add(m4 + 0, ta.x);
+                acc.add(m4 + 1, ta.y);
+                acc.add(m4 + 2, ta.z);
+                acc.add(m4 + 3, wdot(gb, vdcr[k] + wmul(vdwr[k], R)));
+                if (nonzero(vcs[k])) {
+                    const float3 gs = wmul(gb, vcs[k]);
+                    for (int i = 0; i < SKY_PARAMS; ++i) gsky[i] += wdot(gs, A.sun_J[i]);
+                }
+                R = vc[k] + vw[k] * R;
+            }
+        }
+        if (REC && nv > 0) {
+            lrec[nv - 1].flags |= ADJ_LAST | (escaped ? ADJ_ESCAPED : 0);
+            lrec[nv - 1].miss[0] = d_end.x;
+            lrec[nv - 1].miss[1] = d_end.y;
+            lrec[nv - 1].miss[2] = d_end.z;
+            const int base = atomicAdd(A.rec_count, nv);
+            for (int k = 0; k < nv; ++k) {
+                lrec[k].g[0] = g.x;
+                lrec[k].g[1] = g.y;
+                lrec[k].g[2] = g.z;
+                if (base + k < A.max_rec) A.rec[base + k] = lrec[k];
+            }
+        }
+    }
+}
+
+template <bool REC>
+__device__ __forceinline__ void adjoint_block(const FrameParams& F, const AdjParams& A) {
+    extern __shared__ double sg[];
+    const int ng = 4 * A.nmat + ADJ_SKY_PARAMS;
+    grad_begin(sg, ng);
+    GradAcc acc{sg};
+    int stack[STACK_WORDS];
+    double gsky[SKY_PARAMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    adjoint_items<REC>(F, A, acc, stack, gsky);
+    for (int i = 0; i < SKY_PARAMS; ++i) {   // one shared add per warp per sky parameter
+        double v = gsky[i];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sg + 4 * A.nmat + i, v);
+    }
+    grad_end(sg, ng, A.grad);
+}
+
+__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint(FrameParams F, AdjParams A) { adjoint_block<false>(F, A); }
+__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_rec(FrameParams F, AdjParams A) { adjoint_block<true>(F, A); }
+
+}  // namespace kpt

@@ -124,6 +124,11 @@ struct kpt_context {
     DBuf<PrimaryRec> primary, hits;
     DBuf<int> hit_list, hit_index, miss_list, counts, level_counts;
     DBuf<int> fetch;   // queue counter of the ray-batch entry points
+    // adjoint: d(sun radiance)/d(sky), host-call staging, record counter
+    DBuf<float3> sun_J;
+    DBuf<float> adj_in, adj_image;
+    DBuf<double> adj_grad;
+    DBuf<int> rec_count;
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2];
     DBuf<ShadowRec> shadow;
@@ -242,6 +247,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->miss_list.release(); c->counts.release(); c->level_counts.release(); c->pixel_sky.release();
     c->radiance.release(); c->sky_queue.release(); c->paths[0].release(); c->paths[1].release();
     c->shadow.release(); c->fetch.release();
+    c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return KPT_OK;
@@ -731,7 +737,9 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
     c->launches += 3;
     const int shade_block = c->tuning.shade_block > 0 ? c->tuning.shade_block : PATH_BLOCK;
-    const int g_shade = persistent_grid(c, (const void*)k_shade, shade_block);
+    const bool wide = shade_block > PATH_BLOCK;
+    const void* shade_fn = wide ? (const void*)k_shade_wide : (const void*)k_shade;
+    const int g_shade = persistent_grid(c, shade_fn, shade_block);
     const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
     const int g_shd = persistent_grid(c, (const void*)k_shadow, TRACE_BLOCK);
     // every pixel may hit: the last waves find no work when fewer do
@@ -744,7 +752,8 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
             }
             stage_mark(c, KPT_STAGE_SHADE);
-            k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
+            if (wide) k_shade_wide<<<g_shade, shade_block, 0, s>>>(F, l, w0);
+            else k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
             stage_mark(c, KPT_STAGE_SHADOW);
             k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
             c->launches += l > 0 ? 3 : 2;
@@ -1144,6 +1153,113 @@ kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
         return fail(KPT_ERR_INVALID, "kpt_set_tuning: shade_block must be 0, 64, 128 or 256");
     c->tuning = *t;
     if (c->tuning.shade_block == 0) c->tuning.shade_block = PATH_BLOCK;
+    return KPT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// path-replay adjoint
+
+static int adjoint_params(const kpt_context* c) { return 4 * (int)c->materials.size() + ADJ_SKY_PARAMS; }
+
+static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const float* adjoint, double* grad,
+                              float* image, AdjRec* rec, int max_rec) {
+    kpt_status st = ready(c);
+    if (st != KPT_OK) return st;
+    if (nsamples <= 0 || sample0 < 0 || !adjoint || !grad)
+        return fail(KPT_ERR_INVALID, "kpt_adjoint: bad arguments");
+    if (c->settings.max_depth + 1 > ADJ_MAX_VERTICES)
+        return fail(KPT_ERR_INVALID, "kpt_adjoint: max_depth above 16");
+    const int ng = adjoint_params(c);
+    const size_t smem = sizeof(double) * (size_t)ng;
+    if (smem > 200 * 1024) return fail(KPT_ERR_INVALID, "kpt_adjoint: too many materials");
+    st = ensure_work(c, nsamples);
+    if (st != KPT_OK) return st;
+    KPT_CUDA(c->sun_J.ensure(ADJ_SKY_PARAMS));
+    KPT_CUDA(c->rec_count.ensure(1));
+    FrameParams F = frame_params(c, sample0, nsamples);
+    AdjParams A{};
+    A.adjoint = reinterpret_cast<const float4*>(adjoint);
+    A.grad = grad;
+    A.image = reinterpret_cast<float4*>(image);
+    A.sun_J = c->sun_J.p;
+    A.rec = rec;
+    A.rec_count = c->rec_count.p;
+    A.max_rec = max_rec;
+    A.nmat = (int)c->materials.size();
+    cudaStream_t s = c->stream;
+    const int np = c->W * c->H;
+    KPT_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * ng, s));
+    if (image) KPT_CUDA(cudaMemsetAsync(image, 0, sizeof(float4) * (size_t)np, s));
+    KPT_CUDA(cudaMemsetAsync(c->rec_count.p, 0, sizeof(int), s));
+    KPT_CUDA(cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s));
+    const void* kern = rec ? (const void*)k_adjoint_rec : (const void*)k_adjoint;
+    for (const void* k : {kern, (const void*)k_adjoint_miss})
+        KPT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    KPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PATH_BLOCK, smem));
+    const int grid = std::max(1, per_sm) * c->sm_count;
+    k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
+    k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
+    k_adjoint_constants<<<1, 32, 0, s>>>(F, A);
+    k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);
+    if (rec) k_adjoint_rec<<<grid, PATH_BLOCK, smem, s>>>(F, A);
+    else k_adjoint<<<grid, PATH_BLOCK, smem, s>>>(F, A);
+    c->launches += 5;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+kpt_status kpt_adjoint_param_count(kpt_context* c, int* n) {
+    if (!c || !n) return fail(KPT_ERR_INVALID, "kpt_adjoint_param_count: null argument");
+    *n = adjoint_params(c);
+    return KPT_OK;
+}
+
+kpt_status kpt_adjoint_device(kpt_context* c, int sample0, int nsamples, const float* adjoint, double* grad,
+                              float* image) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    return adjoint_run(c, sample0, nsamples, adjoint, grad, image, nullptr, 0);
+}
+
+kpt_status kpt_adjoint(kpt_context* c, int sample0, int nsamples, const float* adjoint, double* grad, float* image) {
+    if (!c || !adjoint || !grad) return fail(KPT_ERR_INVALID, "kpt_adjoint: null argument");
+    KPT_CUDA(cudaSetDevice(c->device));
+    const size_t np = (size_t)c->W * c->H;
+    const int ng = adjoint_params(c);
+    KPT_CUDA(c->adj_in.ensure(4 * np));
+    KPT_CUDA(c->adj_grad.ensure(ng));
+    if (image) KPT_CUDA(c->adj_image.ensure(4 * np));
+    KPT_CUDA(cudaMemcpyAsync(c->adj_in.p, adjoint, sizeof(float) * 4 * np, cudaMemcpyHostToDevice, c->stream));
+    kpt_status st = adjoint_run(c, sample0, nsamples, c->adj_in.p, c->adj_grad.p, image ? c->adj_image.p : nullptr,
+                                nullptr, 0);
+    if (st != KPT_OK) return st;
+    KPT_CUDA(cudaMemcpyAsync(grad, c->adj_grad.p, sizeof(double) * ng, cudaMemcpyDeviceToHost, c->stream));
+    if (image)
+        KPT_CUDA(cudaMemcpyAsync(image, c->adj_image.p, sizeof(float) * 4 * np, cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    return KPT_OK;
+}
+
+int kpt_adjoint_record_size(void) { return (int)sizeof(AdjRec); }
+
+kpt_status kpt_sky_grad_device(kpt_context* c, int n, const float* dirs, float* rgb) {
+    if (!c || n < 0 || (n > 0 && (!dirs || !rgb))) return fail(KPT_ERR_INVALID, "kpt_sky_grad_device: bad arguments");
+    KPT_CUDA(cudaSetDevice(c->device));
+    if (n == 0) return KPT_OK;
+    k_sky_grad<<<(n + 127) / 128, 128, 0, c->stream>>>(sky_params(c->env), n, (const float3*)dirs, (float3*)rgb);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
+}
+
+kpt_status kpt_adjoint_records_device(kpt_context* c, int sample0, int nsamples, const float* adjoint, double* grad,
+                                      void* records, int max_records, int* count) {
+    if (!c || !records || max_records <= 0 || !count)
+        return fail(KPT_ERR_INVALID, "kpt_adjoint_records_device: bad arguments");
+    kpt_status st = adjoint_run(c, sample0, nsamples, adjoint, grad, nullptr, static_cast<AdjRec*>(records), max_records);
+    if (st != KPT_OK) return st;
+    KPT_CUDA(cudaMemcpyAsync(count, c->rec_count.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
     return KPT_OK;
 }
 

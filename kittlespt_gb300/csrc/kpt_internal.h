@@ -78,6 +78,41 @@ struct FrameParams {
     int cap;
 };
 
+// ---------------------------------------------------------------------------
+// path-replay adjoint (kpt_adjoint.cu)
+
+constexpr int ADJ_MAX_VERTICES = 17;   // max_depth <= 16
+constexpr int ADJ_SKY_PARAMS = 6;      // Rayleigh r, g, b, Mie, Rayleigh height, Mie height
+
+// One path vertex as the replay saw it, everything that is held fixed (for
+// the FP64 oracle's finite differences): 192 B.
+enum { ADJ_FIRST = 1, ADJ_BACKFACE = 2, ADJ_LAST = 4, ADJ_ESCAPED = 8, ADJ_NEE_UNOCCLUDED = 16 };
+struct __align__(16) AdjRec {
+    int item, vertex, material, flags;
+    int lobe, nee, pixel, pad0;       // sampled lobe (LOBE_*), light sample (0 none, 1 sun, 2 light)
+    float alb_tex[3], rough_tex;      // texture factors of albedo and roughness
+    float metallic, transmission, ior, eta;
+    float wo[3], cosw;                // local wo; |ng . wi| of the sampled direction
+    float wi[3], pdf;                 // local sampled direction and its pdf
+    float wm[3], rr;                  // local microfacet normal of the sample; roulette factor 1/(1-q)
+    float nwi[3], ncos;               // local light-sample direction and its cosine factor
+    float nfac[3], pad1;              // light sample: sun 6e5/(pdf 0.5); area light Le w/(p 0.5)
+    float emit[3], pad2;              // emission term Le * w (no parameter)
+    float g[3], pad3;                 // adjoint weight of the sample (masked by the clamp)
+    float miss[3], pad4;              // direction of the escaping ray (ADJ_ESCAPED)
+};
+
+struct AdjParams {
+    const float4* adjoint;   // [H*W] dLoss/d(mean clamped radiance), rgb
+    double* grad;            // [4 * nmat + ADJ_SKY_PARAMS]
+    float4* image;           // [H*W] mean clamped radiance, may be null
+    float3* sun_J;           // [ADJ_SKY_PARAMS] d(sun radiance)/d(sky parameters)
+    AdjRec* rec;             // frozen-path records, may be null
+    int* rec_count;
+    int max_rec;
+    int nmat;
+};
+
 // Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
 __device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
     float3 c0, c1;
@@ -98,11 +133,18 @@ __device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
 // kernels (kpt_path.cu, fast maths)
 __global__ void k_primary(FrameParams F);
 __global__ void k_primary_sky(FrameParams F);
-__global__ void k_shade(FrameParams F, int level, long long wave0);
+__global__ void k_shade(FrameParams F, int level, long long wave0);        // blocks of <= PATH_BLOCK threads
+__global__ void k_shade_wide(FrameParams F, int level, long long wave0);   // blocks of <= SHADE_MAX_BLOCK threads
 __global__ void k_extend(FrameParams F, int level);
 __global__ void k_shadow(FrameParams F, int level);
 __global__ void k_sky_queue(FrameParams F);
 __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
+// kpt_adjoint.cu (fast maths)
+__global__ void k_adjoint_constants(FrameParams F, AdjParams A);
+__global__ void k_sky_grad(SkyParams P, int n, const float3* dirs, float3* out);
+__global__ void k_adjoint_miss(FrameParams F, AdjParams A);
+__global__ void k_adjoint(FrameParams F, AdjParams A);
+__global__ void k_adjoint_rec(FrameParams F, AdjParams A);   // also writes the frozen-path records
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
 __global__ void k_accumulate(FrameParams F);
 __global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out);

@@ -317,7 +317,7 @@ __device__ __forceinline__ float3 xpoint(float3 o, float t, float3 d) {
 }
 
 // Radiance of the sky seen from `o` along `d`.
-__device__ __noinline__ float3 nishita(const SkyParams& P, float3 o, float3 d) {
+static __device__ __noinline__ float3 nishita(const SkyParams& P, float3 o, float3 d) {
     float tmin = 0.0f, tmax = __int_as_float(0x7f800000);
     {
         float te, tx;

@@ -282,6 +282,21 @@ class Renderer:
     def sky_device(self, n, dirs_ptr, out_ptr):
         K.check(self._L.kpt_sky_device(self._ctx, n, dirs_ptr, out_ptr))
 
+    # -- path-replay adjoint (no reference counterpart) -----------------------
+    def adjoint(self, sample0: int, nsamples: int, adjoint: np.ndarray, want_image: bool = False):
+        """dLoss/dtheta for dLoss/dimage = adjoint ([H][W][4] float32, host);
+        returns (grad float64 in adjoint_param_names order, image or None)."""
+        n = C.c_int()
+        K.check(self._L.kpt_adjoint_param_count(self._ctx, C.byref(n)))
+        a = np.ascontiguousarray(adjoint, np.float32).reshape(-1)
+        if a.size != self.width * self.height * 4:
+            raise ValueError("adjoint must be [H][W][4]")
+        g = np.zeros(n.value, np.float64)
+        img = np.zeros((self.height, self.width, 4), np.float32) if want_image else None
+        K.check(self._L.kpt_adjoint(self._ctx, sample0, nsamples, K.fptr(a), g.ctypes.data_as(C.POINTER(C.c_double)),
+                                    K.fptr(img.reshape(-1)) if want_image else None))
+        return g, img
+
     # -- launch parameters (no reference counterpart) -------------------------
     def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0):
         t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block)
@@ -343,3 +358,17 @@ class Batch:
                                            K.fptr(ms)))
         return ({"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block},
                 int(lanes[0]), float(ms[0]))
+
+
+# -- path-replay adjoint (no reference counterpart) ----------------------------
+
+SKY_PARAM_NAMES = ("rayleigh_r", "rayleigh_g", "rayleigh_b", "mie", "rayleigh_height", "mie_height")
+
+
+def adjoint_param_names(nmat: int):
+    """Order of kpt_adjoint's gradient: per material (albedo r, g, b,
+    roughness), then the sky."""
+    names = []
+    for m in range(nmat):
+        names += [f"m{m}.albedo_r", f"m{m}.albedo_g", f"m{m}.albedo_b", f"m{m}.roughness"]
+    return names + list(SKY_PARAM_NAMES)

@@ -74,6 +74,9 @@ def lib(prefix: str = "orc"):
                                 C.c_float, _f]
     g("metering_weights").argtypes = [C.c_int, C.c_int, _f]
     if prefix == "orc":
+        g("sky_double").argtypes = [C.c_int, _v, _v, _v, _v]
+        g("adjoint_estimate").restype = C.c_int
+        g("adjoint_estimate").argtypes = [_v, C.c_int, _v, _v, _v, _v, _v]
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _u64]
         g("exposure").argtypes = [_u64, _v, C.c_float, C.c_float, _f]
         g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
@@ -279,3 +282,32 @@ def exposure_scalar(expo) -> float:
     N = float(expo["aperture"])
     lavg = (10.0 / 0.65) * ((N * N) / (float(expo["iso"]) * float(expo["shutter"])))
     return float(np.float32(0.18 / lavg))
+
+
+def sky_double(dirs, sky, fixed):
+    """Nishita radiance in double precision for [n][3] directions (sky and
+    fixed as for adjoint_estimate)."""
+    L = lib("orc")
+    d = np.ascontiguousarray(dirs, np.float32)
+    s = np.ascontiguousarray(sky, np.float64)
+    f = np.ascontiguousarray(fixed, np.float64)
+    out = np.zeros((d.shape[0], 3), np.float64)
+    L.orc_sky_double(d.shape[0], _ptr(d), _ptr(s), _ptr(f), _ptr(out))
+    return out
+
+
+def adjoint_estimate(records: bytes, n: int, albedo, roughness, sky, fixed):
+    """E(theta) = sum over samples of g . L(theta) on the adjoint's frozen
+    path records, in double precision (adjoint_oracle.cpp).  albedo [M][3],
+    roughness [M], sky (Rayleigh r, g, b, Mie, Rayleigh height, Mie height),
+    fixed (sun direction xyz, sun emission factor, Mie absorption, earth
+    radius, atmosphere radius).  Returns (E, number of samples)."""
+    L = lib("orc")
+    buf = np.frombuffer(records, np.uint8)
+    a = np.ascontiguousarray(albedo, np.float64).reshape(-1)
+    r = np.ascontiguousarray(roughness, np.float64)
+    s = np.ascontiguousarray(sky, np.float64)
+    f = np.ascontiguousarray(fixed, np.float64)
+    out = np.zeros(1, np.float64)
+    items = L.orc_adjoint_estimate(_ptr(buf), n, _ptr(a), _ptr(r), _ptr(s), _ptr(f), _ptr(out))
+    return float(out[0]), int(items)
