@@ -411,6 +411,112 @@ def run_batch(args):
     print(json.dumps(out))
 
 
+ADJ_W, ADJ_H, ADJ_SPP, ADJ_DEPTH = 512, 512, 32, 6
+
+
+def adjoint_scene(seed=7):
+    """The differentiation workload: the sphere-pair scene at 512 x 512, depth
+    6, materials with albedo U(0.1, 0.9)^3 and roughness U(0.05, 1), Rayleigh
+    and Mie scale heights 8 km and 1.2 km."""
+    from kittlespt_gb300 import scenes as S
+    sc = S.scene_small(ADJ_W, ADJ_H, ADJ_SPP, ADJ_DEPTH)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mats = sc.materials.copy()
+    for m in mats:
+        m["albedo"] = rng.uniform(0.1, 0.9, 3)
+        m["roughness"] = rng.uniform(0.05, 1.0)
+    sc.materials = mats
+    env = sc.env.copy()
+    env["rayleigh_height"], env["mie_height"] = 8000.0, 1200.0
+    sc.env = env
+    return sc
+
+
+def run_adjoint(args):
+    """Gradient evaluations per second of the L2 image loss: forward image
+    (mean of 32 samples per pixel), the loss's adjoint image and the
+    path-replay adjoint, all on the device (CUDA events on the library's
+    stream), from an initial guess within +-20% of the parameters that
+    rendered the target (target samples: seed 7, i.e. sample indices
+    7*32 .. 7*32+31)."""
+    import torch
+    from kittlespt_gb300 import build as B
+    B.build()
+    from kittlespt_gb300 import _lib as K
+    from kittlespt_gb300.renderer import Renderer
+    sc = adjoint_scene()
+    r = Renderer(0)
+    r.initialize()
+    r.load_scene(sc)
+    nmat = len(sc.materials)
+    stream = torch.cuda.ExternalStream(r.stream(), device=0)
+    buf = torch.zeros((ADJ_SPP, ADJ_H, ADJ_W, 4), dtype=torch.float32, device="cuda")
+    n = C.c_int()
+    K.check(r._L.kpt_adjoint_param_count(r.ctx, C.byref(n)))
+    grad = torch.zeros(n.value, dtype=torch.float64, device="cuda")
+
+    def apply(theta):
+        for k, m in enumerate(sc.materials):
+            mm = m.copy()
+            mm["albedo"], mm["roughness"] = theta[4 * k:4 * k + 3], theta[4 * k + 3]
+            r.set_material(k, mm)
+        e = sc.env.copy()
+        e["rayleigh"], e["mie"] = theta[-6:-3], theta[-3]
+        e["rayleigh_height"], e["mie_height"] = theta[-2], theta[-1]
+        r.set_procedural_environment_data(e)
+
+    theta_true = []
+    for m in sc.materials:
+        theta_true += [float(x) for x in m["albedo"]] + [float(m["roughness"])]
+    e = sc.env
+    theta_true += [float(x) for x in e["rayleigh"]] + [float(e["mie"]), float(e["rayleigh_height"]),
+                                                        float(e["mie_height"])]
+    theta_true = np.array(theta_true)
+    rng = np.random.Generator(np.random.PCG64(7))
+    theta0 = theta_true * (1.0 + rng.uniform(-0.2, 0.2, theta_true.size))
+    theta0[:4 * nmat] = np.clip(theta0[:4 * nmat], 0.02, 0.98)
+    with torch.cuda.stream(stream):
+        r.render_samples_device(7 * ADJ_SPP, ADJ_SPP, buf.data_ptr())
+        target = buf.mean(dim=0).clone()
+        apply(theta0)
+        adj = torch.zeros((ADJ_H, ADJ_W, 4), dtype=torch.float32, device="cuda")
+
+        def gradient():
+            r.render_samples_device(0, ADJ_SPP, buf.data_ptr())
+            img = buf.mean(dim=0)
+            adj[..., :3] = 2.0 * (img[..., :3] - target[..., :3])
+            K.check(r._L.kpt_adjoint_device(r.ctx, 0, ADJ_SPP, adj.data_ptr(), grad.data_ptr(), None))
+            return img
+
+        for _ in range(args.warmup):
+            gradient()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            img = gradient()
+        ev[1].record(stream)
+        K.check(r._L.kpt_adjoint_device(r.ctx, 0, ADJ_SPP, adj.data_ptr(), grad.data_ptr(), None))
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    adj_ms = ev[1].elapsed_time(ev[2])
+    loss = float(((img[..., :3] - target[..., :3]) ** 2).sum())
+    g = grad.cpu().numpy()
+    r.shutdown()
+    out = {"metric": "adjoint gradient evaluations/s (L2 image loss, 512x512, 32 spp, depth 6)",
+           "value": 1e3 / ms, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded sphere-pair scene with random materials)",
+           "config": {"workload": "adjoint_sphere_pair_512_32spp_depth6", "width": ADJ_W, "height": ADJ_H,
+                      "spp": ADJ_SPP, "max_depth": ADJ_DEPTH, "parameters": int(n.value),
+                      "samples_per_gradient": ADJ_W * ADJ_H * ADJ_SPP},
+           "adjoint_ms": adj_ms, "forward_and_loss_ms": ms - adj_ms,
+           "Msamples_per_s_replayed": ADJ_W * ADJ_H * ADJ_SPP / adj_ms / 1e3,
+           "loss": loss, "grad_norm": float(np.linalg.norm(g * np.abs(theta0)))}
+    print(json.dumps(out))
+
+
 def run_profile_case(spec):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
     small case that ncu captures of single kernels run on."""
@@ -434,8 +540,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
-                    help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "adjoint"],
+                    help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one; "
+                         "adjoint: gradient evaluations/s of the path-replay adjoint")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
     args = ap.parse_args()
@@ -446,6 +553,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gpu(args)
 
