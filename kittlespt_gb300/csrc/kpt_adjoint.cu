@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjP
         float3 J[SKY_PARAMS];
         const float ls = le_sun(P, r.d);
         float3 L = nishita_grad(P, obs, r.d, J) * ls;
+        if (fabsf(r.d.y) < 0.05f || dot(r.d, P.sun_dir) > 0.995f) nishita_jacobian_d(P, obs, r.d, J);
         float3 m;
         float3 Lc = make_float3(clamp_out(L.x, &m.x), clamp_out(L.y, &m.y), clamp_out(L.z, &m.z));
         const float4 a = A.adjoint[p];
@@ -172,6 +173,10 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
             if (h.inst < 0) {
                 escaped = true;
                 s_end = nishita_grad(P, obs, d, J_end);
+                // near the sun (Mie forward peak) and the horizon the
+                // single-precision march's derivatives are ill-conditioned:
+                // there the Jacobian is evaluated in double
+                if (fabsf(d.y) < 0.05f || dot(d, P.sun_dir) > 0.995f) nishita_jacobian_d(P, obs, d, J_end);
                 b_end = beta;
                 d_end = d;
                 break;

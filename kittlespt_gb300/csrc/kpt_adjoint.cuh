@@ -385,7 +385,7 @@ static __device__ __noinline__ float3 nishita_grad(const SkyParams& P, float3 o,
         if (te > tmin && te > 0.0f) tmin = te;
         if (tx < tmax) tmax = tx;
     }
-    const float step = __fdiv_rn(xs(tmax, tmin), 16.0f);
+    const float step = xm(xs(tmax, tmin), 0.0625f);
     const float3 tR = make_float3(xa(P.sigma_r.x, 0.0f), xa(P.sigma_r.y, 0.0f), xa(P.sigma_r.z, 0.0f));
     const float tM = xa(P.sigma_m, P.sigma_am);
     const float half = xm(step, 0.5f);
@@ -400,8 +400,8 @@ static __device__ __noinline__ float3 nishita_grad(const SkyParams& P, float3 o,
     for (int i = 0; i < 16; ++i) {
         float3 sp = xpoint(o, xa(t, half), d);
         float alt = xs(__fsqrt_rn(xdot(sp, sp)), P.earth_r);
-        float pR = xm(expf(__fdiv_rn(-alt, P.h_r)), step);
-        float pM = xm(expf(__fdiv_rn(-alt, P.h_m)), step);
+        float pR = xm(expf(-alt * P.inv_h_r), step);
+        float pM = xm(expf(-alt * P.inv_h_m), step);
         float dpR = pR * alt * ihr2, dpM = pM * alt * ihm2;   // d/d h of exp(-alt / h) * step
         oR = xa(oR, pR);
         oM = xa(oM, pM);
@@ -409,7 +409,7 @@ static __device__ __noinline__ float3 nishita_grad(const SkyParams& P, float3 o,
         doM += dpM;
         float lte, ltx;
         sphere_hit(sp, P.sun_dir, P.atm_r, &lte, &ltx);
-        float lstep = __fdiv_rn(ltx, 8.0f);
+        float lstep = xm(ltx, 0.125f);
         float lhalf = xm(lstep, 0.5f);
         float lt = 0.0f, lR = 0.0f, lM = 0.0f, dlR = 0.0f, dlM = 0.0f;
         int j;
@@ -418,7 +418,7 @@ static __device__ __noinline__ float3 nishita_grad(const SkyParams& P, float3 o,
             float3 spl = xpoint(sp, xa(lt, lhalf), P.sun_dir);
             float altl = xs(__fsqrt_rn(xdot(spl, spl)), P.earth_r);
             if (altl < 0.0f) break;
-            float eR = xm(expf(__fdiv_rn(-altl, P.h_r)), lstep), eM = xm(expf(__fdiv_rn(-altl, P.h_m)), lstep);
+            float eR = xm(expf(-altl * P.inv_h_r), lstep), eM = xm(expf(-altl * P.inv_h_m), lstep);
             lR = xa(lR, eR);
             lM = xa(lM, eM);
             dlR += eR * altl * ihr2;

@@ -75,6 +75,10 @@ struct kpt_context {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    // second stream of the frame graph: the shadow rays of a level run on it
+    // while the next level's extension rays run on `stream`
+    cudaStream_t side = nullptr;
+    std::vector<cudaEvent_t> ev_fork, ev_join;
     uint64_t launches = 0;
 
     // host scene
@@ -207,6 +211,7 @@ kpt_status kpt_create(int device, kpt_context** out) {
     c->device = device;
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;
         return fail(KPT_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
@@ -248,6 +253,9 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->radiance.release(); c->sky_queue.release(); c->paths[0].release(); c->paths[1].release();
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
+    for (auto* v : {&c->ev_fork, &c->ev_join})
+        for (cudaEvent_t e : *v) cudaEventDestroy(e);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return KPT_OK;
@@ -642,6 +650,8 @@ static SkyParams sky_params(const kpt_environment& e) {
     P.sigma_am = e.mie_absorption;
     P.h_r = e.rayleigh_height;
     P.h_m = e.mie_height;
+    P.inv_h_r = (float)(1.0 / (double)e.rayleigh_height);
+    P.inv_h_m = (float)(1.0 / (double)e.mie_height);
     P.earth_r = 6378137.0f;
     P.atm_r = 6438137.0f;
     P.cos_half_sun = cosf(e.sun_angular_diameter / 2.0f);   // LeSun (integrator.cuh:137)
@@ -694,6 +704,13 @@ static kpt_status ensure_work(kpt_context* c, int nsamples) {
     KPT_CUDA(c->hits.ensure(cap));
     KPT_CUDA(c->shadow.ensure(cap));
     KPT_CUDA(c->level_counts.ensure((size_t)LEVEL_WORDS * (c->settings.max_depth + 2)));
+    while (c->ev_fork.size() < (size_t)c->settings.max_depth + 1) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        KPT_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+        KPT_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        c->ev_fork.push_back(a);
+        c->ev_join.push_back(b);
+    }
     c->wave_cap = cap;
     KPT_CUDA(c->primary.ensure(np));
     KPT_CUDA(c->hit_list.ensure(np));
@@ -744,20 +761,33 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     const int g_shd = persistent_grid(c, (const void*)k_shadow, TRACE_BLOCK);
     // every pixel may hit: the last waves find no work when fewer do
     const long long items = (long long)np * F.nsamples;
+    // the shadow rays of level l and the extension rays of level l + 1 read
+    // what k_shade(l) wrote and write disjoint buffers: they run on two
+    // streams, joined before k_shade(l + 1); serial when stages are timed
+    const bool fork = c->tf == nullptr && c->ev_fork.size() >= (size_t)D + 1;
     for (long long w0 = 0; w0 < items; w0 += F.cap) {
         cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
         for (int l = 0; l <= D; ++l) {
             if (l > 0) {
                 stage_mark(c, KPT_STAGE_EXTEND);
                 k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
+                if (fork) cudaStreamWaitEvent(s, c->ev_join[l - 1], 0);
             }
             stage_mark(c, KPT_STAGE_SHADE);
             if (wide) k_shade_wide<<<g_shade, shade_block, 0, s>>>(F, l, w0);
             else k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
             stage_mark(c, KPT_STAGE_SHADOW);
-            k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
+            if (fork) {
+                cudaEventRecord(c->ev_fork[l], s);
+                cudaStreamWaitEvent(c->side, c->ev_fork[l], 0);
+                k_shadow<<<g_shd, TRACE_BLOCK, 0, c->side>>>(F, l);
+                cudaEventRecord(c->ev_join[l], c->side);
+            } else {
+                k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
+            }
             c->launches += l > 0 ? 3 : 2;
         }
+        if (fork) cudaStreamWaitEvent(s, c->ev_join[D], 0);
     }
     stage_mark(c, KPT_STAGE_SKY);
     k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);

@@ -115,6 +115,7 @@ struct SkyParams {
     float sun_emission;
     float3 sigma_r;
     float sigma_m, sigma_am, h_r, h_m;
+    float inv_h_r, inv_h_m;   // 1 / scale heights
     float earth_r, atm_r;
     float cos_half_sun;       // LeSun threshold
     float sun_radius_m;       // physical radius of the sun disc at 1 AU

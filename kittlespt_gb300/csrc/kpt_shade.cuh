@@ -294,8 +294,9 @@ __device__ __forceinline__ float srgb_decode(float v) {
 // The geometry of the sky model works with vectors of length ~6.4e6 m, where
 // one float ulp is 0.5 m of altitude and a 1 m altitude error is 1e-3 of Mie
 // density (scale height 1200 m).  It therefore runs in IEEE arithmetic
-// without contraction; only the exponentials use the fast exp (relative
-// error ~1e-6 for these arguments).
+// without contraction; the exponentials use the fast exp and their arguments
+// the reciprocal scale heights (relative error ~1e-6 for these arguments,
+// like the reference's fast-math division).
 __device__ __forceinline__ bool sphere_hit(float3 o, float3 d, float radius, float* t0, float* t1) {
     float3 oc = make_float3(-o.x, -o.y, -o.z);
     float a = xdot(d, d);
@@ -325,7 +326,7 @@ static __device__ __noinline__ float3 nishita(const SkyParams& P, float3 o, floa
         if (te > tmin && te > 0.0f) tmin = te;
         if (tx < tmax) tmax = tx;
     }
-    const float step = __fdiv_rn(xs(tmax, tmin), 16.0f);
+    const float step = xm(xs(tmax, tmin), 0.0625f);   // exact: / 16
     const float3 tR = make_float3(xa(P.sigma_r.x, 0.0f), xa(P.sigma_r.y, 0.0f), xa(P.sigma_r.z, 0.0f));
     const float tM = xa(P.sigma_m, P.sigma_am);
     const float half = xm(step, 0.5f);
@@ -336,13 +337,13 @@ static __device__ __noinline__ float3 nishita(const SkyParams& P, float3 o, floa
     for (int i = 0; i < 16; ++i) {
         float3 sp = xpoint(o, xa(t, half), d);
         float alt = xs(__fsqrt_rn(xdot(sp, sp)), P.earth_r);
-        float pR = xm(expf(__fdiv_rn(-alt, P.h_r)), step);
-        float pM = xm(expf(__fdiv_rn(-alt, P.h_m)), step);
+        float pR = xm(expf(-alt * P.inv_h_r), step);
+        float pM = xm(expf(-alt * P.inv_h_m), step);
         oR = xa(oR, pR);
         oM = xa(oM, pM);
         float lte, ltx;
         sphere_hit(sp, P.sun_dir, P.atm_r, &lte, &ltx);
-        float lstep = __fdiv_rn(ltx, 8.0f);
+        float lstep = xm(ltx, 0.125f);   // exact: / 8
         float lhalf = xm(lstep, 0.5f);
         float lt = 0.0f, lR = 0.0f, lM = 0.0f;
         int j;
@@ -351,8 +352,8 @@ static __device__ __noinline__ float3 nishita(const SkyParams& P, float3 o, floa
             float3 spl = xpoint(sp, xa(lt, lhalf), P.sun_dir);
             float altl = xs(__fsqrt_rn(xdot(spl, spl)), P.earth_r);
             if (altl < 0.0f) break;
-            lR = xa(lR, xm(expf(__fdiv_rn(-altl, P.h_r)), lstep));
-            lM = xa(lM, xm(expf(__fdiv_rn(-altl, P.h_m)), lstep));
+            lR = xa(lR, xm(expf(-altl * P.inv_h_r), lstep));
+            lM = xa(lM, xm(expf(-altl * P.inv_h_m), lstep));
             lt = xa(lt, lstep);
         }
         if (j == 8) {
