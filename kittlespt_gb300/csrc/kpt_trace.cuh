@@ -344,6 +344,10 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
     int inst = -1;           // instance being traversed, -1: in the TLAS
     int base = 0;            // stack height when the instance was entered
     int sp = 0;
+    // the top of the stack lives in a register: a node step keeps its near
+    // child here instead of pushing and popping it through local memory
+    constexpr int NONE = (int)0x80000000;
+    int top = NONE;
     int first = 0, count = 0;   // triangles of the leaf being tested
     best.t = loc.t = INF;
     best.inst = best.tri = loc.inst = loc.tri = -1;
@@ -364,12 +368,13 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             best.u = best.v = 0.0f;
             inst = -1;
             sp = 0;
+            top = NONE;
             count = 0;
             float te;
             st.box_tests++;
             if (s.ninst > 0 &&
                 slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
-                stack[sp++] = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
+                top = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
         } else if (count > 0) {
             // one triangle of the leaf (BLAS2::intersect / intersectP leaf loop)
             float u, v;
@@ -390,7 +395,7 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
                 loc.u = u;
                 loc.v = v;
             }
-        } else if (inst >= 0 && sp == base) {
+        } else if (inst >= 0 && top == NONE && sp == base) {
             // leaving the instance: merge its closest hit (tlas.cu:116-121)
             if (!ANY && loc.t < best.t) {
                 best = loc;
@@ -398,12 +403,13 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             }
             inst = -1;
             r = w;
-        } else if (sp == 0) {
+        } else if (top == NONE && sp == 0) {
             if (ANY) src.any(ray, false);
             else src.closest(ray, best);
             ray = -1;
         } else {
-            const int e = stack[--sp];
+            const int e = top != NONE ? top : stack[--sp];
+            top = NONE;
             if (e >= 0) {
                 // interior node of the TLAS or of the instance's BLAS
                 const bool in_blas = inst >= 0;
@@ -415,18 +421,19 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
                 node_slabs(nd, r, tmin, tmx, &h1, &t1, &h2, &t2);
                 st.box_tests += 2;
                 const bool p1 = h1 && t1 < cull, p2 = h2 && t2 < cull;
-                if (in_blas ? (sp - base + 2 > BLAS_STACK) : (sp + 2 > TLAS_STACK)) {
+                if (in_blas ? (sp - base + 1 > BLAS_STACK) : (sp + 1 > TLAS_STACK)) {
                     st.overflow++;
                     sp = in_blas ? base : 0;   // the reference's stack would overflow: end this level
                 } else {
                     const int c1 = nd.d.y ? (in_blas ? leaf_code(e, 0) : -nd.d.x - 1) : nd.d.x;
                     const int c2 = nd.d.w ? (in_blas ? leaf_code(e, 1) : -nd.d.z - 1) : nd.d.z;
-                    // near child pushed last, popped first
+                    // near child popped first: the far one goes to memory, the
+                    // near one stays in the register
                     const bool far1 = t1 > t2;
                     const int ca = far1 ? c1 : c2, cb = far1 ? c2 : c1;
                     const bool pa = far1 ? p1 : p2, pb = far1 ? p2 : p1;
-                    if (pa) stack[sp++] = ca;
-                    if (pb) stack[sp++] = cb;
+                    if (pa && pb) stack[sp++] = ca;
+                    top = pb ? cb : (pa ? ca : NONE);
                 }
             } else if (inst < 0) {
                 // entering an instance (TLAS leaf): object-space ray (Ray::transform)
@@ -444,7 +451,7 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
                     first = m.leaf_first;
                     count = m.leaf_count;
                 } else {
-                    stack[sp++] = m.node_root;
+                    top = m.node_root;
                 }
             } else {
                 // BLAS leaf: its triangle range is read back from the parent node
