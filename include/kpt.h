@@ -246,12 +246,14 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * persistent grid (resident blocks x SMs) its wave kernels launch with, so
  * that jobs of one batch share the SMs; wave_cap: paths advanced together per
  * wave (queue capacity), 0 = 2^25; shade_block: threads per block of the
- * shading kernel (64, 128 or 256, 0 = 128). */
+ * shading kernel (64, 128 or 256, 0 = 128); sort_rays: 1 groups each level's
+ * extension rays by direction octant before they are traced, 0 keeps them in
+ * pixel order (results are the same either way). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;
     int32_t shade_block;
-    int32_t pad;
+    int32_t sort_rays;
 } kpt_tuning;
 void kpt_tuning_default(kpt_tuning* t);
 kpt_status kpt_set_tuning(kpt_context* ctx, const kpt_tuning* t);

@@ -134,7 +134,8 @@ struct kpt_context {
     DBuf<double> adj_grad;
     DBuf<int> rec_count;
     DBuf<float4> pixel_sky, radiance, sky_queue;
-    DBuf<PathRec> paths[2];
+    DBuf<PathRec> paths[2], unsorted;
+    DBuf<int> octants;
     DBuf<ShadowRec> shadow;
     int wave_cap = 0;
     kpt_tuning tuning{};   // launch parameters of the path stage (kpt_set_tuning)
@@ -251,6 +252,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->primary.release(); c->hits.release(); c->hit_list.release(); c->hit_index.release();
     c->miss_list.release(); c->counts.release(); c->level_counts.release(); c->pixel_sky.release();
     c->radiance.release(); c->sky_queue.release(); c->paths[0].release(); c->paths[1].release();
+    c->unsorted.release(); c->octants.release();
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
@@ -680,6 +682,8 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     F.hits = c->hits.p;
     F.shadow = c->shadow.p;
     F.level_counts = c->level_counts.p;
+    F.unsorted = c->tuning.sort_rays ? c->unsorted.p : nullptr;
+    F.octants = c->octants.p;
     F.cap = c->wave_cap;
     F.primary = c->primary.p;
     F.hit_list = c->hit_list.p;
@@ -704,6 +708,8 @@ static kpt_status ensure_work(kpt_context* c, int nsamples) {
     KPT_CUDA(c->hits.ensure(cap));
     KPT_CUDA(c->shadow.ensure(cap));
     KPT_CUDA(c->level_counts.ensure((size_t)LEVEL_WORDS * (c->settings.max_depth + 2)));
+    KPT_CUDA(c->octants.ensure((size_t)16 * (c->settings.max_depth + 2)));
+    if (c->tuning.sort_rays) KPT_CUDA(c->unsorted.ensure(cap));
     while (c->ev_fork.size() < (size_t)c->settings.max_depth + 1) {
         cudaEvent_t a = nullptr, b = nullptr;
         KPT_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
@@ -767,6 +773,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     const bool fork = c->tf == nullptr && c->ev_fork.size() >= (size_t)D + 1;
     for (long long w0 = 0; w0 < items; w0 += F.cap) {
         cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
+        if (F.unsorted) cudaMemsetAsync(c->octants.p, 0, sizeof(int) * 16 * (size_t)(D + 2), s);
         for (int l = 0; l <= D; ++l) {
             if (l > 0) {
                 stage_mark(c, KPT_STAGE_EXTEND);
@@ -786,6 +793,12 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
             }
             c->launches += l > 0 ? 3 : 2;
+            if (F.unsorted && l < D) {   // the continuations of level l, grouped by octant
+                stage_mark(c, KPT_STAGE_SHADE);
+                k_sort_count<<<c->sm_count * 4, 256, 0, s>>>(F, l + 1);
+                k_sort_scatter<<<c->sm_count * 4, 256, 0, s>>>(F, l + 1);
+                c->launches += 2;
+            }
         }
         if (fork) cudaStreamWaitEvent(s, c->ev_join[D], 0);
     }
@@ -1170,7 +1183,7 @@ void kpt_tuning_default(kpt_tuning* t) {
     t->grid_scale = 1.0f;
     t->wave_cap = 0;
     t->shade_block = PATH_BLOCK;
-    t->pad = 0;
+    t->sort_rays = 0;
 }
 
 kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
@@ -1181,6 +1194,7 @@ kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
         return fail(KPT_ERR_INVALID, "kpt_set_tuning: wave_cap must be 0 or in [1024, 2^25]");
     if (t->shade_block != 0 && t->shade_block != 64 && t->shade_block != 128 && t->shade_block != 256)
         return fail(KPT_ERR_INVALID, "kpt_set_tuning: shade_block must be 0, 64, 128 or 256");
+    if (t->sort_rays != 0 && t->sort_rays != 1) return fail(KPT_ERR_INVALID, "kpt_set_tuning: sort_rays must be 0 or 1");
     c->tuning = *t;
     if (c->tuning.shade_block == 0) c->tuning.shade_block = PATH_BLOCK;
     return KPT_OK;
@@ -1534,6 +1548,14 @@ kpt_status kpt_autotune_batch(kpt_batch* b, int n, kpt_context* const* jobs, con
         for (int blk : {64, 256}) {
             kpt_tuning t = cur;
             t.shade_block = blk;
+            float ms = 0.0f;
+            st = time_batch(b, n, jobs, spp, t, lanes, reps, &ms);
+            if (st != KPT_OK) return st;
+            if (ms < cur_ms) { cur_ms = ms; cur = t; }
+        }
+        {
+            kpt_tuning t = cur;
+            t.sort_rays = 1;
             float ms = 0.0f;
             st = time_batch(b, n, jobs, spp, t, lanes, reps, &ms);
             if (st != KPT_OK) return st;

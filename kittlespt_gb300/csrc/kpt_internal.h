@@ -75,6 +75,8 @@ struct FrameParams {
     PrimaryRec* hits;          // [cap] closest hits of the paths entering a level
     ShadowRec* shadow;         // [cap] shadow rays of a level: sun rays from the front, light rays from the back
     int* level_counts;         // [LEVEL_WORDS * (max_depth + 2)] zeroed per wave
+    PathRec* unsorted;         // [cap] k_shade's continuations before the octant sort, null: no sort
+    int* octants;              // [16 * (max_depth + 2)] per level: paths per direction octant, cursors
     int cap;
 };
 
@@ -136,6 +138,8 @@ __global__ void k_primary_sky(FrameParams F);
 __global__ void k_shade(FrameParams F, int level, long long wave0);        // blocks of <= PATH_BLOCK threads
 __global__ void k_shade_wide(FrameParams F, int level, long long wave0);   // blocks of <= SHADE_MAX_BLOCK threads
 __global__ void k_extend(FrameParams F, int level);
+__global__ void k_sort_count(FrameParams F, int level);     // octant histogram of the paths entering level
+__global__ void k_sort_scatter(FrameParams F, int level);   // paths entering level, grouped by octant
 __global__ void k_shadow(FrameParams F, int level);
 __global__ void k_sky_queue(FrameParams F);
 __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);

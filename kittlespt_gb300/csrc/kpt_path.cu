@@ -145,7 +145,7 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
         n = F.level_counts[LEVEL_WORDS * level];
     }
     const PathRec* in = F.paths[level & 1];
-    PathRec* out = F.paths[(level + 1) & 1];
+    PathRec* out = F.unsorted ? F.unsorted : F.paths[(level + 1) & 1];
     int* here = F.level_counts + LEVEL_WORDS * level;
     int* next = F.level_counts + LEVEL_WORDS * (level + 1);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -315,6 +315,63 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, 
 }
 __global__ void __launch_bounds__(SHADE_MAX_BLOCK) k_shade_wide(FrameParams F, int level, long long wave0) {
     shade_level(F, level, wave0);
+}
+
+// ---------------------------------------------------------------------------
+// octant sort of the continuations: rays of one warp then share a direction
+// octant (the queue order otherwise follows the pixels, so origins are
+// already coherent).  A path's result does not depend on its queue slot.
+
+__device__ __forceinline__ int octant(float4 d) {
+    return (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
+}
+
+__global__ void __launch_bounds__(256) k_sort_count(FrameParams F, int level) {
+    __shared__ int h[8];
+    if (threadIdx.x < 8) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int n = F.level_counts[LEVEL_WORDS * level];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[octant(F.unsorted[i].d_seed)], 1);
+    __syncthreads();
+    if (threadIdx.x < 8 && h[threadIdx.x]) atomicAdd(&F.octants[16 * level + threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(FrameParams F, int level) {
+    const int n = F.level_counts[LEVEL_WORDS * level];
+    const int* cnt = F.octants + 16 * level;
+    int* cursor = F.octants + 16 * level + 8;
+    int off[8];
+    int acc = 0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+        off[o] = acc;
+        acc += cnt[o];
+    }
+    PathRec* out = F.paths[level & 1];
+    const int lane = threadIdx.x & 31;
+    // warp-uniform loop: every lane takes part in the warp-level appends
+    for (int w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += gridDim.x * blockDim.x) {
+        const int i = w0 + lane;
+        const bool ok = i < n;
+        PathRec r;
+        int o = 8;
+        if (ok) {
+            r = F.unsorted[i];
+            o = octant(r.d_seed);
+        }
+        const unsigned same = __match_any_sync(0xffffffffu, o);
+        const int leader = __ffs(same) - 1;
+        int b = 0;
+        if (ok && lane == leader) b = atomicAdd(cursor + o, __popc(same));
+        b = __shfl_sync(0xffffffffu, b, leader);
+        if (ok) {
+            int dst = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) dst = (q == o) ? off[q] : dst;
+            out[dst + b + __popc(same & ((1u << lane) - 1u))] = r;
+        }
+    }
 }
 
 // Closest hits of the paths entering `level` (1 .. max_depth).

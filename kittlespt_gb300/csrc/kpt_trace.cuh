@@ -433,7 +433,17 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
                     const int ca = far1 ? c1 : c2, cb = far1 ? c2 : c1;
                     const bool pa = far1 ? p1 : p2, pb = far1 ? p2 : p1;
                     if (pa && pb) stack[sp++] = ca;
-                    top = pb ? cb : (pa ? ca : NONE);
+                    // the child visited next: a BLAS leaf starts at once, its
+                    // triangle range is in this node (no push, pop, setup step)
+                    const int cn = pb ? (far1 ? 1 : 0) : (far1 ? 0 : 1);
+                    const int ncount = cn ? nd.d.w : nd.d.y;
+                    if ((pa || pb) && in_blas && ncount > 0) {
+                        first = cn ? nd.d.z : nd.d.x;
+                        count = ncount;
+                        top = NONE;
+                    } else {
+                        top = pb ? cb : (pa ? ca : NONE);
+                    }
                 }
             } else if (inst < 0) {
                 // entering an instance (TLAS leaf): object-space ray (Ray::transform)

@@ -298,14 +298,15 @@ class Renderer:
         return g, img
 
     # -- launch parameters (no reference counterpart) -------------------------
-    def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0):
-        t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block)
+    def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0, sort_rays: int = 0):
+        t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block, sort_rays=sort_rays)
         K.check(self._L.kpt_set_tuning(self._ctx, C.byref(t)))
 
     def tuning(self) -> dict:
         t = K.Tuning()
         K.check(self._L.kpt_get_tuning(self._ctx, C.byref(t)))
-        return {"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block}
+        return {"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block,
+                "sort_rays": t.sort_rays}
 
 
 class Batch:
@@ -356,8 +357,8 @@ class Batch:
         ms = np.zeros(1, np.float32)
         K.check(self._L.kpt_autotune_batch(self._b, n, jobs, K.iptr(s), reps, C.byref(t), K.iptr(lanes),
                                            K.fptr(ms)))
-        return ({"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block},
-                int(lanes[0]), float(ms[0]))
+        return ({"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block,
+                 "sort_rays": t.sort_rays}, int(lanes[0]), float(ms[0]))
 
 
 # -- path-replay adjoint (no reference counterpart) ----------------------------

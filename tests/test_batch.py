@@ -4,7 +4,8 @@ A batch renders one frame of each job as a branch of one CUDA graph; every
 job's samples are computed exactly as by kpt_render_frame, so images and
 accumulations must be bit-identical to rendering the jobs one by one, under
 any lane count and any launch tuning (grid share, wave capacity -- a small one
-forces many waves -- and shading block size)."""
+forces many waves --, shading block size, octant sort of the extension
+rays)."""
 
 import ctypes as C
 
@@ -18,7 +19,7 @@ def test_tuning_defaults_and_errors():
     L = K.load()
     t = K.Tuning()
     L.kpt_tuning_default(C.byref(t))
-    assert (t.grid_scale, t.wave_cap, t.shade_block) == (1.0, 0, 128)
+    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays) == (1.0, 0, 128, 0)
     assert L.kpt_set_tuning(None, C.byref(t)) == -1
     assert L.kpt_get_tuning(None, C.byref(t)) == -1
     assert L.kpt_submit_batch(None, 1, None, None, 0) == -1
@@ -80,7 +81,8 @@ def reference_frames():
     (0, None),
     (2, None),
     (1, dict(grid_scale=0.25, wave_cap=1024, shade_block=64)),
-    (3, dict(grid_scale=0.5, wave_cap=4096, shade_block=256)),
+    (3, dict(grid_scale=0.5, wave_cap=4096, shade_block=256, sort_rays=1)),
+    (0, dict(sort_rays=1)),
 ])
 def test_batch_matches_one_by_one(reference_frames, lanes, tuning):
     from kittlespt_gb300.renderer import Batch
@@ -127,6 +129,8 @@ def test_batch_errors():
             rs[0].set_tuning(wave_cap=100)
         with pytest.raises(K.KptError):
             rs[0].set_tuning(shade_block=96)
+        with pytest.raises(K.KptError):
+            rs[0].set_tuning(sort_rays=2)
     finally:
         for r in rs:
             r.shutdown()
