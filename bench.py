@@ -262,6 +262,7 @@ def run_gpu(args):
     traffic = {"extend": (246.9e6 + 20.9e6) * 8.0, "shadow": (131.3e6 + 1.6e6) * 8.0}
     dom = max(kern, key=lambda k: stage_ms[k])
     kname, pre = kern[dom]
+    rays_frame = delta("camera_rays") + delta("path_rays") + delta("shadow_rays")
     boxes, tris, insts = delta(pre + "_box_tests"), delta(pre + "_tri_tests"), delta(pre + "_inst_xforms")
     alg_bytes = 24.0 * boxes + 40.0 * tris + 64.0 * insts
     launch_ms = stage_ms[dom]
@@ -310,6 +311,9 @@ def run_gpu(args):
                                                 "(3 frames with the stages serialised)",
                             "box_tests": boxes, "tri_tests": tris, "inst_xforms": insts},
                "stage_ms_per_frame": stage_ms,
+               "rays_per_s": rays_frame * args.steps * world / (ms_max / 1e3),
+               "rays_per_frame": {"camera": delta("camera_rays"), "extension": delta("path_rays"),
+                                  "shadow": delta("shadow_rays")},
                "cpu_baseline": cpu,
                "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 128,
                        "d2h_bytes_per_step": W * H * 16},
@@ -525,6 +529,56 @@ def run_adjoint(args):
     print(json.dumps(out))
 
 
+def run_traversal(args):
+    """Traversal stress: one BLAS of 2,000,000 random triangles, 1,048,576
+    incoherent rays from the bounding sphere plus 4 diffuse bounces
+    (kpt_trace_bounces_device); rays/s over the rays actually traced (a chain
+    stops at its first miss)."""
+    import torch
+    from kittlespt_gb300 import build as B
+    B.build()
+    from kittlespt_gb300 import scenes as S
+    from kittlespt_gb300.renderer import Renderer
+    sc = S.scene_traversal(2_000_000)
+    o, d = S.random_rays(1_048_576)
+    n, nb = o.shape[0], 4
+    r = Renderer(0)
+    r.initialize()
+    r.load_scene(sc)
+    stream = torch.cuda.ExternalStream(r.stream(), device=0)
+    to = torch.from_numpy(np.ascontiguousarray(o, np.float32)).cuda()
+    td = torch.from_numpy(np.ascontiguousarray(d, np.float32)).cuda()
+    inst = torch.empty((nb + 1) * n, dtype=torch.int32, device="cuda")
+    tri = torch.empty_like(inst)
+    t = torch.empty((nb + 1) * n, dtype=torch.float32, device="cuda")
+
+    def step():
+        r.trace_bounces_device(n, to.data_ptr(), td.data_ptr(), nb, inst.data_ptr(), tri.data_ptr(), t.data_ptr())
+    for _ in range(args.warmup):
+        step()
+    r.synchronize()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            step()
+        ev[1].record(stream)
+    r.synchronize()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    hits = inst.view(nb + 1, n).cpu().numpy() >= 0
+    traced = n + int(hits[:-1].sum())
+    r.shutdown()
+    out = {"metric": "rays/s, traversal stress (2M random triangles, 1M rays + 4 diffuse bounces)",
+           "value": traced / (ms / 1e3), "unit": "rays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded random triangles and rays)",
+           "config": {"workload": "random_triangles_2M_rays_1M_bounces_4", "triangles": 2_000_000, "rays": n,
+                      "bounces": nb, "rays_traced_per_step": traced}}
+    print(json.dumps(out))
+
+
 def run_profile_case(spec):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
     small case that ncu captures of single kernels run on."""
@@ -548,9 +602,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "adjoint"],
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "adjoint", "traversal"],
                     help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one; "
-                         "adjoint: gradient evaluations/s of the path-replay adjoint")
+                         "adjoint: gradient evaluations/s of the path-replay adjoint; "
+                         "traversal: rays/s on 2M random triangles")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
     args = ap.parse_args()
@@ -563,6 +618,8 @@ def main():
         run_batch(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "traversal":
+        run_traversal(args)
     else:
         run_gpu(args)
 

@@ -84,6 +84,7 @@ typedef struct kpt_stats {
     uint64_t box_tests, tri_tests, inst_xforms, overflows;
     uint64_t path_box_tests, path_tri_tests, path_inst_xforms;
     uint64_t shadow_box_tests, shadow_tri_tests, shadow_inst_xforms;
+    uint64_t path_rays, shadow_rays, camera_rays;   /* rays traced by the path stage */
     float avg_luminance, adapted_luminance, exposure_scalar, iso, shutter, avg_bin;
     int32_t frame_index, pad;
 } kpt_stats;

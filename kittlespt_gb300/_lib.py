@@ -58,6 +58,7 @@ class Stats(C.Structure):
                 ("overflows", C.c_uint64), ("path_box_tests", C.c_uint64), ("path_tri_tests", C.c_uint64),
                 ("path_inst_xforms", C.c_uint64), ("shadow_box_tests", C.c_uint64),
                 ("shadow_tri_tests", C.c_uint64), ("shadow_inst_xforms", C.c_uint64),
+                ("path_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("camera_rays", C.c_uint64),
                 ("avg_luminance", C.c_float), ("adapted_luminance", C.c_float),
                 ("exposure_scalar", C.c_float), ("iso", C.c_float), ("shutter", C.c_float),
                 ("avg_bin", C.c_float), ("frame_index", C.c_int32), ("pad", C.c_int32)]

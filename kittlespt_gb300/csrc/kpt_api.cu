@@ -222,14 +222,14 @@ kpt_status kpt_create(int device, kpt_context** out) {
     kpt_exposure_default(&c->exposure);
     kpt_tuning_default(&c->tuning);
     if (c->expo_state.ensure(1) != cudaSuccess || c->sun_radiance.ensure(1) != cudaSuccess ||
-        c->counters.ensure(12) != cudaSuccess ||
+        c->counters.ensure(16) != cudaSuccess ||
         c->counts.ensure(4) != cudaSuccess || c->fetch.ensure(1) != cudaSuccess ||
         c->hist.ensure(256) != cudaSuccess || c->thresholds.ensure(256) != cudaSuccess) {
         kpt_destroy(c);
         return fail(KPT_ERR_NOMEM, "kpt_create: device allocation failed");
     }
     cudaMemsetAsync(c->expo_state.p, 0, sizeof(ExposureState), c->stream);
-    cudaMemsetAsync(c->counters.p, 0, 12 * sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 16 * sizeof(unsigned long long), c->stream);
     *out = c;
     return KPT_OK;
 }
@@ -801,6 +801,8 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
             }
         }
         if (fork) cudaStreamWaitEvent(s, c->ev_join[D], 0);
+        k_count_rays<<<1, 32, 0, s>>>(F);
+        c->launches += 1;
     }
     stage_mark(c, KPT_STAGE_SKY);
     k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
@@ -982,7 +984,7 @@ kpt_status kpt_read_histogram(kpt_context* c, uint64_t* bins) { return read_buf(
 
 kpt_status kpt_get_stats(kpt_context* c, kpt_stats* st) {
     if (!c || !st) return fail(KPT_ERR_INVALID, "null argument");
-    unsigned long long cnt[12];
+    unsigned long long cnt[16];
     ExposureState es;
     KPT_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
     KPT_CUDA(cudaMemcpyAsync(&es, c->expo_state.p, sizeof es, cudaMemcpyDeviceToHost, c->stream));
@@ -997,6 +999,9 @@ kpt_status kpt_get_stats(kpt_context* c, kpt_stats* st) {
     st->shadow_box_tests = cnt[8];
     st->shadow_tri_tests = cnt[9];
     st->shadow_inst_xforms = cnt[10];
+    st->path_rays = cnt[12];
+    st->shadow_rays = cnt[13];
+    st->camera_rays = cnt[14];
     st->avg_luminance = es.avg_lum;
     st->adapted_luminance = es.adapted_lum;
     st->exposure_scalar = es.exposure_scalar;

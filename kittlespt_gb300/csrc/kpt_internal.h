@@ -59,8 +59,9 @@ struct FrameParams {
     float4* albedo;            // [H*W] visible-surface albedo, may be null
     int4* first_hit;           // [H*W] (instance, triangle, t bits, 0), may be null
     float4* sample_out;        // [nsamples][H*W] clamped per-sample radiance, may be null
-    unsigned long long* counters;   // [12] box tests, triangle tests, instance transforms, overflows
-                                    //      of the extension rays, the camera rays, the shadow rays
+    unsigned long long* counters;   // [16] box tests, triangle tests, instance transforms, overflows
+                                    //      of the extension rays, the camera rays, the shadow rays;
+                                    //      then extension rays, shadow rays, camera rays traced
     // work buffers of the frame
     PrimaryRec* primary;       // [H*W]
     int* hit_list;             // [H*W] pixels whose camera ray hits, compacted
@@ -138,6 +139,7 @@ __global__ void k_primary_sky(FrameParams F);
 __global__ void k_shade(FrameParams F, int level, long long wave0);        // blocks of <= PATH_BLOCK threads
 __global__ void k_shade_wide(FrameParams F, int level, long long wave0);   // blocks of <= SHADE_MAX_BLOCK threads
 __global__ void k_extend(FrameParams F, int level);
+__global__ void k_count_rays(FrameParams F);   // adds the wave's ray counts to counters[12..13]
 __global__ void k_sort_count(FrameParams F, int level);     // octant histogram of the paths entering level
 __global__ void k_sort_scatter(FrameParams F, int level);   // paths entering level, grouped by octant
 __global__ void k_shadow(FrameParams F, int level);

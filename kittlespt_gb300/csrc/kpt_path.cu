@@ -76,6 +76,11 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary(FrameParams F) {
         if (F.first_hit) F.first_hit[p] = make_int4(-1, -1, 0x7f800000, 0);
     }
     flush_stats(st, F.counters ? F.counters + 4 : nullptr);
+    if (F.counters && threadIdx.x == 0) {   // camera rays of this block
+        const int first_px = blockIdx.x * blockDim.x;
+        const int nb = min((int)blockDim.x, npix - first_px);
+        if (nb > 0) atomicAdd(F.counters + 14, (unsigned long long)nb);
+    }
 }
 
 // sky (times LeSun) of every pixel whose camera ray misses
@@ -315,6 +320,21 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, 
 }
 __global__ void __launch_bounds__(SHADE_MAX_BLOCK) k_shade_wide(FrameParams F, int level, long long wave0) {
     shade_level(F, level, wave0);
+}
+
+// Rays the wave traced: extension rays (paths entering levels >= 1) and
+// shadow rays (every level), from the level counters before the next wave
+// clears them; the camera rays are counted by k_primary.
+__global__ void k_count_rays(FrameParams F) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long ext = 0, shd = 0;
+    for (int l = 0; l <= F.max_depth; ++l) {
+        const int* lc = F.level_counts + LEVEL_WORDS * l;
+        if (l > 0) ext += (unsigned)lc[0];
+        shd += (unsigned)lc[1] + (unsigned)lc[2];
+    }
+    F.counters[12] += ext;
+    F.counters[13] += shd;
 }
 
 // ---------------------------------------------------------------------------
