@@ -1080,8 +1080,9 @@ kpt_status kpt_trace_bounces_device(kpt_context* c, int n, const float* o, const
     if (n < 0 || nb < 0 || (n > 0 && (!o || !d || !inst || !tri || !t)))
         return fail(KPT_ERR_INVALID, "kpt_trace_bounces_device: bad arguments");
     if (n == 0) return KPT_OK;
-    k_trace_bounces<<<trace_grid(c, (const void*)k_trace_bounces, n), TRACE_BLOCK, 0, c->stream>>>(
-        c->view, n, (const float3*)o, (const float3*)d, nb, inst, tri, t, c->counters.p);
+    KPT_CUDA(cudaMemsetAsync(c->fetch.p, 0, sizeof(int), c->stream));
+    k_trace_chains<<<trace_grid(c, (const void*)k_trace_chains, n), TRACE_BLOCK, 0, c->stream>>>(
+        c->view, n, (const float3*)o, (const float3*)d, nb, inst, tri, t, c->fetch.p, c->counters.p);
     c->launches += 1;
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;

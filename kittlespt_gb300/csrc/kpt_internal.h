@@ -160,5 +160,7 @@ __global__ void k_occluded(SceneView s, int n, const float3* o, const float3* d,
                            uint8_t* out, int* next, unsigned long long* counters);
 __global__ void k_trace_bounces(SceneView s, int n, const float3* o, const float3* d, int nbounces,
                                 int* inst, int* tri, float* t, unsigned long long* counters);
+__global__ void k_trace_chains(SceneView s, int n, const float3* o, const float3* d, int nbounces, int* inst,
+                               int* tri, float* t, int* next, unsigned long long* counters);
 
 }  // namespace kpt

@@ -405,7 +405,7 @@ struct ExtendQueue {
         tmin = 0.0f;
         tmax = __int_as_float(0x7f800000);
     }
-    __device__ __forceinline__ void closest(int i, const Hit& h) const {
+    __device__ __forceinline__ bool closest(int i, const Hit& h, float3&, float3&) const {
         PrimaryRec r;
         r.t = h.t;
         r.u = h.u;
@@ -414,6 +414,7 @@ struct ExtendQueue {
         r.tri = h.tri;
         r.pad0 = r.pad1 = r.pad2 = 0;
         out[i] = r;
+        return false;
     }
     __device__ __forceinline__ void any(int, bool) const {}
 };
@@ -442,7 +443,7 @@ struct ShadowQueue {
         tmin = 0.0f;
         tmax = a.w;
     }
-    __device__ __forceinline__ void closest(int, const Hit&) const {}
+    __device__ __forceinline__ bool closest(int, const Hit&, float3&, float3&) const { return false; }
     __device__ __forceinline__ void any(int i, bool occluded) const {
         if (occluded) return;
         const int j = slot(i);
@@ -508,11 +509,12 @@ struct RayBatch {
         t0 = tmin;
         t1 = tmax_each ? tmax_each[i] : tmax;
     }
-    __device__ __forceinline__ void closest(int i, const Hit& h) const {
+    __device__ __forceinline__ bool closest(int i, const Hit& h, float3&, float3&) const {
         inst[i] = h.inst;
         tri[i] = h.tri;
         t[i] = h.t;
         if (uv) uv[i] = make_float2(h.u, h.v);
+        return false;
     }
     __device__ __forceinline__ void any(int i, bool occluded) const { occ[i] = occluded ? 1 : 0; }
 };
@@ -536,6 +538,87 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_occluded(Scen
     TraceStats st = {0, 0, 0, 0};
     RayBatch q{o, d, tmin, 0.0f, tmax, nullptr, nullptr, nullptr, nullptr, out};
     trace_queue<true>(s, n, next, q, st, stack);
+    flush_stats(st, counters);
+}
+
+// The diffuse bounce of ray i after hit h at bounce b: cosine-weighted about
+// the geometric normal facing the incoming ray (Malley's method: a uniform
+// unit-disk point rejection-sampled from pairs of PCG draws seeded with
+// 4 * ray index + bounce, lifted to the hemisphere, rotated by the Frisvad
+// basis), origin offset 1e-3 along the normal; IEEE arithmetic throughout.
+__device__ __forceinline__ void diffuse_bounce(const SceneView& s, const Hit& h, float3 ro, float3 rd, int i, int b,
+                                               float3* no, float3* nd) {
+    const InstRec& ir = s.inst[h.inst];
+    const TriShade sh = s.shade[s.meshes[ir.mesh].shade_base + h.tri];
+    float3 gn = make_float3(sh.gnx, sh.gny, sh.gnz);
+    float3 nn = xnormalize(make_float3(xrow(ir.model[0], gn, 0.0f), xrow(ir.model[1], gn, 0.0f),
+                                       xrow(ir.model[2], gn, 0.0f)));
+    if (xdot(nn, rd) > 0.0f) nn = make_float3(-nn.x, -nn.y, -nn.z);
+    float3 p = make_float3(xa(ro.x, xm(h.t, rd.x)), xa(ro.y, xm(h.t, rd.y)), xa(ro.z, xm(h.t, rd.z)));
+    Sampler S;
+    S.seed = (uint32_t)i * 4u + (uint32_t)b;
+    float lx = 0.0f, ly = 0.0f, r2 = 0.0f;
+    for (int q = 0; q < 64; ++q) {
+        float u0 = S.get1D(), u1 = S.get1D();
+        float a = xs(xm(2.0f, u0), 1.0f), c = xs(xm(2.0f, u1), 1.0f);
+        float m = xa(xm(a, a), xm(c, c));
+        if (m < 1.0f) { lx = a; ly = c; r2 = m; break; }
+    }
+    float3 l = make_float3(lx, ly, __fsqrt_rn(xs(1.0f, r2)));
+    *nd = onb_apply_exact(nn, l);
+    *no = make_float3(xa(p.x, xm(nn.x, HIT_EPS)), xa(p.y, xm(nn.y, HIT_EPS)), xa(p.z, xm(nn.z, HIT_EPS)));
+}
+
+// Bounce chains on the queue traversal: entry i is ray i; after each closest
+// hit the lane writes bounce b's hit and continues with the next bounce ray
+// (diffuse_bounce), so chains of different lengths share warps.
+struct BounceQueue {
+    const float3 *o, *d;
+    int n, nbounces;
+    int *inst, *tri;
+    float* t;
+    const SceneView* s;
+    int b;   // bounce of the chain this lane is tracing
+    float3 ro, rd;
+    __device__ __forceinline__ void ray(int i, float3& oo, float3& dd, float& tmin, float& tmax) {
+        b = 0;
+        ro = oo = o[i];
+        rd = dd = d[i];
+        tmin = 0.0f;
+        tmax = __int_as_float(0x7f800000);
+    }
+    __device__ __forceinline__ bool closest(int i, const Hit& h, float3& no, float3& nd) {
+        const size_t k = (size_t)b * n + i;
+        inst[k] = h.inst;
+        tri[k] = h.tri;
+        t[k] = h.t;
+        if (h.inst < 0) {
+            for (int bb = b + 1; bb <= nbounces; ++bb) {
+                const size_t kk = (size_t)bb * n + i;
+                inst[kk] = -1;
+                tri[kk] = -1;
+                t[kk] = __int_as_float(0x7f800000);
+            }
+            return false;
+        }
+        if (b == nbounces) return false;
+        diffuse_bounce(*s, h, ro, rd, i, b, &no, &nd);
+        ++b;
+        ro = no;
+        rd = nd;
+        return true;
+    }
+    __device__ __forceinline__ void any(int, bool) {}
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_trace_chains(SceneView s, int n, const float3* o,
+                                                                              const float3* d, int nbounces, int* inst,
+                                                                              int* tri, float* t, int* next,
+                                                                              unsigned long long* counters) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    BounceQueue q{o, d, n, nbounces, inst, tri, t, &s, 0, make_float3(0.0f, 0.0f, 0.0f), make_float3(0.0f, 0.0f, 0.0f)};
+    trace_queue<false>(s, n, next, q, st, stack);
     flush_stats(st, counters);
 }
 
@@ -568,25 +651,9 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_bounces(SceneView s, int 
                 break;
             }
             if (b == nbounces) break;
-            const InstRec& ir = s.inst[h.inst];
-            const TriShade sh = s.shade[s.meshes[ir.mesh].shade_base + h.tri];
-            float3 gn = make_float3(sh.gnx, sh.gny, sh.gnz);
-            float3 nn = xnormalize(make_float3(xrow(ir.model[0], gn, 0.0f), xrow(ir.model[1], gn, 0.0f),
-                                               xrow(ir.model[2], gn, 0.0f)));
-            if (xdot(nn, r.d) > 0.0f) nn = make_float3(-nn.x, -nn.y, -nn.z);
-            float3 p = make_float3(xa(r.o.x, xm(h.t, r.d.x)), xa(r.o.y, xm(h.t, r.d.y)), xa(r.o.z, xm(h.t, r.d.z)));
-            Sampler S;
-            S.seed = (uint32_t)i * 4u + (uint32_t)b;
-            float lx = 0.0f, ly = 0.0f, r2 = 0.0f;
-            for (int q = 0; q < 64; ++q) {
-                float u0 = S.get1D(), u1 = S.get1D();
-                float a = xs(xm(2.0f, u0), 1.0f), c = xs(xm(2.0f, u1), 1.0f);
-                float m = xa(xm(a, a), xm(c, c));
-                if (m < 1.0f) { lx = a; ly = c; r2 = m; break; }
-            }
-            float3 l = make_float3(lx, ly, __fsqrt_rn(xs(1.0f, r2)));
-            float3 w = onb_apply_exact(nn, l);
-            r = make_xray(make_float3(xa(p.x, xm(nn.x, HIT_EPS)), xa(p.y, xm(nn.y, HIT_EPS)), xa(p.z, xm(nn.z, HIT_EPS))), w);
+            float3 no, nd;
+            diffuse_bounce(s, h, r.o, r.d, i, b, &no, &nd);
+            r = make_xray(no, nd);
         }
     }
     flush_stats(st, counters);

@@ -331,8 +331,10 @@ __device__ __forceinline__ bool trace_any(const SceneView& s, const XRay& r, flo
 // every result is identical to theirs.
 //
 // Src supplies the queue:  void ray(int i, float3& o, float3& d, float& tmin, float& tmax);
-//                          void closest(int i, const Hit& h);   (ANY == false)
+//                          bool closest(int i, const Hit& h, float3& o, float3& d);   (ANY == false)
 //                          void any(int i, bool occluded);      (ANY == true)
+// closest() may return true with the next ray of entry i (a bounce chain):
+// the lane traces it at once, with the same tmin and tmax.
 template <bool ANY, class Src>
 __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next, Src& src, TraceStats& st,
                                             int* stack) {
@@ -352,6 +354,23 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
     best.t = loc.t = INF;
     best.inst = best.tri = loc.inst = loc.tri = -1;
     best.u = best.v = loc.u = loc.v = 0.0f;
+    // a new ray: the TLAS root box (TLAS::intersect, tlas.cu:60-75), then its root
+    auto start = [&](float3 o, float3 d) {
+        w = make_xray(o, d);
+        r = w;
+        best.t = INF;
+        best.inst = best.tri = -1;
+        best.u = best.v = 0.0f;
+        inst = -1;
+        sp = 0;
+        top = NONE;
+        count = 0;
+        float te;
+        st.box_tests++;
+        if (s.ninst > 0 &&
+            slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
+            top = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
+    };
     for (;;) {
         if (ray < 0) {
             cg::coalesced_group g = cg::coalesced_threads();
@@ -361,20 +380,7 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             if (ray >= n) break;
             float3 o, d;
             src.ray(ray, o, d, tmin, tmax0);
-            w = make_xray(o, d);
-            r = w;
-            best.t = INF;
-            best.inst = best.tri = -1;
-            best.u = best.v = 0.0f;
-            inst = -1;
-            sp = 0;
-            top = NONE;
-            count = 0;
-            float te;
-            st.box_tests++;
-            if (s.ninst > 0 &&
-                slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
-                top = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
+            start(o, d);
         } else if (count > 0) {
             // one triangle of the leaf (BLAS2::intersect / intersectP leaf loop)
             float u, v;
@@ -404,9 +410,15 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             inst = -1;
             r = w;
         } else if (top == NONE && sp == 0) {
-            if (ANY) src.any(ray, false);
-            else src.closest(ray, best);
-            ray = -1;
+            float3 o, d;
+            if (ANY) {
+                src.any(ray, false);
+                ray = -1;
+            } else if (src.closest(ray, best, o, d)) {
+                start(o, d);
+            } else {
+                ray = -1;
+            }
         } else {
             const int e = top != NONE ? top : stack[--sp];
             top = NONE;
