@@ -78,6 +78,10 @@ struct kpt_context {
     // second stream of the frame graph: the shadow rays of a level run on it
     // while the next level's extension rays run on `stream`
     cudaStream_t side = nullptr;
+    // third stream: the sky of the paths that left the scene at level l runs
+    // on it once k_shadow(l) has ended, beside the later levels
+    cudaStream_t sky = nullptr;
+    cudaEvent_t ev_sky = nullptr;
     std::vector<cudaEvent_t> ev_fork, ev_join;
     uint64_t launches = 0;
 
@@ -213,6 +217,8 @@ kpt_status kpt_create(int device, kpt_context** out) {
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->sky, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_sky, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(KPT_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
@@ -257,6 +263,8 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
+    if (c->ev_sky) cudaEventDestroy(c->ev_sky);
+    if (c->sky) cudaStreamDestroy(c->sky);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -771,8 +779,13 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     // what k_shade(l) wrote and write disjoint buffers: they run on two
     // streams, joined before k_shade(l + 1); serial when stages are timed
     const bool fork = c->tf == nullptr && c->ev_fork.size() >= (size_t)D + 1;
+    const int g_sky = persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK);
     for (long long w0 = 0; w0 < items; w0 += F.cap) {
         cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
+        // the sky queue's length when the wave starts: where its level 0 begins
+        if (fork)
+            cudaMemcpyAsync(c->level_counts.p + LEVEL_WORDS * (D + 1) + 5, c->counts.p + 2, sizeof(int),
+                            cudaMemcpyDeviceToDevice, s);
         if (F.unsorted) cudaMemsetAsync(c->octants.p, 0, sizeof(int) * 16 * (size_t)(D + 2), s);
         for (int l = 0; l <= D; ++l) {
             if (l > 0) {
@@ -789,6 +802,10 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 cudaStreamWaitEvent(c->side, c->ev_fork[l], 0);
                 k_shadow<<<g_shd, TRACE_BLOCK, 0, c->side>>>(F, l);
                 cudaEventRecord(c->ev_join[l], c->side);
+                // k_shade(l)'s sky entries are final (their paths ended)
+                cudaStreamWaitEvent(c->sky, c->ev_join[l], 0);
+                k_sky_queue<<<g_sky, PATH_BLOCK, 0, c->sky>>>(F, l);
+                c->launches += 1;
             } else {
                 k_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, l);
             }
@@ -800,15 +817,22 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 c->launches += 2;
             }
         }
-        if (fork) cudaStreamWaitEvent(s, c->ev_join[D], 0);
+        if (fork) {
+            cudaStreamWaitEvent(s, c->ev_join[D], 0);
+            cudaEventRecord(c->ev_sky, c->sky);
+            cudaStreamWaitEvent(s, c->ev_sky, 0);
+        }
         k_count_rays<<<1, 32, 0, s>>>(F);
         c->launches += 1;
     }
-    stage_mark(c, KPT_STAGE_SKY);
-    k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
+    if (!fork) {
+        stage_mark(c, KPT_STAGE_SKY);
+        k_sky_queue<<<g_sky, PATH_BLOCK, 0, s>>>(F, -1);
+        c->launches += 1;
+    }
     stage_mark(c, KPT_STAGE_ACCUMULATE);
     k_accumulate<<<(np + 255) / 256, 256, 0, s>>>(F);
-    c->launches += 2;
+    c->launches += 1;
 }
 
 static kpt_status ready(kpt_context* c) {

@@ -75,7 +75,8 @@ struct FrameParams {
     PathRec* paths[2];         // [cap] paths entering even / odd levels
     PrimaryRec* hits;          // [cap] closest hits of the paths entering a level
     ShadowRec* shadow;         // [cap] shadow rays of a level: sun rays from the front, light rays from the back
-    int* level_counts;         // [LEVEL_WORDS * (max_depth + 2)] zeroed per wave
+    int* level_counts;         // [LEVEL_WORDS * (max_depth + 2)] zeroed per wave; word 5: sky queue
+                               // length after level l (of level max_depth + 1: at the wave's start)
     PathRec* unsorted;         // [cap] k_shade's continuations before the octant sort, null: no sort
     int* octants;              // [16 * (max_depth + 2)] per level: paths per direction octant, cursors
     int cap;
@@ -143,7 +144,7 @@ __global__ void k_count_rays(FrameParams F);   // adds the wave's ray counts to 
 __global__ void k_sort_count(FrameParams F, int level);     // octant histogram of the paths entering level
 __global__ void k_sort_scatter(FrameParams F, int level);   // paths entering level, grouped by octant
 __global__ void k_shadow(FrameParams F, int level);
-__global__ void k_sky_queue(FrameParams F);
+__global__ void k_sky_queue(FrameParams F, int level);
 __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
 // kpt_adjoint.cu (fast maths)
 __global__ void k_adjoint_constants(FrameParams F, AdjParams A);

@@ -458,17 +458,28 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameP
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
     int* lc = F.level_counts + LEVEL_WORDS * level;
+    // the sky queue cannot grow while this kernel runs (k_shade(level) has
+    // ended, k_shade(level + 1) waits for it): its length ends level's range
+    if (blockIdx.x == 0 && threadIdx.x == 0) lc[5] = F.counts[2];
     ShadowQueue q{F.shadow, F.radiance, lc[1], F.cap};
     trace_queue<true>(F.scene, lc[1] + lc[2], lc + 4, q, st, stack);
     flush_stats(st, F.counters + 8);
 }
 
-// sky * throughput of every path that left the scene, added to its sample
-__global__ void __launch_bounds__(PATH_BLOCK) k_sky_queue(FrameParams F) {
-    const int n = F.counts[2];
+// sky * throughput of every path that left the scene, added to its sample:
+// the whole queue (level < 0), or the entries k_shade(level) appended, from
+// the end of level - 1's range (the wave's starting length for level 0) to
+// the length k_shadow(level) recorded
+__global__ void __launch_bounds__(PATH_BLOCK) k_sky_queue(FrameParams F, int level) {
+    int i0 = 0, n = F.counts[2];
+    if (level >= 0) {
+        const int* mark = F.level_counts + 5;
+        i0 = mark[LEVEL_WORDS * (level > 0 ? level - 1 : F.max_depth + 1)];
+        n = mark[LEVEL_WORDS * level];
+    }
     const SkyParams& P = F.sky;
     const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = i0 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 a = F.sky_queue[2 * (size_t)i], b = F.sky_queue[2 * (size_t)i + 1];
         int item = __float_as_int(a.x);
         float3 sk = nishita(P, obs, make_float3(a.y, a.z, a.w));
