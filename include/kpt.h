@@ -249,12 +249,16 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * wave (queue capacity), 0 = 2^25; shade_block: threads per block of the
  * shading kernel (64, 128 or 256, 0 = 128); sort_rays: 1 groups each level's
  * extension rays by direction octant before they are traced, 0 keeps them in
- * pixel order (results are the same either way). */
+ * pixel order (results are the same either way); fetch_batch: in the ray
+ * kernels, the lanes of a warp whose rays are done wait until this many are
+ * (or the whole warp is) and then store their results and fetch their next
+ * rays together (1 .. 32, 0 = 8; results are the same for every value). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;
     int32_t shade_block;
     int32_t sort_rays;
+    int32_t fetch_batch;
 } kpt_tuning;
 void kpt_tuning_default(kpt_tuning* t);
 kpt_status kpt_set_tuning(kpt_context* ctx, const kpt_tuning* t);

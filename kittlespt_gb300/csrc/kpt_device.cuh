@@ -107,6 +107,7 @@ struct SceneView {
     int ntlas, nlights, ninst, ntextures;
     float4 tlas_lo, tlas_hi;  // root bounds of the TLAS
     int tlas_root_leaf;       // single instance: the TLAS root is that instance
+    int fetch_batch;          // queue traversal: finished lanes of a warp wait for this many to fetch together
 };
 
 // Nishita and sun parameters of one frame.

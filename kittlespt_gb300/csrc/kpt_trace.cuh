@@ -371,8 +371,28 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
             top = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
     };
+    bool occluded = false;   // ANY: a triangle blocked the ray
     for (;;) {
-        if (ray < 0) {
+        // a lane whose ray is done waits until fetch_batch lanes of the warp
+        // are (or all are): the result write and the next fetch and set-up
+        // then run for those lanes together instead of one lane at a time
+        const bool fin = ray < 0 || (count == 0 && inst < 0 && top == NONE && sp == 0);
+        const unsigned act = __activemask();
+        const unsigned idle = __ballot_sync(act, fin);
+        if (fin) {
+            if (idle != act && __popc(idle) < s.fetch_batch) continue;
+            if (ray >= 0) {
+                float3 o, d;
+                if (ANY) {
+                    src.any(ray, occluded);
+                    ray = -1;
+                } else if (src.closest(ray, best, o, d)) {
+                    start(o, d);   // the next ray of a bounce chain
+                    continue;
+                } else {
+                    ray = -1;
+                }
+            }
             cg::coalesced_group g = cg::coalesced_threads();
             int b = 0;
             if (g.thread_rank() == 0) b = atomicAdd(next, (int)g.size());
@@ -381,6 +401,7 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             float3 o, d;
             src.ray(ray, o, d, tmin, tmax0);
             start(o, d);
+            occluded = false;
         } else if (count > 0) {
             // one triangle of the leaf (BLAS2::intersect / intersectP leaf loop)
             float u, v;
@@ -391,9 +412,12 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             ++first;
             --count;
             if (ANY) {
-                if (t < INF) {
-                    src.any(ray, true);
-                    ray = -1;
+                if (t < INF) {   // blocked: the ray is done
+                    occluded = true;
+                    count = 0;
+                    inst = -1;
+                    top = NONE;
+                    sp = 0;
                 }
             } else if (t < loc.t) {
                 loc.t = t;
@@ -409,16 +433,6 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
             }
             inst = -1;
             r = w;
-        } else if (top == NONE && sp == 0) {
-            float3 o, d;
-            if (ANY) {
-                src.any(ray, false);
-                ray = -1;
-            } else if (src.closest(ray, best, o, d)) {
-                start(o, d);
-            } else {
-                ray = -1;
-            }
         } else {
             const int e = top != NONE ? top : stack[--sp];
             top = NONE;

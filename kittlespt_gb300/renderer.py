@@ -298,15 +298,17 @@ class Renderer:
         return g, img
 
     # -- launch parameters (no reference counterpart) -------------------------
-    def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0, sort_rays: int = 0):
-        t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block, sort_rays=sort_rays)
+    def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0, sort_rays: int = 0,
+                   fetch_batch: int = 0):
+        t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block, sort_rays=sort_rays,
+                     fetch_batch=fetch_batch)
         K.check(self._L.kpt_set_tuning(self._ctx, C.byref(t)))
 
     def tuning(self) -> dict:
         t = K.Tuning()
         K.check(self._L.kpt_get_tuning(self._ctx, C.byref(t)))
         return {"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block,
-                "sort_rays": t.sort_rays}
+                "sort_rays": t.sort_rays, "fetch_batch": t.fetch_batch}
 
 
 class Batch:
@@ -358,7 +360,7 @@ class Batch:
         K.check(self._L.kpt_autotune_batch(self._b, n, jobs, K.iptr(s), reps, C.byref(t), K.iptr(lanes),
                                            K.fptr(ms)))
         return ({"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block,
-                 "sort_rays": t.sort_rays}, int(lanes[0]), float(ms[0]))
+                 "sort_rays": t.sort_rays, "fetch_batch": t.fetch_batch}, int(lanes[0]), float(ms[0]))
 
 
 # -- path-replay adjoint (no reference counterpart) ----------------------------

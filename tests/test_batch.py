@@ -19,7 +19,7 @@ def test_tuning_defaults_and_errors():
     L = K.load()
     t = K.Tuning()
     L.kpt_tuning_default(C.byref(t))
-    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays) == (1.0, 0, 128, 0)
+    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays, t.fetch_batch) == (1.0, 0, 128, 0, 8)
     assert L.kpt_set_tuning(None, C.byref(t)) == -1
     assert L.kpt_get_tuning(None, C.byref(t)) == -1
     assert L.kpt_submit_batch(None, 1, None, None, 0) == -1
@@ -83,6 +83,8 @@ def reference_frames():
     (1, dict(grid_scale=0.25, wave_cap=1024, shade_block=64)),
     (3, dict(grid_scale=0.5, wave_cap=4096, shade_block=256, sort_rays=1)),
     (0, dict(sort_rays=1)),
+    (2, dict(fetch_batch=1)),
+    (0, dict(fetch_batch=32)),
 ])
 def test_batch_matches_one_by_one(reference_frames, lanes, tuning):
     from kittlespt_gb300.renderer import Batch
@@ -131,6 +133,8 @@ def test_batch_errors():
             rs[0].set_tuning(shade_block=96)
         with pytest.raises(K.KptError):
             rs[0].set_tuning(sort_rays=2)
+        with pytest.raises(K.KptError):
+            rs[0].set_tuning(fetch_batch=33)
     finally:
         for r in rs:
             r.shutdown()
