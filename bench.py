@@ -314,6 +314,10 @@ def run_gpu(args):
                "rays_per_s": rays_frame * args.steps * world / (ms_max / 1e3),
                "rays_per_frame": {"camera": delta("camera_rays"), "extension": delta("path_rays"),
                                   "shadow": delta("shadow_rays")},
+               "traversal_work_per_frame": {k: {"box_tests": delta(pre + "_box_tests"),
+                                                "tri_tests": delta(pre + "_tri_tests"),
+                                                "inst_xforms": delta(pre + "_inst_xforms")}
+                                            for k, pre in (("extension", "path"), ("shadow", "shadow"))},
                "cpu_baseline": cpu,
                "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 128,
                        "d2h_bytes_per_step": W * H * 16},
