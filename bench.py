@@ -583,6 +583,53 @@ def run_traversal(args):
     print(json.dumps(out))
 
 
+def run_blas(args):
+    """BLAS build time on upload (kpt_upload_mesh), host build against the
+    device build (kpt_set_blas_build), for the 2M-random-triangle mesh and
+    one 81,920-triangle displaced icosphere of the full-frame scene.  The
+    device time includes the positions' copy to the GPU and the tree's copy
+    back; both builds give the same tree (tests/test_blas_build.py)."""
+    from kittlespt_gb300 import _lib as K
+    from kittlespt_gb300 import scenes as S
+    L = K.load()
+    ctx = C.c_void_p()
+    K.check(L.kpt_create(0, C.byref(ctx)))
+    meshes = [("random_triangles_2M", S.random_triangles(2_000_000, seed=3)),
+              ("displaced_icosphere_81920", S.displaced_icosphere(subdiv=6, amplitude=0.1, seed=0))]
+    res = {}
+    try:
+        for name, m in meshes:
+            pos = np.ascontiguousarray(m.positions, np.float32).reshape(-1)
+            n = m.ntris
+            mat = np.zeros(n, np.int32)
+            out = C.c_int()
+            times = {}
+            for device, reps in ((0, 1), (1, max(1, args.steps))):
+                K.check(L.kpt_set_blas_build(ctx, device))
+                for _ in range(args.warmup if device else 0):
+                    K.check(L.kpt_upload_mesh(ctx, n, K.fptr(pos), None, None, K.iptr(mat), C.byref(out)))
+                    K.check(L.kpt_clear_scene(ctx))
+                best = float("inf")
+                for _ in range(reps):
+                    t0 = time.perf_counter()
+                    K.check(L.kpt_upload_mesh(ctx, n, K.fptr(pos), None, None, K.iptr(mat), C.byref(out)))
+                    best = min(best, time.perf_counter() - t0)
+                    K.check(L.kpt_clear_scene(ctx))
+                times["device" if device else "host"] = best * 1e3
+            res[name] = {"triangles": n, "host_ms": times["host"], "device_ms": times["device"],
+                         "speedup": times["host"] / times["device"]}
+            print(f"[bench] {name}: host {times['host']:.1f} ms, device {times['device']:.1f} ms", file=sys.stderr)
+    finally:
+        L.kpt_destroy(ctx)
+    big = res["random_triangles_2M"]
+    out = {"metric": "BLAS build, Mtriangles/s (kpt_upload_mesh with the device build, 2M random triangles)",
+           "value": big["triangles"] / big["device_ms"] / 1e3, "unit": "Mtriangles/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": big["device_ms"], "higher_is_better": True,
+           "dtype": "f32", "data": "synthetic (seeded random triangles, displaced icosphere)",
+           "config": {"workload": "blas_build"}, "builds": res}
+    print(json.dumps(out))
+
+
 def run_profile_case(spec):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
     small case that ncu captures of single kernels run on."""
@@ -606,10 +653,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "adjoint", "traversal"],
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "adjoint", "traversal", "blas"],
                     help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one; "
                          "adjoint: gradient evaluations/s of the path-replay adjoint; "
-                         "traversal: rays/s on 2M random triangles")
+                         "traversal: rays/s on 2M random triangles; blas: BLAS build on upload, host vs device")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
     args = ap.parse_args()
@@ -624,6 +671,8 @@ def main():
         run_adjoint(args)
     elif args.workload == "traversal":
         run_traversal(args)
+    elif args.workload == "blas":
+        run_blas(args)
     else:
         run_gpu(args)
 

@@ -117,6 +117,24 @@ kpt_status kpt_add_instance(kpt_context* ctx, int mesh, const float* model, int 
 kpt_status kpt_commit_scene(kpt_context* ctx);
 kpt_status kpt_clear_scene(kpt_context* ctx);
 
+/* Where kpt_upload_mesh builds a BLAS.  No counterpart in the reference,
+ * which builds every BLAS on the host (BLASBuilder, as_builder.cuh:181-261).
+ * device = 1: on the GPU, on the context's stream -- the reference's tree
+ * exactly (the same splits, child boxes and triangle order in every leaf);
+ * 0 (the default): on the host. */
+kpt_status kpt_set_blas_build(kpt_context* ctx, int device);
+
+/* The BLAS of an uploaded mesh in the device format.  info[5] = interior
+ * nodes, root node (-1: the root is a leaf), the root leaf's first triangle
+ * and count, the mesh's triangles; nodes[16 per interior node] = both children's boxes (lo xyz, hi
+ * xyz, 12 floats) then four int32 bit patterns (child 1 reference, child 1
+ * triangle count, child 2 reference, count; a count of 0 marks an interior
+ * child, whose reference is its node index, else the reference is the first
+ * triangle in leaf order), depth-first with the left child first;
+ * order[ntris] = the mesh triangle at each leaf-order position; bounds[6] =
+ * the mesh's box.  Any output but info may be null. */
+kpt_status kpt_get_blas(kpt_context* ctx, int mesh, int32_t* info, float* nodes, int32_t* order, float* bounds);
+
 /* getMaterialsCount / getMeshCount (renderer.cu:280-288); the reference's
  * meshes are this library's instances. */
 kpt_status kpt_counts(kpt_context* ctx, int* materials, int* meshes, int* instances, int* lights);

@@ -89,6 +89,8 @@ SIGNATURES = {
     "kpt_set_textures": (_S, [_P, C.c_int, _I, C.c_size_t, C.POINTER(C.c_uint8)]),
     "kpt_upload_mesh": (_S, [_P, C.c_int, _F, _F, _F, _I, C.POINTER(C.c_int)]),
     "kpt_add_instance": (_S, [_P, C.c_int, _F, C.c_int, C.POINTER(C.c_int)]),
+    "kpt_set_blas_build": (_S, [_P, C.c_int]),
+    "kpt_get_blas": (_S, [_P, C.c_int, _I, _F, _I, _F]),
     "kpt_commit_scene": (_S, [_P]),
     "kpt_clear_scene": (_S, [_P]),
     "kpt_counts": (_S, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),

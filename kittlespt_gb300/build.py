@@ -1,10 +1,11 @@
 """Builds libkpt.so (the CUDA path tracer behind include/kpt.h) in-tree.
 
-Five translation units, compiled in parallel with nvcc for sm_103a only:
+Six translation units, compiled in parallel with nvcc for sm_103a only:
 kpt_path.cu (path and ray kernels, fast maths like the reference's GPU
 build), kpt_adjoint.cu (path-replay adjoint, fast maths), kpt_post.cu (post
-chain, IEEE), kpt_api.cu (C ABI) and kpt_scene.cpp (host
-acceleration-structure build).  Host code is compiled without
+chain, IEEE), kpt_api.cu (C ABI), kpt_scene.cpp (host
+acceleration-structure build) and kpt_build.cu (the same BLAS build on the
+GPU, IEEE without contraction).  Host code is compiled without
 floating-point contraction so x86-64 and aarch64 builds agree.
 """
 
@@ -32,6 +33,7 @@ UNITS = {
     "kpt_post.cu": [],
     "kpt_api.cu": [],
     "kpt_scene.cpp": [],
+    "kpt_build.cu": ["-fmad=false"],
 }
 
 

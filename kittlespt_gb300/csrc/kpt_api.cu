@@ -142,6 +142,7 @@ struct kpt_context {
     DBuf<int> octants;
     DBuf<ShadowRec> shadow;
     int wave_cap = 0;
+    bool device_blas = false;   // kpt_set_blas_build
     kpt_tuning tuning{};   // launch parameters of the path stage (kpt_set_tuning)
 
     // stage timing inside the frame graph: per frame, event-record nodes
@@ -344,10 +345,40 @@ kpt_status kpt_upload_mesh(kpt_context* c, int ntris, const float* pos, const fl
     m.material.assign(mat, mat + ntris);
     for (int i = 0; i < ntris; ++i)
         if (mat[i] < 0) return fail(KPT_ERR_INVALID, "kpt_upload_mesh: negative material id");
-    build_blas(m);
+    if (c->device_blas) {
+        const int e = build_blas_device(m, c->stream);
+        if (e != 0) return fail(KPT_ERR_CUDA, std::string("kpt_upload_mesh: device BLAS build: ") +
+                                                  cudaGetErrorString((cudaError_t)e));
+    } else {
+        build_blas(m);
+    }
     c->meshes.push_back(std::move(m));
     if (mesh_out) *mesh_out = (int)c->meshes.size() - 1;
     c->committed = false;
+    return KPT_OK;
+}
+
+kpt_status kpt_set_blas_build(kpt_context* c, int device) {
+    if (!c || (device != 0 && device != 1)) return fail(KPT_ERR_INVALID, "kpt_set_blas_build: bad arguments");
+    c->device_blas = device == 1;
+    return KPT_OK;
+}
+
+kpt_status kpt_get_blas(kpt_context* c, int mesh, int32_t* info, float* nodes, int32_t* order, float* bounds) {
+    if (!c || !info || mesh < 0 || mesh >= (int)c->meshes.size())
+        return fail(KPT_ERR_INVALID, "kpt_get_blas: bad mesh or null info");
+    const HostMesh& m = c->meshes[mesh];
+    info[0] = (int32_t)m.nodes.size();
+    info[1] = m.root;
+    info[2] = m.leaf_first;
+    info[3] = m.leaf_count;
+    info[4] = m.ntris();
+    if (nodes && !m.nodes.empty()) std::memcpy(nodes, m.nodes.data(), m.nodes.size() * sizeof(BvhNode));
+    if (order) std::memcpy(order, m.order.data(), m.order.size() * sizeof(int32_t));
+    if (bounds) {
+        std::memcpy(bounds, m.lo, 3 * sizeof(float));
+        std::memcpy(bounds + 3, m.hi, 3 * sizeof(float));
+    }
     return KPT_OK;
 }
 

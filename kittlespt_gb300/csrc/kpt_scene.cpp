@@ -145,6 +145,55 @@ inline BvhNode make_node(const Box& b1, int r1, int c1, const Box& b2, int r2, i
 
 }  // namespace
 
+void pack_blas(HostMesh& m, const std::vector<BlasNode>& nodes, std::vector<int>&& order) {
+    const BlasNode& rb = nodes[0];
+    for (int k = 0; k < 3; ++k) {
+        m.lo[k] = rb.lo[k];
+        m.hi[k] = rb.hi[k];
+    }
+    m.order = std::move(order);
+    m.nodes.clear();
+    m.max_depth = 0;
+    if (nodes[0].count != 0) {       // the root is a leaf
+        m.root = -1;
+        m.leaf_first = 0;
+        m.leaf_count = nodes[0].count;
+        return;
+    }
+    // interior nodes in depth-first order (left first)
+    std::vector<int> dev(nodes.size(), -1);
+    std::vector<std::pair<int, int>> stack;   // (reference node, depth)
+    stack.push_back({0, 1});
+    std::vector<int> seq;
+    while (!stack.empty()) {
+        auto [ni, dep] = stack.back();
+        stack.pop_back();
+        m.max_depth = std::max(m.max_depth, dep);
+        dev[ni] = (int)seq.size();
+        seq.push_back(ni);
+        const BlasNode& n = nodes[ni];
+        int l = n.left_first, r = n.left_first + 1;
+        if (nodes[r].count == 0) stack.push_back({r, dep + 1});
+        if (nodes[l].count == 0) stack.push_back({l, dep + 1});
+    }
+    auto box = [](const BlasNode& n) {
+        Box b;
+        b.lo = {n.lo[0], n.lo[1], n.lo[2]};
+        b.hi = {n.hi[0], n.hi[1], n.hi[2]};
+        return b;
+    };
+    m.nodes.resize(seq.size());
+    for (size_t k = 0; k < seq.size(); ++k) {
+        const BlasNode& n = nodes[seq[k]];
+        const BlasNode& l = nodes[n.left_first];
+        const BlasNode& r = nodes[n.left_first + 1];
+        int lr = l.count ? l.left_first : dev[n.left_first];
+        int rr = r.count ? r.left_first : dev[n.left_first + 1];
+        m.nodes[k] = make_node(box(l), lr, l.count, box(r), rr, r.count);
+    }
+    m.root = 0;
+}
+
 void build_blas(HostMesh& m) {
     const int N = m.ntris();
     Builder b;
@@ -164,44 +213,12 @@ void build_blas(HostMesh& m) {
     b.bounds(0);
     uint32_t next = 1;
     b.subdivide(0, &next);
-    const Box& rb = b.nodes[0].b;
-    m.lo[0] = rb.lo.x; m.lo[1] = rb.lo.y; m.lo[2] = rb.lo.z;
-    m.hi[0] = rb.hi.x; m.hi[1] = rb.hi.y; m.hi[2] = rb.hi.z;
-    m.order = b.idx;
-    m.nodes.clear();
-    m.max_depth = 0;
-    if (b.nodes[0].count != 0) {       // the root is a leaf
-        m.root = -1;
-        m.leaf_first = 0;
-        m.leaf_count = (int)b.nodes[0].count;
-        return;
+    std::vector<BlasNode> nodes(next);
+    for (uint32_t k = 0; k < next; ++k) {
+        const RefNode& r = b.nodes[k];
+        nodes[k] = {r.left_first, (int)r.count, {r.b.lo.x, r.b.lo.y, r.b.lo.z}, {r.b.hi.x, r.b.hi.y, r.b.hi.z}};
     }
-    // interior nodes in depth-first order (left first)
-    std::vector<int> dev(b.nodes.size(), -1);
-    std::vector<std::pair<int, int>> stack;   // (reference node, depth)
-    stack.push_back({0, 1});
-    std::vector<int> order;
-    while (!stack.empty()) {
-        auto [ni, dep] = stack.back();
-        stack.pop_back();
-        m.max_depth = std::max(m.max_depth, dep);
-        dev[ni] = (int)order.size();
-        order.push_back(ni);
-        const RefNode& n = b.nodes[ni];
-        int l = n.left_first, r = n.left_first + 1;
-        if (b.nodes[r].count == 0) stack.push_back({r, dep + 1});
-        if (b.nodes[l].count == 0) stack.push_back({l, dep + 1});
-    }
-    m.nodes.resize(order.size());
-    for (size_t k = 0; k < order.size(); ++k) {
-        const RefNode& n = b.nodes[order[k]];
-        const RefNode& l = b.nodes[n.left_first];
-        const RefNode& r = b.nodes[n.left_first + 1];
-        int lr = l.count ? l.left_first : dev[n.left_first];
-        int rr = r.count ? r.left_first : dev[n.left_first + 1];
-        m.nodes[k] = make_node(l.b, lr, (int)l.count, r.b, rr, (int)r.count);
-    }
-    m.root = 0;
+    pack_blas(m, nodes, std::move(b.idx));
 }
 
 void inverse4(const float* m, float* out) {

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 #include <vector>
+#include <cuda_runtime.h>
 #include "kpt_device.cuh"
 
 namespace kpt {
@@ -29,6 +30,23 @@ struct HostInstance {
 
 // Binned SAH build of the reference (as_builder.cuh:110-261).
 void build_blas(HostMesh& m);
+
+// A node of the reference's BLAS array: interior (count 0) with children at
+// left_first and left_first + 1, or a leaf of `count` triangles
+// order[left_first ..].  Node 0 is the root.
+struct BlasNode {
+    int left_first;
+    int count;
+    float lo[3], hi[3];
+};
+
+// Packs a reference-form tree (nodes, triangle order) into m: device nodes
+// in depth-first order (left first), leaf ranges, root, bounds and depth.
+void pack_blas(HostMesh& m, const std::vector<BlasNode>& nodes, std::vector<int>&& order);
+
+// The same build on the GPU (kpt_build.cu): identical nodes, boxes and
+// triangle order.  Returns a CUDA error code (0 on success).
+int build_blas_device(HostMesh& m, cudaStream_t stream);
 
 // World bounds of an instance: the 8 transformed corners of the mesh bounds
 // (BLAS2::setTransform, blas.cuh:338-348).

@@ -105,6 +105,28 @@ class Renderer:
         self.set_exposure(scene.exposure)
         self.scene = scene
 
+    # -- BLAS build (no reference counterpart) --------------------------------
+    def set_blas_build(self, device: bool):
+        """Build the BLAS of meshes uploaded from now on on the GPU (True) or
+        the host (False, the default); the trees are the same."""
+        K.check(self._L.kpt_set_blas_build(self._ctx, 1 if device else 0))
+
+    def get_blas(self, mesh: int) -> dict:
+        """The device-format BLAS of an uploaded mesh: nodes (float32 [k, 12]
+        child boxes, int32 [k, 4] child references and counts), leaf order,
+        root (-1: a leaf of leaf_count triangles from leaf_first), bounds."""
+        info = np.zeros(5, np.int32)
+        K.check(self._L.kpt_get_blas(self._ctx, mesh, K.iptr(info), None, None, None))
+        k, ntris = int(info[0]), int(info[4])
+        raw = np.zeros((max(k, 1), 16), np.float32)
+        order = np.zeros(ntris, np.int32)
+        bounds = np.zeros(6, np.float32)
+        K.check(self._L.kpt_get_blas(self._ctx, mesh, K.iptr(info), K.fptr(raw.reshape(-1)), K.iptr(order),
+                                     K.fptr(bounds)))
+        return {"boxes": raw[:k, :12].copy(), "refs": raw[:k, 12:].view(np.int32).copy(),
+                "order": order, "root": int(info[1]), "leaf_first": int(info[2]),
+                "leaf_count": int(info[3]), "bounds": bounds}
+
     def get_materials_count(self) -> int:
         n = C.c_int()
         K.check(self._L.kpt_counts(self._ctx, C.byref(n), None, None, None))
