@@ -45,6 +45,10 @@ constexpr int LEAF_MAX = 8;      // a node of at most 8 triangles is a leaf (as_
 constexpr int BINS = 8;
 constexpr int BIG = 1024;        // threads per block for a large node
 constexpr int SMALL_MAX = 2048;  // larger nodes get a BIG block, smaller ones a warp
+constexpr int WIDE_MIN = 65536;  // larger nodes are split by WG blocks of WT threads each
+constexpr int WG = 256;
+constexpr int WT = 256;
+constexpr int TINY_MAX = 128;    // a node of at most this many triangles is finished by one thread
 
 struct Split {                   // outcome of one node's split
     int nl;                      // triangles going left, 0: the node stays a leaf
@@ -52,8 +56,21 @@ struct Split {                   // outcome of one node's split
 };
 
 struct Counters {                // written by k_assign, read by the host after each depth
-    int next_id, nlevel, nbig, nsmall;
+    int next_id, nlevel, nbig, nsmall, nwide, ntiny;
     int bad;                     // partition destinations outside the node (none when the closed form holds)
+};
+
+// Accumulators of one wide node, combined across its WG blocks by atomics
+// (boxes as order-preserving keys).
+struct WideAcc {
+    unsigned cmin[3], cmax[3];            // centroid bounds
+    int bn[3][BINS];                      // per axis and bin: triangles
+    unsigned blo[3][BINS][3], bhi[3][BINS][3];
+    int axis;
+    float split;
+    int nl, ev;                           // left-going count; first run that cannot complete
+    unsigned llo[3], lhi[3], rlo[3], rhi[3];
+    int boff[WG];                         // per block: left-going count, then the count before the block
 };
 
 __device__ __forceinline__ float comp(float4 c, int a) { return a == 0 ? c.x : (a == 1 ? c.y : c.z); }
@@ -169,6 +186,48 @@ __device__ __forceinline__ void grow_box(float* lo, float* hi, const float* olo,
     }
 }
 
+// The sweep of BLASBuilder::findBestSplitPlane over one axis's bins, in its
+// order of operations: left and right counts and grown boxes, cost
+// nl * Al + nr * Ar, first strict minimum (over the axes in order).
+__device__ __forceinline__ void sweep(const int* bn, const float (*blo)[3], const float (*bhi)[3], float mn,
+                                      float mx, int a, float& best, int& axis, float& split) {
+    constexpr int P = BINS - 1;
+    float la[P], ra[P];
+    int lc[P], rc[P];
+    float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int ls = 0, rs = 0;
+    for (int i = 0; i < P; ++i) {
+        ls += bn[i];
+        lc[i] = ls;
+        grow_box(llo, lhi, blo[i], bhi[i]);
+        la[i] = area(llo, lhi);
+        rs += bn[P - i];
+        rc[P - 1 - i] = rs;
+        grow_box(rlo, rhi, blo[P - i], bhi[P - i]);
+        ra[P - 1 - i] = area(rlo, rhi);
+    }
+    const float step = __fdiv_rn(__fsub_rn(mx, mn), (float)BINS);
+    for (int i = 0; i < P; ++i) {
+        const float cost = __fadd_rn(__fmul_rn((float)lc[i], la[i]), __fmul_rn((float)rc[i], ra[i]));
+        if (cost < best) {
+            axis = a;
+            split = __fadd_rn(mn, __fmul_rn(step, (float)(i + 1)));
+            best = cost;
+        }
+    }
+}
+
+// Order-preserving keys of floats for atomicMin / atomicMax on unsigned
+// (-0 below +0).
+__device__ __forceinline__ unsigned fkey(float f) {
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float kfloat(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
 __global__ void k_centroids(const float* pos, int n, float4* cen, int* order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -268,34 +327,7 @@ __global__ void __launch_bounds__(T) k_split(const float* pos, const float4* cen
                 bhi[b][q] = block_max<T>(bhi[b][q], shf);
             }
         }
-        if (threadIdx.x == 0) {
-            // the sweep of findBestSplitPlane, in its order of operations
-            constexpr int P = BINS - 1;
-            float la[P], ra[P];
-            int lc[P], rc[P];
-            float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-            float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-            int ls = 0, rs = 0;
-            for (int i = 0; i < P; ++i) {
-                ls += bn[i];
-                lc[i] = ls;
-                grow_box(llo, lhi, blo[i], bhi[i]);
-                la[i] = area(llo, lhi);
-                rs += bn[P - i];
-                rc[P - 1 - i] = rs;
-                grow_box(rlo, rhi, blo[P - i], bhi[P - i]);
-                ra[P - 1 - i] = area(rlo, rhi);
-            }
-            const float step = __fdiv_rn(__fsub_rn(mx, mn), (float)BINS);
-            for (int i = 0; i < P; ++i) {
-                const float cost = __fadd_rn(__fmul_rn((float)lc[i], la[i]), __fmul_rn((float)rc[i], ra[i]));
-                if (cost < best) {
-                    axis = a;
-                    split = __fadd_rn(mn, __fmul_rn(step, (float)(i + 1)));
-                    best = cost;
-                }
-            }
-        }
+        if (threadIdx.x == 0) sweep(bn, blo, bhi, mn, mx, a, best, axis, split);
     }
     if (threadIdx.x == 0) {
         s_axis = axis;   // -1 when no axis had distinct centroids: the reference then splits z at 0
@@ -372,15 +404,26 @@ __global__ void __launch_bounds__(T) k_split(const float* pos, const float4* cen
 }
 
 // Children of the depth's split nodes: ids next_id + 2j for the j-th split
-// node (left, then right), the next depth's list (children of more than
-// LEAF_MAX triangles, in order) and its large / small node lists.
+// node (left, then right); the next depth's list (children of more than
+// TINY_MAX triangles, in order) with its wide / large / small node lists
+// (positions in that list), and the tiny children (LEAF_MAX < count <=
+// TINY_MAX, node ids) that k_subtree finishes.
+__device__ __forceinline__ void classify(int o, int id, int count, int* wide, int* big, int* small, int* tiny,
+                                         int* nwide, int* nbig, int* nsmall, int* ntiny) {
+    if (count > WIDE_MIN) wide[atomicAdd(nwide, 1)] = o;
+    else if (count > SMALL_MAX) big[atomicAdd(nbig, 1)] = o;
+    else if (count > TINY_MAX) small[atomicAdd(nsmall, 1)] = o;
+    else if (count > LEAF_MAX) tiny[atomicAdd(ntiny, 1)] = id;
+}
+
 __global__ void __launch_bounds__(1024) k_assign(BlasNode* nodes, const int* level, int nlevel, const Split* sp,
-                                                 int* next_level, int* big, int* small, Counters* cnt) {
+                                                 int* next_level, int* wide, int* big, int* small, int* tiny,
+                                                 Counters* cnt) {
     __shared__ int shi[32];
-    __shared__ int s_next_id, s_nnext, s_nbig, s_nsmall;
+    __shared__ int s_next_id, s_nnext, s_nwide, s_nbig, s_nsmall, s_ntiny;
     if (threadIdx.x == 0) {
         s_next_id = cnt->next_id;
-        s_nnext = s_nbig = s_nsmall = 0;
+        s_nnext = s_nwide = s_nbig = s_nsmall = s_ntiny = 0;
     }
     __syncthreads();
     for (int base = 0; base < nlevel; base += 1024) {
@@ -395,8 +438,8 @@ __global__ void __launch_bounds__(1024) k_assign(BlasNode* nodes, const int* lev
         BlasNode p{};
         if (split) {
             p = nodes[level[k]];
-            la = s.nl > LEAF_MAX;
-            ra = p.count - s.nl > LEAF_MAX;
+            la = s.nl > TINY_MAX;
+            ra = p.count - s.nl > TINY_MAX;
             na = (la ? 1 : 0) + (ra ? 1 : 0);
         }
         int nact;
@@ -419,17 +462,11 @@ __global__ void __launch_bounds__(1024) k_assign(BlasNode* nodes, const int* lev
             nodes[level[k]].left_first = lid;
             nodes[level[k]].count = 0;
             int o = s_nnext + q;
-            if (la) {
-                next_level[o] = lid;
-                if (l.count > SMALL_MAX) big[atomicAdd(&s_nbig, 1)] = o;
-                else small[atomicAdd(&s_nsmall, 1)] = o;
-                ++o;
-            }
-            if (ra) {
-                next_level[o] = lid + 1;
-                if (r.count > SMALL_MAX) big[atomicAdd(&s_nbig, 1)] = o;
-                else small[atomicAdd(&s_nsmall, 1)] = o;
-            }
+            if (la) next_level[o] = lid;
+            classify(o, lid, l.count, wide, big, small, tiny, &s_nwide, &s_nbig, &s_nsmall, &s_ntiny);
+            if (la) ++o;
+            if (ra) next_level[o] = lid + 1;
+            classify(o, lid + 1, r.count, wide, big, small, tiny, &s_nwide, &s_nbig, &s_nsmall, &s_ntiny);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -441,9 +478,549 @@ __global__ void __launch_bounds__(1024) k_assign(BlasNode* nodes, const int* lev
     if (threadIdx.x == 0) {
         cnt->next_id = s_next_id;
         cnt->nlevel = s_nnext;
+        cnt->nwide = s_nwide;
         cnt->nbig = s_nbig;
-        cnt->nsmall = s_nsmall;   // cnt->bad accumulates
+        cnt->nsmall = s_nsmall;
+        cnt->ntiny = s_ntiny;   // cnt->bad accumulates
     }
+}
+
+// --- wide nodes: WG blocks per node, each over a contiguous chunk ----------
+
+__device__ __forceinline__ void wide_chunk(const BlasNode& nd, int sub, int* b, int* e) {
+    const int c = (nd.count + WG - 1) / WG;
+    *b = min(nd.count, sub * c);
+    *e = min(nd.count, *b + c);
+}
+
+__global__ void kw_init(WideAcc* acc) {
+    WideAcc& A = acc[blockIdx.x];
+    const int t = threadIdx.x;
+    if (t < 3) {
+        A.cmin[t] = fkey(INFINITY);
+        A.cmax[t] = fkey(-INFINITY);
+        A.llo[t] = A.rlo[t] = fkey(FLT_MAX);
+        A.lhi[t] = A.rhi[t] = fkey(-FLT_MAX);
+    }
+    if (t < 3 * BINS) {
+        (&A.bn[0][0])[t] = 0;
+        for (int q = 0; q < 3; ++q) {
+            (&A.blo[0][0][0])[3 * t + q] = fkey(FLT_MAX);
+            (&A.bhi[0][0][0])[3 * t + q] = fkey(-FLT_MAX);
+        }
+    }
+    if (t == 0) {
+        A.nl = 0;
+        A.ev = INT_MAX;
+    }
+}
+
+__global__ void __launch_bounds__(WT) kw_cbounds(const float4* cen, const int* order, const BlasNode* nodes,
+                                                 const int* level, const int* wide, WideAcc* acc) {
+    __shared__ float sh[32];
+    const int w = blockIdx.x / WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, blockIdx.x % WG, &b, &e);
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int p = b + threadIdx.x; p < e; p += WT) {
+        const float4 c = cen[order[nd.left_first + p]];
+        mn[0] = fminf(mn[0], c.x); mn[1] = fminf(mn[1], c.y); mn[2] = fminf(mn[2], c.z);
+        mx[0] = fmaxf(mx[0], c.x); mx[1] = fmaxf(mx[1], c.y); mx[2] = fmaxf(mx[2], c.z);
+    }
+    for (int a = 0; a < 3; ++a) {
+        const float lo = block_min<WT>(mn[a], sh), hi = block_max<WT>(mx[a], sh);
+        if (threadIdx.x == 0 && b < e) {
+            atomicMin(&acc[w].cmin[a], fkey(lo));
+            atomicMax(&acc[w].cmax[a], fkey(hi));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(WT) kw_bins(const float* pos, const float4* cen, const int* order,
+                                              const BlasNode* nodes, const int* level, const int* wide, WideAcc* acc) {
+    __shared__ float shf[32];
+    __shared__ int shi[32];
+    const int w = blockIdx.x / WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, blockIdx.x % WG, &b, &e);
+    WideAcc& A = acc[w];
+    for (int a = 0; a < 3; ++a) {
+        const float mn = kfloat(A.cmin[a]), mx = kfloat(A.cmax[a]);
+        if (mn == mx) continue;
+        const float scale = __fdiv_rn((float)BINS, __fsub_rn(mx, mn));
+        int bn[BINS];
+        float blo[BINS][3], bhi[BINS][3];
+#pragma unroll
+        for (int k = 0; k < BINS; ++k) {
+            bn[k] = 0;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                blo[k][q] = FLT_MAX;
+                bhi[k][q] = -FLT_MAX;
+            }
+        }
+        for (int p = b + threadIdx.x; p < e; p += WT) {
+            const int t = order[nd.left_first + p];
+            const int bi = min(BINS - 1, __float2int_rz(__fmul_rn(__fsub_rn(comp(cen[t], a), mn), scale)));
+            const float* v = pos + 9 * (size_t)t;
+            float tl[3], th[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                tl[q] = fminf(fminf(v[q], v[3 + q]), v[6 + q]);
+                th[q] = fmaxf(fmaxf(v[q], v[3 + q]), v[6 + q]);
+            }
+#pragma unroll
+            for (int k = 0; k < BINS; ++k) {
+                if (bi == k) {
+                    bn[k]++;
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        blo[k][q] = fminf(blo[k][q], tl[q]);
+                        bhi[k][q] = fmaxf(bhi[k][q], th[q]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < BINS; ++k) {
+            const int c = block_sum<WT>(bn[k], shi);
+            float lo[3], hi[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                lo[q] = block_min<WT>(blo[k][q], shf);
+                hi[q] = block_max<WT>(bhi[k][q], shf);
+            }
+            if (threadIdx.x == 0 && c) {
+                atomicAdd(&A.bn[a][k], c);
+                for (int q = 0; q < 3; ++q) {
+                    atomicMin(&A.blo[a][k][q], fkey(lo[q]));
+                    atomicMax(&A.bhi[a][k][q], fkey(hi[q]));
+                }
+            }
+        }
+    }
+}
+
+__global__ void kw_decide(WideAcc* acc, int nw) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    WideAcc& A = acc[w];
+    float best = INFINITY, split = 0.0f;
+    int axis = -1;
+    for (int a = 0; a < 3; ++a) {
+        const float mn = kfloat(A.cmin[a]), mx = kfloat(A.cmax[a]);
+        if (mn == mx) continue;
+        float blo[BINS][3], bhi[BINS][3];
+        for (int k = 0; k < BINS; ++k)
+            for (int q = 0; q < 3; ++q) {
+                blo[k][q] = kfloat(A.blo[a][k][q]);
+                bhi[k][q] = kfloat(A.bhi[a][k][q]);
+            }
+        sweep(A.bn[a], blo, bhi, mn, mx, a, best, axis, split);
+    }
+    A.axis = axis;
+    A.split = split;
+}
+
+__global__ void __launch_bounds__(WT) kw_count(const float4* cen, const int* order, const BlasNode* nodes,
+                                               const int* level, const int* wide, WideAcc* acc) {
+    __shared__ int shi[32];
+    const int w = blockIdx.x / WG, sub = blockIdx.x % WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, sub, &b, &e);
+    WideAcc& A = acc[w];
+    const int axis = A.axis;
+    const float split = A.split;
+    int c = 0;
+    for (int p = b + threadIdx.x; p < e; p += WT) c += comp(cen[order[nd.left_first + p]], axis) < split ? 1 : 0;
+    c = block_sum<WT>(c, shi);
+    if (threadIdx.x == 0) {
+        A.boff[sub] = c;
+        atomicAdd(&A.nl, c);
+    }
+}
+
+// one warp per node: the per-block counts become the counts before each block
+__global__ void kw_offsets(WideAcc* acc) {
+    WideAcc& A = acc[blockIdx.x];
+    int carry = 0;
+    for (int base = 0; base < WG; base += 32) {
+        const int v = A.boff[base + threadIdx.x];
+        int tot;
+        const int x = block_scan<32>(v, nullptr, &tot);
+        A.boff[base + threadIdx.x] = carry + x;
+        carry += tot;
+    }
+}
+
+__global__ void __launch_bounds__(WT) kw_rank(const float4* cen, const int* order, int* xr, int* yl, int* rank,
+                                              const BlasNode* nodes, const int* level, const int* wide,
+                                              const WideAcc* acc) {
+    __shared__ int shi[32];
+    const int w = blockIdx.x / WG, sub = blockIdx.x % WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, sub, &b, &e);
+    const WideAcc& A = acc[w];
+    const int f = nd.left_first, n = nd.count, nl = A.nl, axis = A.axis;
+    const float split = A.split;
+    int carry_l = A.boff[sub];
+    for (int base = b; base < e; base += WT) {
+        const int p = base + threadIdx.x;
+        const bool in = p < e;
+        const bool left = in && comp(cen[order[f + p]], axis) < split;
+        int tot;
+        const int lb = carry_l + block_scan<WT>(left ? 1 : 0, shi, &tot);
+        if (in) {
+            if (left) {
+                const int m = nl - lb;
+                yl[f + m - 1] = n - p;
+                rank[f + p] = m;
+            } else {
+                const int m = p - lb + 1;
+                xr[f + m - 1] = p;
+                rank[f + p] = m;
+            }
+        }
+        carry_l += tot;
+    }
+}
+
+__global__ void __launch_bounds__(WT) kw_meet(const int* xr, const int* yl, const BlasNode* nodes, const int* level,
+                                              const int* wide, WideAcc* acc) {
+    __shared__ int shi[32];
+    const int w = blockIdx.x / WG, sub = blockIdx.x % WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    WideAcc& A = acc[w];
+    const int f = nd.left_first, n = nd.count, nl = A.nl, nr = n - nl;
+    const int mmax = min(nr, nl) + 1;
+    int ev = INT_MAX;
+    for (int m = 1 + sub * WT + threadIdx.x; m <= mmax; m += WG * WT) {
+        const int ylp = m > 1 ? yl[f + m - 2] : 0;
+        if (m > nr || xr[f + m - 1] >= n - ylp) ev = min(ev, 2 * m - 1);
+        else if (m > nl || n - yl[f + m - 1] <= xr[f + m - 1]) ev = min(ev, 2 * m);
+    }
+    ev = block_min_int<WT>(ev, shi);
+    if (threadIdx.x == 0 && ev != INT_MAX) atomicMin(&A.ev, ev);
+}
+
+__global__ void __launch_bounds__(WT) kw_scatter(const float4* cen, const int* order, int* tmp, const int* xr,
+                                                 const int* yl, const int* rank, const BlasNode* nodes,
+                                                 const int* level, const int* wide, const WideAcc* acc,
+                                                 Counters* cnt) {
+    const int w = blockIdx.x / WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, blockIdx.x % WG, &b, &e);
+    const WideAcc& A = acc[w];
+    const int f = nd.left_first, n = nd.count, axis = A.axis, ev = A.ev;
+    const float split = A.split;
+    const int me = (ev + 1) >> 1;
+    const int a = (ev & 1) ? n - (me > 1 ? yl[f + me - 2] : 0) : xr[f + me - 1] + 1;
+    for (int p = b + threadIdx.x; p < e; p += WT) {
+        const bool left = comp(cen[order[f + p]], axis) < split;
+        const int m = rank[f + p];
+        int dst;
+        if (p < a) dst = left ? p : n - 1 - (m > 1 ? yl[f + m - 2] : 0);
+        else dst = left ? xr[f + m - 1] : p - 1;
+        if (dst < 0 || dst >= n) {   // cannot happen; guards the write
+            atomicAdd(&cnt->bad, 1);
+            continue;
+        }
+        tmp[f + dst] = order[f + p];
+    }
+}
+
+__global__ void __launch_bounds__(WT) kw_copy(int* order, const int* tmp, const BlasNode* nodes, const int* level,
+                                              const int* wide) {
+    const int w = blockIdx.x / WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, blockIdx.x % WG, &b, &e);
+    for (int p = b + threadIdx.x; p < e; p += WT) order[nd.left_first + p] = tmp[nd.left_first + p];
+}
+
+__global__ void __launch_bounds__(WT) kw_cbox(const float* pos, const int* order, const BlasNode* nodes,
+                                              const int* level, const int* wide, WideAcc* acc) {
+    __shared__ float sh[32];
+    const int w = blockIdx.x / WG;
+    const BlasNode nd = nodes[level[wide[w]]];
+    int b, e;
+    wide_chunk(nd, blockIdx.x % WG, &b, &e);
+    WideAcc& A = acc[w];
+    const int nl = A.nl;
+    if (nl == 0 || nl == nd.count) return;   // uniform in the block
+    float l[2][3], h[2][3];
+    for (int s = 0; s < 2; ++s)
+        for (int q = 0; q < 3; ++q) {
+            l[s][q] = FLT_MAX;
+            h[s][q] = -FLT_MAX;
+        }
+    for (int p = b + threadIdx.x; p < e; p += WT) {
+        const float* v = pos + 9 * (size_t)order[nd.left_first + p];
+        const int s = p < nl ? 0 : 1;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            if (s == 0) {
+                l[0][k % 3] = fminf(l[0][k % 3], v[k]);
+                h[0][k % 3] = fmaxf(h[0][k % 3], v[k]);
+            } else {
+                l[1][k % 3] = fminf(l[1][k % 3], v[k]);
+                h[1][k % 3] = fmaxf(h[1][k % 3], v[k]);
+            }
+        }
+    }
+    for (int s = 0; s < 2; ++s)
+        for (int q = 0; q < 3; ++q) {
+            const float lo = block_min<WT>(l[s][q], sh), hi = block_max<WT>(h[s][q], sh);
+            if (threadIdx.x == 0 && lo <= hi) {   // the chunk holds triangles of side s
+                atomicMin(s ? &A.rlo[q] : &A.llo[q], fkey(lo));
+                atomicMax(s ? &A.rhi[q] : &A.lhi[q], fkey(hi));
+            }
+        }
+}
+
+__global__ void kw_finish(const WideAcc* acc, const BlasNode* nodes, const int* level, const int* wide, int nw,
+                          Split* out) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    const WideAcc& A = acc[w];
+    const int n = nodes[level[wide[w]]].count;
+    Split s;
+    s.nl = (A.nl == 0 || A.nl == n) ? 0 : A.nl;
+    for (int q = 0; q < 3; ++q) {
+        s.llo[q] = kfloat(A.llo[q]);
+        s.lhi[q] = kfloat(A.lhi[q]);
+        s.rlo[q] = kfloat(A.rlo[q]);
+        s.rhi[q] = kfloat(A.rhi[q]);
+    }
+    out[wide[w]] = s;
+}
+
+// --- tiny nodes: one warp finishes the node's subtree ----------------------
+// BLASBuilder::subdivide as the host runs it (as_builder.cuh:181-233) over
+// the node's triangles held in shared memory: per split the lanes find the
+// centroid bounds, 24 lanes build one (axis, bin) each, lane 0 sweeps and
+// runs the in-place partition itself, the lanes reduce the children's
+// boxes; children are numbered from the shared counter.  One block (one
+// warp) per tiny node; all control flow below is uniform in the block.
+__global__ void __launch_bounds__(32) k_subtree(const float* pos, const float4* cen, int* order, BlasNode* nodes,
+                                                const int* tiny, Counters* cnt) {
+    __shared__ float s_c[TINY_MAX][3], s_lo[TINY_MAX][3], s_hi[TINY_MAX][3];
+    __shared__ int s_id[TINY_MAX], s_perm[TINY_MAX], s_stack[TINY_MAX];
+    __shared__ int s_bn[3][BINS];
+    __shared__ float s_blo[3][BINS][3], s_bhi[3][BINS][3];
+    __shared__ int s_nl, s_lid;
+    const int lane = threadIdx.x;
+    const int root = tiny[blockIdx.x];
+    const BlasNode r0 = nodes[root];
+    const int f0 = r0.left_first, n0 = r0.count;
+    for (int p = lane; p < n0; p += 32) {
+        const int t = order[f0 + p];
+        const float4 c = cen[t];
+        const float* v = pos + 9 * (size_t)t;
+        s_c[p][0] = c.x;
+        s_c[p][1] = c.y;
+        s_c[p][2] = c.z;
+        for (int q = 0; q < 3; ++q) {
+            s_lo[p][q] = fminf(fminf(v[q], v[3 + q]), v[6 + q]);
+            s_hi[p][q] = fmaxf(fmaxf(v[q], v[3 + q]), v[6 + q]);
+        }
+        s_id[p] = t;
+        s_perm[p] = p;
+    }
+    if (lane == 0) s_stack[0] = root;
+    int sp = 1;
+    __syncthreads();
+    while (sp > 0) {
+        const int ni = s_stack[--sp];
+        const BlasNode nd = nodes[ni];
+        const int lf = nd.left_first - f0, n = nd.count;
+        // centroid bounds per axis
+        float mn[3], mx[3];
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = INFINITY;
+            mx[a] = -INFINITY;
+        }
+        for (int p = lane; p < n; p += 32) {
+            const int el = s_perm[lf + p];
+            for (int a = 0; a < 3; ++a) {
+                mn[a] = fminf(mn[a], s_c[el][a]);
+                mx[a] = fmaxf(mx[a], s_c[el][a]);
+            }
+        }
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = block_min<32>(mn[a], nullptr);
+            mx[a] = block_max<32>(mx[a], nullptr);
+        }
+        // lane 8a + k: bin k of axis a
+        if (lane < 3 * BINS) {
+            const int a = lane / BINS, k = lane % BINS;
+            int c = 0;
+            float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            if (mn[a] != mx[a]) {
+                const float scale = __fdiv_rn((float)BINS, __fsub_rn(mx[a], mn[a]));
+                for (int p = 0; p < n; ++p) {
+                    const int el = s_perm[lf + p];
+                    const int bi = min(BINS - 1, __float2int_rz(__fmul_rn(__fsub_rn(s_c[el][a], mn[a]), scale)));
+                    if (bi == k) {
+                        c++;
+                        for (int q = 0; q < 3; ++q) {
+                            lo[q] = fminf(lo[q], s_lo[el][q]);
+                            hi[q] = fmaxf(hi[q], s_hi[el][q]);
+                        }
+                    }
+                }
+            }
+            s_bn[a][k] = c;
+            for (int q = 0; q < 3; ++q) {
+                s_blo[a][k][q] = lo[q];
+                s_bhi[a][k][q] = hi[q];
+            }
+        }
+        __syncthreads();
+        if (lane == 0) {
+            float best = INFINITY, split = 0.0f;
+            int axis = -1;
+            for (int a = 0; a < 3; ++a)
+                if (mn[a] != mx[a]) sweep(s_bn[a], s_blo[a], s_bhi[a], mn[a], mx[a], a, best, axis, split);
+            const int ax = axis < 0 ? 2 : axis;   // comp() reads z for axis -1
+            int l = lf, r = lf + n - 1;
+            while (l <= r) {
+                if (s_c[s_perm[l]][ax] < split) {
+                    l++;
+                } else {
+                    const int x = s_perm[l];
+                    s_perm[l] = s_perm[r];
+                    s_perm[r--] = x;
+                }
+            }
+            s_nl = l - lf;
+            s_lid = (s_nl == 0 || s_nl == n) ? -1 : atomicAdd(&cnt->next_id, 2);
+        }
+        __syncthreads();
+        const int nl = s_nl, lid = s_lid;
+        if (lid < 0) continue;   // a leaf: uniform in the block
+        float lo[2][3], hi[2][3];
+        for (int s2 = 0; s2 < 2; ++s2)
+            for (int q = 0; q < 3; ++q) {
+                lo[s2][q] = FLT_MAX;
+                hi[s2][q] = -FLT_MAX;
+            }
+        for (int p = lane; p < n; p += 32) {
+            const int el = s_perm[lf + p];
+            const int s2 = p < nl ? 0 : 1;
+            for (int q = 0; q < 3; ++q) {
+                lo[s2][q] = fminf(lo[s2][q], s_lo[el][q]);
+                hi[s2][q] = fmaxf(hi[s2][q], s_hi[el][q]);
+            }
+        }
+        for (int s2 = 0; s2 < 2; ++s2)
+            for (int q = 0; q < 3; ++q) {
+                lo[s2][q] = block_min<32>(lo[s2][q], nullptr);
+                hi[s2][q] = block_max<32>(hi[s2][q], nullptr);
+            }
+        if (lane == 0) {
+            BlasNode c[2];
+            c[0].left_first = nd.left_first;
+            c[0].count = nl;
+            c[1].left_first = nd.left_first + nl;
+            c[1].count = n - nl;
+            for (int s2 = 0; s2 < 2; ++s2)
+                for (int q = 0; q < 3; ++q) {
+                    c[s2].lo[q] = lo[s2][q];
+                    c[s2].hi[q] = hi[s2][q];
+                }
+            nodes[lid] = c[0];
+            nodes[lid + 1] = c[1];
+            nodes[ni].left_first = lid;
+            nodes[ni].count = 0;
+        }
+        // children with more than LEAF_MAX triangles: right pushed first, so left is taken next
+        if (n - nl > LEAF_MAX) {
+            if (lane == 0) s_stack[sp] = lid + 1;
+            ++sp;
+        }
+        if (nl > LEAF_MAX) {
+            if (lane == 0) s_stack[sp] = lid;
+            ++sp;
+        }
+        __syncthreads();
+    }
+    for (int p = lane; p < n0; p += 32) order[f0 + p] = s_id[s_perm[p]];
+}
+
+// --- packing into the device format (pack_blas of kpt_scene.cpp) ------------
+// Interior nodes are numbered depth first, left child first: the left child
+// of v is dfs(v) + 1, the right one dfs(v) + 1 + (interior nodes under the
+// left child).  Children always have larger ids than their parent.
+
+__global__ void k_parents(const BlasNode* nodes, int nn, int* parent, int* need) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn) return;
+    if (v == 0) parent[0] = -1;
+    const BlasNode nd = nodes[v];
+    need[v] = 0;
+    if (nd.count != 0) return;
+    parent[nd.left_first] = v;
+    parent[nd.left_first + 1] = v;
+    need[v] = (nodes[nd.left_first].count == 0 ? 1 : 0) + (nodes[nd.left_first + 1].count == 0 ? 1 : 0);
+}
+
+// interior nodes under and including each interior node, bottom up: a node
+// is finished by the thread of the last of its interior children to finish
+__global__ void k_sizes(const BlasNode* nodes, int nn, const int* parent, const int* need, int* size, int* arrive) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn || nodes[v].count != 0 || need[v] != 0) return;
+    int c = v;
+    size[c] = 1;
+    for (;;) {
+        const int p = parent[c];
+        if (p < 0) break;
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1) + 1 != need[p]) break;   // the other interior child finishes p
+        __threadfence();
+        const int l = nodes[p].left_first;
+        const int sl = nodes[l].count == 0 ? ((volatile int*)size)[l] : 0;
+        const int sr = nodes[l + 1].count == 0 ? ((volatile int*)size)[l + 1] : 0;
+        size[p] = 1 + sl + sr;
+        c = p;
+    }
+}
+
+__device__ __forceinline__ int dfs_index(const BlasNode* nodes, const int* parent, const int* size, int v,
+                                         int* depth) {
+    int d = 0, k = 1;
+    for (int c = v, p = parent[v]; p >= 0; c = p, p = parent[p]) {
+        const int l = nodes[p].left_first;
+        d += c == l ? 1 : 1 + (nodes[l].count == 0 ? size[l] : 0);
+        ++k;
+    }
+    *depth = k;
+    return d;
+}
+
+__global__ void k_pack(const BlasNode* nodes, int nn, const int* parent, const int* size, BvhNode* out,
+                       int* max_depth) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn) return;
+    const BlasNode nd = nodes[v];
+    if (nd.count != 0) return;
+    int dep, dl, dr;
+    const int dv = dfs_index(nodes, parent, size, v, &dep);
+    atomicMax(max_depth, dep);
+    const BlasNode l = nodes[nd.left_first], r = nodes[nd.left_first + 1];
+    dl = dv + 1;
+    dr = dv + 1 + (l.count == 0 ? size[nd.left_first] : 0);
+    BvhNode o;
+    o.a = make_float4(l.lo[0], l.lo[1], l.lo[2], l.hi[0]);
+    o.b = make_float4(l.hi[1], l.hi[2], r.lo[0], r.lo[1]);
+    o.c = make_float4(r.lo[2], r.hi[0], r.hi[1], r.hi[2]);
+    o.d = make_int4(l.count ? l.left_first : dl, l.count, r.count ? r.left_first : dr, r.count);
+    out[dv] = o;
 }
 
 template <class X>
@@ -461,16 +1038,19 @@ int build_blas_device(HostMesh& m, cudaStream_t st) {
     const int N = m.ntris();
     if (N <= 0) return (int)cudaErrorInvalidValue;
     const size_t lcap = (size_t)N / (LEAF_MAX + 1) + 2;   // nodes of one depth with more than LEAF_MAX triangles
+    const size_t wcap = (size_t)N / WIDE_MIN + 2;
     DevArray<float> pos;
     DevArray<float4> cen;
-    DevArray<int> order, tmp, xr, yl, rank, level, next_level, big, small;
+    DevArray<int> order, tmp, xr, yl, rank, level, next_level, wide, big, small, tiny;
     DevArray<BlasNode> nodes;
     DevArray<Split> sp;
+    DevArray<WideAcc> acc;
     DevArray<Counters> cnt;
     cudaError_t e = cudaSuccess;
     for (cudaError_t r : {pos.alloc(9 * (size_t)N), cen.alloc(N), order.alloc(N), tmp.alloc(N), xr.alloc(N),
                           yl.alloc(N), rank.alloc(N), nodes.alloc(2 * (size_t)N), level.alloc(lcap),
-                          next_level.alloc(lcap), big.alloc(lcap), small.alloc(lcap), sp.alloc(lcap), cnt.alloc(1)})
+                          next_level.alloc(lcap), wide.alloc(wcap), big.alloc(lcap), small.alloc(lcap),
+                          tiny.alloc(lcap), sp.alloc(lcap), acc.alloc(wcap), cnt.alloc(1)})
         if (r != cudaSuccess && e == cudaSuccess) e = r;
     if (e != cudaSuccess) return (int)e;
     e = cudaMemcpyAsync(pos.p, m.pos.data(), 9 * (size_t)N * sizeof(float), cudaMemcpyHostToDevice, st);
@@ -479,23 +1059,46 @@ int build_blas_device(HostMesh& m, cudaStream_t st) {
     k_root<<<1, BIG, 0, st>>>(pos.p, order.p, N, nodes.p);
     int nodes_used = 1;
     if (N > LEAF_MAX) {
-        // depth 0: the root alone
+        // depth 0: the root alone, in the list its size picks
         const int zero = 0;
-        Counters c{1, 1, N > SMALL_MAX ? 1 : 0, N > SMALL_MAX ? 0 : 1, 0};
+        Counters c{1, N > TINY_MAX ? 1 : 0, 0, 0, 0, 0, 0};
+        int* first_list = N > WIDE_MIN ? wide.p : N > SMALL_MAX ? big.p : N > TINY_MAX ? small.p : tiny.p;
+        (N > WIDE_MIN ? c.nwide : N > SMALL_MAX ? c.nbig : N > TINY_MAX ? c.nsmall : c.ntiny) = 1;
         e = cudaMemcpyAsync(level.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(N > SMALL_MAX ? big.p : small.p, &zero, sizeof(int),
-                                                  cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(first_list, &zero, sizeof(int), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.p, &c, sizeof c, cudaMemcpyHostToDevice, st);
         int* cur = level.p;
         int* nxt = next_level.p;
-        while (e == cudaSuccess && c.nlevel > 0) {
+        while (e == cudaSuccess && (c.nlevel > 0 || c.ntiny > 0)) {
+            if (c.ntiny) k_subtree<<<c.ntiny, 32, 0, st>>>(pos.p, cen.p, order.p, nodes.p, tiny.p, cnt.p);
+            if (c.nlevel == 0) {
+                e = cudaMemcpyAsync(&c, cnt.p, sizeof c, cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                break;
+            }
+            if (c.nwide) {
+                const int g = c.nwide * WG;
+                kw_init<<<c.nwide, 32, 0, st>>>(acc.p);
+                kw_cbounds<<<g, WT, 0, st>>>(cen.p, order.p, nodes.p, cur, wide.p, acc.p);
+                kw_bins<<<g, WT, 0, st>>>(pos.p, cen.p, order.p, nodes.p, cur, wide.p, acc.p);
+                kw_decide<<<(c.nwide + 31) / 32, 32, 0, st>>>(acc.p, c.nwide);
+                kw_count<<<g, WT, 0, st>>>(cen.p, order.p, nodes.p, cur, wide.p, acc.p);
+                kw_offsets<<<c.nwide, 32, 0, st>>>(acc.p);
+                kw_rank<<<g, WT, 0, st>>>(cen.p, order.p, xr.p, yl.p, rank.p, nodes.p, cur, wide.p, acc.p);
+                kw_meet<<<g, WT, 0, st>>>(xr.p, yl.p, nodes.p, cur, wide.p, acc.p);
+                kw_scatter<<<g, WT, 0, st>>>(cen.p, order.p, tmp.p, xr.p, yl.p, rank.p, nodes.p, cur, wide.p, acc.p,
+                                             cnt.p);
+                kw_copy<<<g, WT, 0, st>>>(order.p, tmp.p, nodes.p, cur, wide.p);
+                kw_cbox<<<g, WT, 0, st>>>(pos.p, order.p, nodes.p, cur, wide.p, acc.p);
+                kw_finish<<<(c.nwide + 31) / 32, 32, 0, st>>>(acc.p, nodes.p, cur, wide.p, c.nwide, sp.p);
+            }
             if (c.nbig)
                 k_split<BIG><<<c.nbig, BIG, 0, st>>>(pos.p, cen.p, order.p, tmp.p, xr.p, yl.p, rank.p, nodes.p, cur,
                                                    big.p, sp.p, cnt.p);
             if (c.nsmall)
                 k_split<32><<<c.nsmall, 32, 0, st>>>(pos.p, cen.p, order.p, tmp.p, xr.p, yl.p, rank.p, nodes.p, cur,
                                                    small.p, sp.p, cnt.p);
-            k_assign<<<1, 1024, 0, st>>>(nodes.p, cur, c.nlevel, sp.p, nxt, big.p, small.p, cnt.p);
+            k_assign<<<1, 1024, 0, st>>>(nodes.p, cur, c.nlevel, sp.p, nxt, wide.p, big.p, small.p, tiny.p, cnt.p);
             e = cudaMemcpyAsync(&c, cnt.p, sizeof c, cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             std::swap(cur, nxt);
@@ -506,14 +1109,43 @@ int build_blas_device(HostMesh& m, cudaStream_t st) {
     if (e != cudaSuccess) return (int)e;
     e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
-    std::vector<BlasNode> h_nodes(nodes_used);
-    std::vector<int> h_order(N);
-    e = cudaMemcpyAsync(h_nodes.data(), nodes.p, nodes_used * sizeof(BlasNode), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h_order.data(), order.p, (size_t)N * sizeof(int), cudaMemcpyDeviceToHost, st);
+    // the device format, as pack_blas writes it
+    BlasNode root;
+    e = cudaMemcpyAsync(&root, nodes.p, sizeof root, cudaMemcpyDeviceToHost, st);
+    const int ninterior = (nodes_used - 1) / 2;
+    DevArray<int> parent, need, size, arrive, depth;
+    DevArray<BvhNode> packed;
+    for (cudaError_t r : {parent.alloc(nodes_used), need.alloc(nodes_used), size.alloc(nodes_used),
+                          arrive.alloc(nodes_used), depth.alloc(1), packed.alloc(ninterior)})
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
+    if (e == cudaSuccess) e = cudaMemsetAsync(arrive.p, 0, nodes_used * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(depth.p, 0, sizeof(int), st);
+    if (e != cudaSuccess) return (int)e;
+    const int gb = (nodes_used + 255) / 256;
+    k_parents<<<gb, 256, 0, st>>>(nodes.p, nodes_used, parent.p, need.p);
+    k_sizes<<<gb, 256, 0, st>>>(nodes.p, nodes_used, parent.p, need.p, size.p, arrive.p);
+    k_pack<<<gb, 256, 0, st>>>(nodes.p, nodes_used, parent.p, size.p, packed.p, depth.p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+    m.nodes.resize(ninterior);
+    m.order.resize(N);
+    if (ninterior) e = cudaMemcpyAsync(m.nodes.data(), packed.p, ninterior * sizeof(BvhNode), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m.order.data(), order.p, (size_t)N * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&m.max_depth, depth.p, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return (int)e;
-    pack_blas(m, h_nodes, std::move(h_order));
+    for (int k = 0; k < 3; ++k) {
+        m.lo[k] = root.lo[k];
+        m.hi[k] = root.hi[k];
+    }
+    if (root.count != 0) {   // the root is a leaf
+        m.root = -1;
+        m.leaf_first = 0;
+        m.leaf_count = root.count;
+        m.max_depth = 0;
+    } else {
+        m.root = 0;
+    }
     return 0;
 }
 
