@@ -104,8 +104,8 @@ struct ProceduralEnvironmentSettings {
     float sun_emission_factor = 1.0f;
 };
 
-// pod_types.hpp:46-57 (temporal accumulation, effects and upscale are not
-// part of this path and are ignored)
+// pod_types.hpp:46-57 (effects and upscale are not supported: setting them
+// fails)
 struct RendererSettings {
     int32_t integrator_max_ray_depth = 3;
     bool integrator_use_temporal_accumulation = false;
@@ -382,6 +382,9 @@ public:
         s.auto_exposure = r.tonemapper_enable_auto_exposure;
         s.bloom_final_blend = r.bloom_final_blend;
         s.bloom_internal_blend = r.bloom_internal_blend;
+        s.temporal_accumulation = r.integrator_use_temporal_accumulation;
+        s.postprocess_effects = r.postprocess_enable_effects;
+        s.upscale = r.upscale_enable;
         detail::check(kpt_set_settings(ctx(), &s));
     }
     RendererSettings getRendererSettings() const {
@@ -394,6 +397,9 @@ public:
         r.tonemapper_enable_auto_exposure = s.auto_exposure != 0;
         r.bloom_final_blend = s.bloom_final_blend;
         r.bloom_internal_blend = s.bloom_internal_blend;
+        r.integrator_use_temporal_accumulation = s.temporal_accumulation != 0;
+        r.postprocess_enable_effects = s.postprocess_effects != 0;
+        r.upscale_enable = s.upscale != 0;
         return r;
     }
 

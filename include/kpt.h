@@ -59,14 +59,27 @@ typedef struct kpt_environment {
     float pad;
 } kpt_environment;
 
-/* RendererSettings (pod_types.hpp:46-57); the temporal, upscale and effects
- * switches of the reference are not part of this path. */
+/* RendererSettings (pod_types.hpp:46-57).
+ * temporal_accumulation: the reference's integrator_use_temporal_accumulation
+ * (kernels.cu:164-327, :422-428): every sample is one reference frame; its
+ * radiance is blended into the previous frame's image reprojected along the
+ * visible surface's motion (camera and instance transforms), with depth
+ * rejection and a history of at most 16 frames, instead of the running mean.
+ * In this mode setting the view or an instance transform keeps the history
+ * (other setters clear it, as in the reference).  The first camera a context
+ * receives is its own previous camera.
+ * postprocess_effects, upscale: the reference's effects and upscale switches
+ * (not supported: KPT_ERR_INVALID when set). */
 typedef struct kpt_settings {
     int32_t max_depth;
     int32_t bloom, karis, auto_exposure;
     float bloom_final_blend, bloom_internal_blend;
     float frame_delta_ms;
     int32_t rng_order;         /* argument order of the reference's paired RNG draws: 0 left-to-right, 1 right-to-left */
+    int32_t temporal_accumulation;
+    int32_t postprocess_effects;
+    int32_t upscale;
+    int32_t pad;
 } kpt_settings;
 
 /* ExposureValues (pod_types.hpp:9-33) with the compensation and white/black

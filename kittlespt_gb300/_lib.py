@@ -44,7 +44,9 @@ class Environment(C.Structure):
 class Settings(C.Structure):
     _fields_ = [("max_depth", C.c_int32), ("bloom", C.c_int32), ("karis", C.c_int32),
                 ("auto_exposure", C.c_int32), ("bloom_final_blend", C.c_float),
-                ("bloom_internal_blend", C.c_float), ("frame_delta_ms", C.c_float), ("rng_order", C.c_int32)]
+                ("bloom_internal_blend", C.c_float), ("frame_delta_ms", C.c_float), ("rng_order", C.c_int32),
+                ("temporal_accumulation", C.c_int32), ("postprocess_effects", C.c_int32), ("upscale", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 class Exposure(C.Structure):
@@ -70,7 +72,7 @@ class Tuning(C.Structure):
 
 
 assert C.sizeof(Material) == 72 and C.sizeof(Environment) == 48
-assert C.sizeof(Settings) == 32 and C.sizeof(Exposure) == 48
+assert C.sizeof(Settings) == 48 and C.sizeof(Exposure) == 48
 
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)

@@ -110,6 +110,7 @@ struct kpt_context {
 
     // camera and settings
     float inv_proj[16], inv_view[16];
+    float prev_inv_proj[16], prev_inv_view[16];   // Camera::prev_* (camera.cuh:27-35)
     bool has_camera = false;
     kpt_environment env;
     kpt_settings settings;
@@ -119,6 +120,15 @@ struct kpt_context {
     int W = 0, H = 0;
     int frame_index = 0;
     DBuf<float4> acc, albedo, render, image;
+    // temporal accumulation: visible surface, distances of the previous frame
+    // and this one, history images (color, frames), per-instance matrices
+    DBuf<float4> vis, thist[2];
+    DBuf<float> tdepth[2];
+    int tdepth_prev = 0;
+    DBuf<TemporalInst> tinst;
+    std::vector<TemporalInst> h_tinst;
+    float4 tvp[2][4];           // current view-projection rows (the same for both)
+    float3 torigin[2];          // previous camera position: first sample, later samples
     DBuf<int4> first_hit;
     std::vector<DBuf<float4>> mips;
     std::vector<int2> mip_dims;
@@ -194,6 +204,10 @@ void kpt_settings_default(kpt_settings* s) {   // pod_types.hpp:46-57
     s->bloom_internal_blend = 0.65f;
     s->frame_delta_ms = 16.0f;
     s->rng_order = 0;
+    s->temporal_accumulation = 0;
+    s->postprocess_effects = 0;
+    s->upscale = 0;
+    s->pad = 0;
 }
 
 void kpt_exposure_default(kpt_exposure* e) {   // SampleApp camera_controller.hpp:55-60
@@ -257,6 +271,8 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
+    c->vis.release(); c->tinst.release();
+    for (int k = 0; k < 2; ++k) { c->thist[k].release(); c->tdepth[k].release(); }
     for (auto& m : c->mips) m.release();
     c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
     c->sun_radiance.release();
@@ -279,6 +295,23 @@ kpt_status kpt_destroy(kpt_context* c) {
 static kpt_status clear_accumulation(kpt_context* c) {
     c->frame_index = 0;
     if (c->acc.p) KPT_CUDA(cudaMemsetAsync(c->acc.p, 0, sizeof(float4) * (size_t)c->W * c->H, c->stream));
+    // Renderer::resetAccumulation (renderer.cu:336-340) clears the history
+    // image in temporal mode; the previous frame's depth stays
+    if (c->thist[0].p) KPT_CUDA(cudaMemsetAsync(c->thist[0].p, 0, sizeof(float4) * c->thist[0].n, c->stream));
+    return KPT_OK;
+}
+
+// Buffers of the temporal mode, allocated when it is first used (zeroed).
+static kpt_status ensure_temporal(kpt_context* c) {
+    const size_t np = (size_t)c->W * c->H;
+    if (c->vis.n >= np && c->thist[0].n >= np) return KPT_OK;
+    KPT_CUDA(c->vis.ensure(np));
+    for (int k = 0; k < 2; ++k) {
+        KPT_CUDA(c->thist[k].ensure(np));
+        KPT_CUDA(c->tdepth[k].ensure(np));
+        KPT_CUDA(cudaMemsetAsync(c->thist[k].p, 0, sizeof(float4) * np, c->stream));
+        KPT_CUDA(cudaMemsetAsync(c->tdepth[k].p, 0, sizeof(float) * np, c->stream));
+    }
     return KPT_OK;
 }
 
@@ -305,6 +338,11 @@ kpt_status kpt_resize(kpt_context* c, int w, int h) {
     }
     c->W = w;
     c->H = h;
+    c->vis.release();   // the temporal buffers are re-created (zeroed) at the new size
+    for (int k = 0; k < 2; ++k) {
+        c->thist[k].release();
+        c->tdepth[k].release();
+    }
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
     return clear_accumulation(c);
 }
@@ -388,6 +426,7 @@ kpt_status kpt_add_instance(kpt_context* c, int mesh, const float* model, int ma
     HostInstance hi;
     hi.mesh = mesh;
     std::memcpy(hi.model, model, sizeof hi.model);
+    std::memcpy(hi.prev_model, model, sizeof hi.prev_model);
     hi.material = material;
     c->instances.push_back(hi);
     if (out) *out = (int)c->instances.size() - 1;
@@ -615,9 +654,13 @@ kpt_status kpt_set_instance_transform(kpt_context* c, int idx, const float* mode
     if (idx < 0 || idx >= (int)c->instances.size()) return fail(KPT_ERR_INVALID, "kpt_set_instance_transform: index out of range");
     for (int i = 0; i < 16; ++i)
         if (!std::isfinite(model[i])) return fail(KPT_ERR_INVALID, "kpt_set_instance_transform: non-finite matrix");
+    // TriangleMesh::setTransform (triangle.cuh:142-146): the old transform
+    // becomes the previous one
+    std::memcpy(c->instances[idx].prev_model, c->instances[idx].model, 16 * sizeof(float));
     std::memcpy(c->instances[idx].model, model, 16 * sizeof(float));
     c->tlas_dirty = true;
-    return clear_accumulation(c);
+    // Renderer::setMeshTransform keeps the history in temporal mode (renderer.cu:264-266)
+    return c->settings.temporal_accumulation ? KPT_OK : clear_accumulation(c);
 }
 
 kpt_status kpt_get_instance_transform(kpt_context* c, int idx, float* model) {
@@ -629,10 +672,15 @@ kpt_status kpt_get_instance_transform(kpt_context* c, int idx, float* model) {
 
 kpt_status kpt_set_camera_inverse(kpt_context* c, const float* ip, const float* iv) {
     if (!c || !ip || !iv) return fail(KPT_ERR_INVALID, "kpt_set_camera_inverse: null argument");
+    // Camera::setView (camera.cuh:27-35): the current camera becomes the
+    // previous one (the first camera is its own previous camera)
+    std::memcpy(c->prev_inv_proj, c->has_camera ? c->inv_proj : ip, sizeof c->prev_inv_proj);
+    std::memcpy(c->prev_inv_view, c->has_camera ? c->inv_view : iv, sizeof c->prev_inv_view);
     std::memcpy(c->inv_proj, ip, sizeof c->inv_proj);
     std::memcpy(c->inv_view, iv, sizeof c->inv_view);
     c->has_camera = true;
-    return clear_accumulation(c);
+    // Renderer::setView keeps the history in temporal mode (renderer.cu:351-353)
+    return c->settings.temporal_accumulation ? KPT_OK : clear_accumulation(c);
 }
 
 kpt_status kpt_set_view(kpt_context* c, const float* proj, const float* view) {
@@ -657,6 +705,10 @@ kpt_status kpt_get_environment(kpt_context* c, kpt_environment* e) {
 kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
     if (!c || !s) return fail(KPT_ERR_INVALID, "kpt_set_settings: null argument");
     if (s->max_depth < 0 || s->max_depth > 64) return fail(KPT_ERR_INVALID, "kpt_set_settings: max_depth out of range");
+    if (s->temporal_accumulation != 0 && s->temporal_accumulation != 1)
+        return fail(KPT_ERR_INVALID, "kpt_set_settings: temporal_accumulation must be 0 or 1");
+    if (s->postprocess_effects != 0 || s->upscale != 0)
+        return fail(KPT_ERR_INVALID, "kpt_set_settings: post-process effects and upscaling are not supported");
     c->settings = *s;
     return clear_accumulation(c);
 }
@@ -900,12 +952,20 @@ static void update_thresholds(kpt_context* c) {
 }
 
 // The frame: enqueued on the context stream (captured into a graph).
+static void enqueue_temporal(kpt_context* c, const FrameParams& F);
+
 static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
     enqueue_paths(c, F);
     stage_mark(c, KPT_STAGE_POST);
-    k_resolve<<<(np + 255) / 256, 256, 0, s>>>(np, c->acc.p, c->albedo.p, (float)total_samples, c->render.p);
+    if (c->settings.temporal_accumulation) {
+        enqueue_temporal(c, F);
+        // modulateSamples of the blended image (kernels.cu:453-472)
+        k_resolve<<<(np + 255) / 256, 256, 0, s>>>(np, c->thist[0].p, c->albedo.p, 1.0f, c->render.p);
+    } else {
+        k_resolve<<<(np + 255) / 256, 256, 0, s>>>(np, c->acc.p, c->albedo.p, (float)total_samples, c->render.p);
+    }
     c->launches += 1;
     if (c->settings.auto_exposure) {
         ExposureIn in{};
@@ -955,6 +1015,50 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
 
 // Host-side work of a frame, outside any capture: TLAS rebuild, exposure
 // thresholds, work buffers, the frame's parameters.
+// Mat4 * Mat4 (matrix_maths.cuh:269-283): entry (r, c) = row r of a dotted
+// with column c of b, left to right; column-major in and out.
+static void mat4_mul(const float* a, const float* b, float* out) {
+    float r[16];
+    for (int row = 0; row < 4; ++row)
+        for (int col = 0; col < 4; ++col)
+            r[4 * col + row] = a[row] * b[4 * col] + a[4 + row] * b[4 * col + 1] + a[8 + row] * b[4 * col + 2] +
+                               a[12 + row] * b[4 * col + 3];
+    std::memcpy(out, r, sizeof r);
+}
+
+// The per-frame matrices of computeVelocity / testReprojection
+// (kernels.cu:164-223): view-projections from the inverse camera matrices,
+// per instance the current inverse model, the previous model and
+// prev view-projection * prev model; `prev_cam` selects the camera whose
+// view-projection multiplies the previous model (the previous camera for the
+// first sample of a call, the current one after it).
+static void temporal_matrices(kpt_context* c, bool prev_cam, float4* vp, float3* prev_origin) {
+    float pj[16], vw[16], cur_vp[16], prv_vp[16];
+    inverse4(c->inv_proj, pj);
+    inverse4(c->inv_view, vw);
+    mat4_mul(pj, vw, cur_vp);
+    const float* pip = prev_cam ? c->prev_inv_proj : c->inv_proj;
+    const float* piv = prev_cam ? c->prev_inv_view : c->inv_view;
+    inverse4(pip, pj);
+    inverse4(piv, vw);
+    mat4_mul(pj, vw, prv_vp);
+    rows_of(cur_vp, vp, 4);
+    *prev_origin = make_float3(piv[12], piv[13], piv[14]);
+    c->h_tinst.resize(c->instances.size());
+    for (size_t i = 0; i < c->instances.size(); ++i) {
+        const HostInstance& hi = c->instances[i];
+        float inv[16], pinv[16], pmodel[16], pm[16];
+        inverse4(hi.model, inv);            // curr_inv_model_matrix
+        inverse4(hi.prev_model, pinv);      // prev_inv_model_matrix
+        inverse4(pinv, pmodel);             // prev_inv_model_matrix.inverse()
+        mat4_mul(prv_vp, pmodel, pm);
+        TemporalInst& t = c->h_tinst[i];
+        rows_of(inv, t.inv, 3);
+        rows_of(pmodel, t.prev_model, 3);
+        rows_of(pm, t.pm, 4);
+    }
+}
+
 static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     kpt_status st = ready(c);
     if (st != KPT_OK) return st;
@@ -966,12 +1070,70 @@ static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     F->acc = c->acc.p;
     F->albedo = c->albedo.p;
     F->first_hit = c->first_hit.p;
+    if (c->settings.temporal_accumulation) {
+        st = ensure_temporal(c);
+        if (st != KPT_OK) return st;
+        F->acc = nullptr;
+        F->vis = c->vis.p;
+        // matrices of the first sample (previous camera) and of the others
+        const size_t ni = c->instances.size();
+        std::vector<TemporalInst> both(2 * ni);
+        temporal_matrices(c, true, c->tvp[0], &c->torigin[0]);
+        std::copy(c->h_tinst.begin(), c->h_tinst.end(), both.begin());
+        temporal_matrices(c, false, c->tvp[1], &c->torigin[1]);
+        std::copy(c->h_tinst.begin(), c->h_tinst.end(), both.begin() + ni);
+        c->h_tinst.swap(both);
+        KPT_CUDA(c->tinst.upload(c->h_tinst.data(), c->h_tinst.size(), c->stream));
+    }
     return KPT_OK;
 }
 
 static void finish_frame(kpt_context* c, int spp) {
     c->frame_index += spp;
     c->frames_rendered++;
+    if (c->settings.temporal_accumulation) {
+        // executeRendering ends with setView(curr, curr) (renderer.cu:187-191)
+        std::memcpy(c->prev_inv_proj, c->inv_proj, sizeof c->prev_inv_proj);
+        std::memcpy(c->prev_inv_view, c->inv_view, sizeof c->prev_inv_view);
+        c->tdepth_prev ^= 1;
+    }
+}
+
+static void k_temporal_launch(kpt_context* c, const TemporalParams& T, int np, cudaStream_t s) {
+    k_temporal<<<(np + 255) / 256, 256, 0, s>>>(T);
+    c->launches += 1;
+}
+
+// Temporal accumulation of the call's samples, one reference frame each
+// (kernels.cu:422-428): the history ping-pongs between thist[0] and
+// thist[1] and ends in thist[0].
+static void enqueue_temporal(kpt_context* c, const FrameParams& F) {
+    cudaStream_t s = c->stream;
+    const int np = c->W * c->H;
+    const int ni = (int)c->instances.size();
+    TemporalParams T{};
+    T.W = c->W;
+    T.H = c->H;
+    T.counts = F.counts;
+    T.hit_index = F.hit_index;
+    T.primary = F.primary;
+    T.radiance = F.radiance;
+    T.pixel_sky = F.pixel_sky;
+    T.vis = F.vis;
+    for (int k = 0; k < F.nsamples; ++k) {
+        const int cam = k == 0 ? 0 : 1;
+        T.sample = k;
+        T.inst = c->tinst.p + (size_t)cam * ni;
+        for (int r = 0; r < 4; ++r) T.vp[r] = c->tvp[cam][r];
+        T.prev_origin = c->torigin[cam];
+        T.prev_depth = k == 0 ? c->tdepth[c->tdepth_prev].p : c->tdepth[c->tdepth_prev ^ 1].p;
+        T.depth_out = k == 0 ? c->tdepth[c->tdepth_prev ^ 1].p : nullptr;
+        T.hist_in = c->thist[k & 1].p;
+        T.hist_out = c->thist[(k & 1) ^ 1].p;
+        k_temporal_launch(c, T, np, s);
+    }
+    if (F.nsamples & 1)
+        cudaMemcpyAsync(c->thist[0].p, c->thist[1].p, sizeof(float4) * (size_t)np, cudaMemcpyDeviceToDevice, s);
 }
 
 // Instantiates `g` into *exec, updating the previous executable in place when

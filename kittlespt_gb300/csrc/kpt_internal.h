@@ -58,6 +58,7 @@ struct FrameParams {
     float4* acc;               // [H*W] running sum of samples (rgb), may be null
     float4* albedo;            // [H*W] visible-surface albedo, may be null
     int4* first_hit;           // [H*W] (instance, triangle, t bits, 0), may be null
+    float4* vis;               // [H*W] visible surface (position, distance; INF distance for a miss), may be null
     float4* sample_out;        // [nsamples][H*W] clamped per-sample radiance, may be null
     unsigned long long* counters;   // [16] box tests, triangle tests, instance transforms, overflows
                                     //      of the extension rays, the camera rays, the shadow rays;
@@ -153,6 +154,33 @@ __global__ void k_adjoint_miss(FrameParams F, AdjParams A);
 __global__ void k_adjoint(FrameParams F, AdjParams A);
 __global__ void k_adjoint_rec(FrameParams F, AdjParams A);   // also writes the frozen-path records
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
+// Temporal accumulation (kernels.cu:164-327): per instance, the matrices of
+// computeVelocity and testReprojection for one frame, rows of column-major
+// Mat4s (row r = column 0..3 entries r).
+struct TemporalInst {
+    float4 inv[3];             // curr_inv_model_matrix rows 0..2 (object <- world)
+    float4 prev_model[3];      // prev_inv_model_matrix.inverse(), rows 0..2
+    float4 pm[4];              // prev view-projection * prev model, rows 0..3
+};
+// One reference frame of the temporal path: the clamped sample `sample` of
+// every pixel blended into hist_in reprojected, written to hist_out.
+struct TemporalParams {
+    int W, H, sample;
+    const int* counts;         // [0]: camera rays that hit (slots of a sample in `radiance`)
+    const int* hit_index;      // pixel -> hit slot, -1: the camera ray missed
+    const PrimaryRec* primary; // per pixel: first hit (instance)
+    const float4* radiance;    // [nsamples][nhit] path radiance
+    const float4* pixel_sky;   // per pixel: the sky of a missing camera ray
+    const float4* vis;         // per pixel: visible surface position, distance
+    const TemporalInst* inst;
+    float4 vp[4];              // current view-projection rows
+    float3 prev_origin;        // previous camera position (prev_inv_view column 3)
+    const float* prev_depth;   // per pixel: visible-surface distance of the previous frame
+    float* depth_out;          // per pixel: this frame's distance for the next frame, may be null
+    const float4* hist_in;
+    float4* hist_out;
+};
+__global__ void k_temporal(TemporalParams T);
 __global__ void k_accumulate(FrameParams F);
 __global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out);
 __global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, float tmin, float tmax,

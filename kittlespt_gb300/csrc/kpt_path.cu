@@ -70,10 +70,15 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary(FrameParams F) {
         float3 alb = nonzero(Le) ? Le : bsdf_at(F.scene, si).albedo;
         if (F.albedo) F.albedo[p] = make_float4(alb.x, alb.y, alb.z, 0.0f);
         if (F.first_hit) F.first_hit[p] = make_int4(h.inst, h.tri, __float_as_int(h.t), 0);
+        // Ray::getPointAt, IEEE: the visible surface's position (interaction.cu:23)
+        if (F.vis)
+            F.vis[p] = make_float4(__fadd_rn(r.o.x, __fmul_rn(h.t, r.d.x)), __fadd_rn(r.o.y, __fmul_rn(h.t, r.d.y)),
+                                   __fadd_rn(r.o.z, __fmul_rn(h.t, r.d.z)), h.t);
     } else if (miss) {
         F.miss_list[m] = p;
         F.hit_index[p] = -1;
         if (F.first_hit) F.first_hit[p] = make_int4(-1, -1, 0x7f800000, 0);
+        if (F.vis) F.vis[p] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7f800000));
     }
     flush_stats(st, F.counters ? F.counters + 4 : nullptr);
     if (F.counters && threadIdx.x == 0) {   // camera rays of this block

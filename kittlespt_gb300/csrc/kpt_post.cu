@@ -52,6 +52,93 @@ __global__ void k_accumulate(FrameParams F) {
     if (F.acc) F.acc[p] = make_float4(acc.x, acc.y, acc.z, 1.0f);
 }
 
+// --- temporal accumulation (kernels.cu:164-327) ------------------------------
+// IEEE single precision in the reference's order of operations throughout.
+
+// Mat4 row r times (x, y, z, w): c0[r]*x + c1[r]*y + c2[r]*z + c3[r]*w
+// (matrix_maths.cuh:258-267)
+__device__ __forceinline__ float trow(float4 r, float x, float y, float z, float w) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r.x, x), __fmul_rn(r.y, y)), __fmul_rn(r.z, z)), __fmul_rn(r.w, w));
+}
+
+// RGBSpectrum::clampOutput (color.cuh:295-302), as k_accumulate applies it
+__device__ __forceinline__ float4 clamp_sample(float4 L) {
+    if (isnan(L.x) || isnan(L.y) || isnan(L.z) || isinf(L.x) || isinf(L.y) || isinf(L.z))
+        return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return make_float4(fmaxf(0.0f, fminf(L.x, 1.0e8f)), fmaxf(0.0f, fminf(L.y, 1.0e8f)),
+                       fmaxf(0.0f, fminf(L.z, 1.0e8f)), 0.0f);
+}
+
+__device__ __forceinline__ float4 tex_nearest(const float4* t, int W, int H, int x, int y) {   // cudaBoundaryModeClamp
+    x = min(max(x, 0), W - 1);
+    y = min(max(y, 0), H - 1);
+    return t[(size_t)y * W + x];
+}
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {   // a + t * (b - a)
+    return make_float4(__fadd_rn(a.x, __fmul_rn(t, __fsub_rn(b.x, a.x))), __fadd_rn(a.y, __fmul_rn(t, __fsub_rn(b.y, a.y))),
+                       __fadd_rn(a.z, __fmul_rn(t, __fsub_rn(b.z, a.z))), __fadd_rn(a.w, __fmul_rn(t, __fsub_rn(b.w, a.w))));
+}
+
+// computeVelocity, then reprojectAccumulate without SUPER_SAMPLE: the pixel
+// moves back by velocity * resolution; off screen, or when the depth of the
+// previous frame there (nearest texel) differs from the reprojected
+// distance by 4.5% or more, the history restarts; otherwise the previous
+// image is read bilinearly (its history count from the nearest texel) and
+// blended with weight 1 / min(history + 1, 16).
+__global__ void k_temporal(TemporalParams T) {
+    const int npix = T.W * T.H;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const int x = p % T.W, y = p / T.W;
+    const int j = T.hit_index[p];
+    const float4 curr = clamp_sample(j < 0 ? T.pixel_sky[p] : T.radiance[(size_t)T.sample * T.counts[0] + j]);
+    const float4 vs = T.vis[p];
+    if (T.depth_out) T.depth_out[p] = vs.w;
+    float4 out = make_float4(curr.x, curr.y, curr.z, 0.0f);
+    if (j >= 0) {
+        const TemporalInst& I = T.inst[T.primary[p].inst];
+        // computeVelocity (kernels.cu:164-192)
+        const float lx = trow(I.inv[0], vs.x, vs.y, vs.z, 1.0f), ly = trow(I.inv[1], vs.x, vs.y, vs.z, 1.0f),
+                    lz = trow(I.inv[2], vs.x, vs.y, vs.z, 1.0f);
+        const float cw = trow(T.vp[3], vs.x, vs.y, vs.z, 1.0f);
+        const float cx = __fdiv_rn(trow(T.vp[0], vs.x, vs.y, vs.z, 1.0f), cw);
+        const float cy = __fdiv_rn(trow(T.vp[1], vs.x, vs.y, vs.z, 1.0f), cw);
+        const float pw = trow(I.pm[3], lx, ly, lz, 1.0f);
+        const float px = __fdiv_rn(trow(I.pm[0], lx, ly, lz, 1.0f), pw);
+        const float py = __fdiv_rn(trow(I.pm[1], lx, ly, lz, 1.0f), pw);
+        const float vx = __fsub_rn(__fdiv_rn(__fadd_rn(cx, 1.0f), 2.0f), __fdiv_rn(__fadd_rn(px, 1.0f), 2.0f));
+        const float vy = __fsub_rn(__fdiv_rn(__fadd_rn(cy, 1.0f), 2.0f), __fdiv_rn(__fadd_rn(py, 1.0f), 2.0f));
+        // reprojectAccumulate (kernels.cu:299-327)
+        const float qx = __fsub_rn((float)x, __fmul_rn(vx, (float)T.W));
+        const float qy = __fsub_rn((float)y, __fmul_rn(vy, (float)T.H));
+        if (!(qx < 0.0f || qx >= (float)T.W || qy < 0.0f || qy >= (float)T.H)) {
+            // testReprojection (kernels.cu:206-223)
+            const int ix = (int)qx, iy = (int)qy;
+            const float d2 = T.prev_depth[(size_t)min(max(iy, 0), T.H - 1) * T.W + min(max(ix, 0), T.W - 1)];
+            const float wx = trow(I.prev_model[0], lx, ly, lz, 1.0f), wy = trow(I.prev_model[1], lx, ly, lz, 1.0f),
+                        wz = trow(I.prev_model[2], lx, ly, lz, 1.0f);
+            const float dx = __fsub_rn(T.prev_origin.x, wx), dy = __fsub_rn(T.prev_origin.y, wy),
+                        dz = __fsub_rn(T.prev_origin.z, wz);
+            const float d1 = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+            if (fabsf(__fsub_rn(d1, d2)) < __fmul_rn(d2, 0.045f)) {
+                // DeviceTextureBuffer::textureReadBilinear (device_texture_buffer.cuh:42-80), alpha point-sampled
+                const float ws = __fsub_rn(qx, (float)ix), wt = __fsub_rn(qy, (float)iy);
+                const float4 c0 = tex_nearest(T.hist_in, T.W, T.H, ix, iy), c1 = tex_nearest(T.hist_in, T.W, T.H, ix + 1, iy);
+                const float4 c2 = tex_nearest(T.hist_in, T.W, T.H, ix, iy + 1),
+                             c3 = tex_nearest(T.hist_in, T.W, T.H, ix + 1, iy + 1);
+                float4 prev = lerp4(lerp4(c0, c1, ws), lerp4(c2, c3, ws), wt);
+                prev.w = c0.w;
+                const float alpha = __fdiv_rn(1.0f, fminf(__fadd_rn(prev.w, 1.0f), 16.0f));
+                out = make_float4(__fadd_rn(prev.x, __fmul_rn(alpha, __fsub_rn(curr.x, prev.x))),
+                                  __fadd_rn(prev.y, __fmul_rn(alpha, __fsub_rn(curr.y, prev.y))),
+                                  __fadd_rn(prev.z, __fmul_rn(alpha, __fsub_rn(curr.z, prev.z))),
+                                  __fadd_rn(prev.w, 1.0f));
+            }
+        }
+    }
+    T.hist_out[p] = out;
+}
+
 __device__ __forceinline__ float qbyte(float v) {  // floatToByte then byteToFloat (packing.cuh:10-18)
     v = fmaxf(0.0f, fminf(v, 1.0f));
     uint32_t b = (uint32_t)__fmul_rn(v, 255.0f) & 0xFFu;

@@ -26,6 +26,7 @@ struct HostInstance {
     int mesh;
     float model[16];                 // column-major
     int material;                    // override or -1
+    float prev_model[16];            // the transform before the last change (TriangleMesh prev, triangle.cuh:142-146)
 };
 
 // Binned SAH build of the reference (as_builder.cuh:110-261).

@@ -2051,4 +2051,89 @@ void orc_post_frame(int W, int H, const float* acc_sum, int nsamples, const floa
         }
 }
 
+// Temporal accumulation of one reference frame over every pixel: the
+// megakernel's temporal branch (kernels.cu:422-428) with computeVelocity
+// (:164-192), testReprojection (:206-223) and reprojectAccumulate without
+// SUPER_SAMPLE (:299-327).  Inputs: the previous and current inverse camera
+// matrices, every instance's current and previous model matrix
+// (column-major, 16 floats each), per pixel the first hit's instance (-1:
+// miss) and distance, this frame's clamped sample, the previous frame's
+// distances and history image (color, frames); writes the new history.
+static M4 mul44(const M4& a, const M4& b) {   // matrix_maths.cuh:269-283: rows of a dotted with columns of b
+    M4 r;
+    for (int c = 0; c < 4; ++c) {
+        const f4 bc = b.c[c];
+        r.c[c] = {a.c[0].x * bc.x + a.c[1].x * bc.y + a.c[2].x * bc.z + a.c[3].x * bc.w,
+                  a.c[0].y * bc.x + a.c[1].y * bc.y + a.c[2].y * bc.z + a.c[3].y * bc.w,
+                  a.c[0].z * bc.x + a.c[1].z * bc.y + a.c[2].z * bc.z + a.c[3].z * bc.w,
+                  a.c[0].w * bc.x + a.c[1].w * bc.y + a.c[2].w * bc.z + a.c[3].w * bc.w};
+    }
+    return r;
+}
+
+void orc_temporal_frame(int W, int H, const float* prev_ip, const float* prev_iv, const float* curr_ip,
+                        const float* curr_iv, int ninst, const float* curr_models, const float* prev_models,
+                        const int32_t* vis_inst, const float* vis_t, const float* sample, const float* prev_depth,
+                        const float* hist_in, float* hist_out) {
+    const M4 cip = m4_from(curr_ip), civ = m4_from(curr_iv), pip = m4_from(prev_ip), piv = m4_from(prev_iv);
+    const M4 curr_vp = mul44(inverse(cip), inverse(civ));
+    const M4 prev_vp = mul44(inverse(pip), inverse(piv));
+    std::vector<M4> inv_m(ninst), prev_m(ninst), pm(ninst);
+    for (int i = 0; i < ninst; ++i) {
+        inv_m[i] = inverse(m4_from(curr_models + 16 * i));           // mesh.curr_inv_model_matrix
+        prev_m[i] = inverse(inverse(m4_from(prev_models + 16 * i)));  // mesh.prev_inv_model_matrix.inverse()
+        pm[i] = mul44(prev_vp, prev_m[i]);
+    }
+    Frame F{};
+    F.inv_proj = cip;
+    F.inv_view = civ;
+    F.cam_pos = xyz(civ.c[3]);
+    const f3 prev_origin = xyz(piv.c[3]);
+    auto tex = [&](const float* t, int x, int y) {   // cudaBoundaryModeClamp
+        x = std::min(std::max(x, 0), W - 1);
+        y = std::min(std::max(y, 0), H - 1);
+        const float* q = t + 4 * ((size_t)y * W + x);
+        return F4(q[0], q[1], q[2], q[3]);
+    };
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t p = (size_t)y * W + x;
+            const f4 curr = F4(sample[4 * p], sample[4 * p + 1], sample[4 * p + 2], 0.0f);
+            f4 out = curr;
+            const int inst = vis_inst[p];
+            if (inst >= 0) {
+                f2 uv = {((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H};
+                f2 ndc = {2.0f * uv.x - 1.0f, 2.0f * uv.y - 1.0f};
+                const f3 pos = point_at(camera_ray(F, ndc), vis_t[p]);
+                const f3 local = xyz(mul(inv_m[inst], F4(pos, 1.0f)));
+                const f4 cc = mul(curr_vp, F4(pos, 1.0f));
+                const f4 pc = mul(pm[inst], F4(local, 1.0f));
+                const f3 cn = xyz(cc) / cc.w, pn = xyz(pc) / pc.w;
+                const float vx = (cn.x + 1.0f) / 2.0f - (pn.x + 1.0f) / 2.0f;
+                const float vy = (cn.y + 1.0f) / 2.0f - (pn.y + 1.0f) / 2.0f;
+                const float qx = (float)x - vx * (float)W, qy = (float)y - vy * (float)H;
+                if (!(qx < 0 || qx >= (float)W || qy < 0 || qy >= (float)H)) {
+                    const int ix = (int)qx, iy = (int)qy;
+                    const float d2 = prev_depth[(size_t)std::min(std::max(iy, 0), H - 1) * W + std::min(std::max(ix, 0), W - 1)];
+                    const f3 pw = xyz(mul(prev_m[inst], F4(local, 1.0f)));
+                    const float d1 = length(prev_origin - pw);
+                    if (fabsf(d1 - d2) < (d2 * 0.045f)) {
+                        const float ws = qx - (float)ix, wt = qy - (float)iy;
+                        const f4 c0 = tex(hist_in, ix, iy), c1 = tex(hist_in, ix + 1, iy);
+                        const f4 c2 = tex(hist_in, ix, iy + 1), c3 = tex(hist_in, ix + 1, iy + 1);
+                        f4 prev = lerp4(lerp4(c0, c1, ws), lerp4(c2, c3, ws), wt);
+                        prev.w = c0.w;
+                        const float alpha = 1.0f / fminf(prev.w + 1, 16.0f);
+                        out = F4(prev.x + alpha * (curr.x - prev.x), prev.y + alpha * (curr.y - prev.y),
+                                 prev.z + alpha * (curr.z - prev.z), prev.w + 1);
+                    }
+                }
+            }
+            hist_out[4 * p] = out.x;
+            hist_out[4 * p + 1] = out.y;
+            hist_out[4 * p + 2] = out.z;
+            hist_out[4 * p + 3] = out.w;
+        }
+}
+
 }  // extern "C"

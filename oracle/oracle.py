@@ -80,6 +80,7 @@ def lib(prefix: str = "orc"):
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _u64]
         g("exposure").argtypes = [_u64, _v, C.c_float, C.c_float, _f]
         g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
+        g("temporal_frame").argtypes = [C.c_int, C.c_int, _f, _f, _f, _f, C.c_int, _f, _f, _i, _f, _f, _f, _f, _f]
     else:
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _f]
         g("exposure").argtypes = [_f] + [C.c_float] * 12 + [_f]
@@ -213,6 +214,31 @@ def hist_thresholds(black_ev=-10.0, white_ev=6.5):
     thr = np.zeros(255, np.float32)
     lib("orc").orc_hist_thresholds(black_ev, white_ev, thr)
     return thr
+
+
+def _cm(m):
+    """4x4 numpy M[row, col] -> 16 floats column-major."""
+    return np.ascontiguousarray(np.asarray(m, np.float32).T, np.float32).reshape(-1)
+
+
+def temporal_frame(prev_cam, curr_cam, curr_models, prev_models, vis_inst, vis_t, sample, prev_depth, hist_in):
+    """One reference frame of temporal accumulation (kernels.cu:164-327,
+    :422-428) for every pixel.  Cameras are (inv_proj, inv_view) pairs of 4x4
+    M[row, col]; models [n, 4, 4]; vis_inst / vis_t [H, W] (first-hit
+    instance, -1 for a miss, and distance); sample, hist_in [H, W, 4];
+    prev_depth [H, W].  Returns the new history image [H, W, 4]."""
+    H, W = vis_inst.shape
+    n = len(curr_models)
+    cm = np.concatenate([_cm(m) for m in curr_models]) if n else np.zeros(16, np.float32)
+    pm = np.concatenate([_cm(m) for m in prev_models]) if n else np.zeros(16, np.float32)
+    out = np.zeros((H, W, 4), np.float32)
+    lib().orc_temporal_frame(W, H, _cm(prev_cam[0]), _cm(prev_cam[1]), _cm(curr_cam[0]), _cm(curr_cam[1]), n, cm, pm,
+                             np.ascontiguousarray(vis_inst, np.int32).reshape(-1),
+                             np.ascontiguousarray(vis_t, np.float32).reshape(-1),
+                             np.ascontiguousarray(sample, np.float32).reshape(-1),
+                             np.ascontiguousarray(prev_depth, np.float32).reshape(-1),
+                             np.ascontiguousarray(hist_in, np.float32).reshape(-1), out.reshape(-1))
+    return out
 
 
 def modulate(acc_sum, nsamples, albedo, prefix="orc"):
