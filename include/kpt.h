@@ -68,8 +68,11 @@ typedef struct kpt_environment {
  * In this mode setting the view or an instance transform keeps the history
  * (other setters clear it, as in the reference).  The first camera a context
  * receives is its own previous camera.
- * postprocess_effects, upscale: the reference's effects and upscale switches
- * (not supported: KPT_ERR_INVALID when set). */
+ * postprocess_effects: the reference's lens effects on the display image
+ * (computeEffects, kernels.cu:340-374, 506-527): fisheye (power 1.65) and
+ * chromatic aberration.
+ * upscale: the reference's render-at-1/2.5-resolution switch (not supported:
+ * KPT_ERR_INVALID when set). */
 typedef struct kpt_settings {
     int32_t max_depth;
     int32_t bloom, karis, auto_exposure;

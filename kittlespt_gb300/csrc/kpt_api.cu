@@ -123,6 +123,7 @@ struct kpt_context {
     // temporal accumulation: visible surface, distances of the previous frame
     // and this one, history images (color, frames), per-instance matrices
     DBuf<float4> vis, thist[2];
+    DBuf<float4> backbuf;       // the tonemapped image before the effects (postprocess_effects)
     DBuf<float> tdepth[2];
     int tdepth_prev = 0;
     DBuf<TemporalInst> tinst;
@@ -271,7 +272,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
-    c->vis.release(); c->tinst.release();
+    c->vis.release(); c->tinst.release(); c->backbuf.release();
     for (int k = 0; k < 2; ++k) { c->thist[k].release(); c->tdepth[k].release(); }
     for (auto& m : c->mips) m.release();
     c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
@@ -707,8 +708,9 @@ kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
     if (s->max_depth < 0 || s->max_depth > 64) return fail(KPT_ERR_INVALID, "kpt_set_settings: max_depth out of range");
     if (s->temporal_accumulation != 0 && s->temporal_accumulation != 1)
         return fail(KPT_ERR_INVALID, "kpt_set_settings: temporal_accumulation must be 0 or 1");
-    if (s->postprocess_effects != 0 || s->upscale != 0)
-        return fail(KPT_ERR_INVALID, "kpt_set_settings: post-process effects and upscaling are not supported");
+    if (s->postprocess_effects != 0 && s->postprocess_effects != 1)
+        return fail(KPT_ERR_INVALID, "kpt_set_settings: postprocess_effects must be 0 or 1");
+    if (s->upscale != 0) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscaling is not supported");
     c->settings = *s;
     return clear_accumulation(c);
 }
@@ -1006,10 +1008,15 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
     double N = c->exposure.aperture;
     double lavg = (10.0 / 0.65) * ((N * N) / ((double)c->exposure.iso * (double)c->exposure.shutter));
     float fixed_scalar = (float)(0.18 / lavg);
+    const bool fx = c->settings.postprocess_effects != 0;
     k_tonemap<<<dim3((c->W + 15) / 16, (c->H + 15) / 16), dim3(16, 16), 0, s>>>(
         c->W, c->H, c->render.p, bloom0, bloom0 != nullptr, c->settings.bloom_final_blend, c->expo_state.p, fixed_scalar,
-        c->settings.auto_exposure, c->exposure.white_ev, c->exposure.black_ev, c->image.p);
+        c->settings.auto_exposure, c->exposure.white_ev, c->exposure.black_ev, fx ? c->backbuf.p : c->image.p);
     c->launches += 1;
+    if (fx) {   // launchFxComputeKernel (renderer.cu:162-167)
+        k_effects<<<dim3((c->W + 15) / 16, (c->H + 15) / 16), dim3(16, 16), 0, s>>>(c->W, c->H, c->backbuf.p, c->image.p);
+        c->launches += 1;
+    }
     stage_mark(c, KPT_STAGE_COUNT);   // end of the last interval
 }
 
@@ -1070,6 +1077,7 @@ static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     F->acc = c->acc.p;
     F->albedo = c->albedo.p;
     F->first_hit = c->first_hit.p;
+    if (c->settings.postprocess_effects) KPT_CUDA(c->backbuf.ensure((size_t)c->W * c->H));
     if (c->settings.temporal_accumulation) {
         st = ensure_temporal(c);
         if (st != KPT_OK) return st;

@@ -383,3 +383,46 @@ __global__ void k_tonemap(int W, int H, const float4* render, const float4* bloo
 }
 
 }  // namespace kpt
+
+namespace kpt {
+
+// textureReadNearestUV (device_texture_buffer.cuh:35-40): texel
+// (int)(uv * size), clamped at the edges
+__device__ __forceinline__ float4 nearest_uv(const float4* t, int W, int H, float u, float v) {
+    int x = (int)__fmul_rn(u, (float)W), y = (int)__fmul_rn(v, (float)H);
+    x = min(max(x, 0), W - 1);
+    y = min(max(y, 0), H - 1);
+    return t[(size_t)y * W + x];
+}
+
+// computeEffects with getFishEyeUV (kernels.cu:340-374, 506-527): the pixel's
+// fisheye position (power 1.65, radius bound to the corners), then the red
+// and blue channels read at +- a chromatic offset that grows with the square
+// of the distance from the centre.  IEEE arithmetic in the reference's order;
+// rsqrt as 1 / sqrt, tan and pow are CUDA's.
+__global__ void k_effects(int W, int H, const float4* src, float4* dst) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const float res_x = (float)W, res_y = (float)H;
+    const float px = __fdiv_rn((float)x, res_x), py = __fdiv_rn((float)y, res_x);
+    const float prop = __fdiv_rn(res_x, res_y);
+    const float mx = 0.5f, my = __fdiv_rn(0.5f, prop);
+    const float dx = __fsub_rn(px, mx), dy = __fsub_rn(py, my);
+    const float r = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    const float power = 1.65f;
+    const float bind = __fsqrt_rn(__fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my)));
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy))));
+    const float t1 = tanf(__fmul_rn(r, power)), t2 = tanf(__fmul_rn(bind, power));
+    float u = __fadd_rn(mx, __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(dx, inv), t1), bind), t2));
+    float v = __fadd_rn(my, __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(dy, inv), t1), bind), t2));
+    v = __fmul_rn(v, prop);
+    const float ux = __fdiv_rn(__fadd_rn((float)x, 0.5f), res_x), uy = __fdiv_rn(__fadd_rn((float)y, 0.5f), res_y);
+    const float ox = __fmul_rn(powf(__fmul_rn(fabsf(__fsub_rn(ux, 0.5f)), 2.0f), 2.0f), 0.01f);
+    const float oy = __fmul_rn(powf(__fmul_rn(fabsf(__fsub_rn(uy, 0.5f)), 2.0f), 2.0f), 0.01f);
+    const float rr = nearest_uv(src, W, H, __fadd_rn(u, ox), __fadd_rn(v, oy)).x;
+    const float gg = nearest_uv(src, W, H, u, v).y;
+    const float bb = nearest_uv(src, W, H, __fsub_rn(u, ox), __fsub_rn(v, oy)).z;
+    dst[(size_t)y * W + x] = make_float4(rr, gg, bb, 1.0f);
+}
+
+}  // namespace kpt

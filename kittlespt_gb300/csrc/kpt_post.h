@@ -25,5 +25,8 @@ __global__ void k_bloom_up(const float4* src, int sw, int sh, float4* dst, int d
 __global__ void k_tonemap(int W, int H, const float4* render, const float4* bloom, int use_bloom, float final_blend,
                           const ExposureState* st, float fixed_scalar, int auto_exposure, float white_ev, float black_ev,
                           float4* image);
+// computeEffects (kernels.cu:506-527): fisheye and chromatic aberration of
+// the tonemapped image
+__global__ void k_effects(int W, int H, const float4* src, float4* dst);
 
 }  // namespace kpt

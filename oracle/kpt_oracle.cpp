@@ -2136,4 +2136,39 @@ void orc_temporal_frame(int W, int H, const float* prev_ip, const float* prev_iv
         }
 }
 
+// computeEffects with getFishEyeUV (kernels.cu:340-374, 506-527) on the
+// tonemapped image src [H][W][4]: fisheye position (power 1.65, bound to the
+// corners), red and blue read at +- the chromatic offset, texels by
+// textureReadNearestUV (clamped).
+void orc_effects(int W, int H, const float* src, float* dst) {
+    auto nearest_uv = [&](float u, float v, int ch) {
+        int x = (int)(u * (float)W), y = (int)(v * (float)H);
+        x = std::min(std::max(x, 0), W - 1);
+        y = std::min(std::max(y, 0), H - 1);
+        return src[4 * ((size_t)y * W + x) + ch];
+    };
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const f2 res = {(float)W, (float)H};
+            const f2 p = {(float)x / res.x, (float)y / res.x};
+            const float prop = res.x / res.y;
+            const f2 m = {0.5f, 0.5f / prop};
+            const f2 d = {p.x - m.x, p.y - m.y};
+            const float r = sqrtf(d.x * d.x + d.y * d.y);
+            const float power = 1.65f;
+            const float bind = sqrtf(m.x * m.x + m.y * m.y);
+            const float inv = rsqrt_(d.x * d.x + d.y * d.y);
+            const float t1 = tanf(r * power), t2 = tanf(bind * power);
+            f2 uv = {m.x + (d.x * inv) * t1 * bind / t2, m.y + (d.y * inv) * t1 * bind / t2};
+            uv.y *= prop;
+            const f2 uc = {((float)x + 0.5f) / res.x, ((float)y + 0.5f) / res.y};
+            const f2 off = {powf(fabsf(uc.x - 0.5f) * 2.0f, 2.0f) * 0.01f, powf(fabsf(uc.y - 0.5f) * 2.0f, 2.0f) * 0.01f};
+            float* o = dst + 4 * ((size_t)y * W + x);
+            o[0] = nearest_uv(uv.x + off.x, uv.y + off.y, 0);
+            o[1] = nearest_uv(uv.x, uv.y, 1);
+            o[2] = nearest_uv(uv.x - off.x, uv.y - off.y, 2);
+            o[3] = 1.0f;
+        }
+}
+
 }  // extern "C"

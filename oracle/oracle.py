@@ -81,6 +81,7 @@ def lib(prefix: str = "orc"):
         g("exposure").argtypes = [_u64, _v, C.c_float, C.c_float, _f]
         g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
         g("temporal_frame").argtypes = [C.c_int, C.c_int, _f, _f, _f, _f, C.c_int, _f, _f, _i, _f, _f, _f, _f, _f]
+        g("effects").argtypes = [C.c_int, C.c_int, _f, _f]
     else:
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _f]
         g("exposure").argtypes = [_f] + [C.c_float] * 12 + [_f]
@@ -238,6 +239,15 @@ def temporal_frame(prev_cam, curr_cam, curr_models, prev_models, vis_inst, vis_t
                              np.ascontiguousarray(sample, np.float32).reshape(-1),
                              np.ascontiguousarray(prev_depth, np.float32).reshape(-1),
                              np.ascontiguousarray(hist_in, np.float32).reshape(-1), out.reshape(-1))
+    return out
+
+
+def effects(image):
+    """computeEffects (kernels.cu:506-527): fisheye and chromatic aberration of
+    a tonemapped image [H, W, 4]."""
+    H, W = image.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    lib().orc_effects(W, H, np.ascontiguousarray(image, np.float32).reshape(-1), out.reshape(-1))
     return out
 
 

@@ -1,0 +1,38 @@
+"""Lens effects (kpt_settings.postprocess_effects, the reference's
+postprocess_enable_effects: computeEffects with getFishEyeUV,
+kernels.cu:340-374, 506-527).  The frame with effects is the frame without
+them resampled by the oracle's restatement: every output texel is a copy of
+one input texel, so pixels compare exactly; a pixel may pick a neighbouring
+texel where CUDA's tanf / powf and the host's round a coordinate across a
+texel edge."""
+
+import numpy as np
+import pytest
+
+from kittlespt_gb300 import scenes as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("w,h", [(96, 64), (80, 80), (67, 45)])
+def test_effects_match_oracle(w, h):
+    from kittlespt_gb300.renderer import Renderer
+    sc = S.scene_small(w, h, 1, 3)
+    sc.settings["bloom"] = 1
+    imgs = []
+    for fx in (0, 1):
+        r = Renderer(0)
+        r.initialize()
+        try:
+            r.load_scene(sc)
+            r.set_renderer_settings(postprocess_effects=fx)
+            r.execute_rendering(16.0, 2)
+            r.synchronize()
+            imgs.append(r.get_render_target())
+        finally:
+            r.shutdown()
+    ref = O.effects(imgs[0])
+    same = (imgs[1] == ref).all(-1)
+    assert same.mean() >= 0.995, f"{same.mean():.4f} of pixels equal"
+    assert not np.array_equal(imgs[0], imgs[1])   # the effects changed the image
