@@ -133,6 +133,17 @@ kpt_status kpt_add_instance(kpt_context* ctx, int mesh, const float* model, int 
 kpt_status kpt_commit_scene(kpt_context* ctx);
 kpt_status kpt_clear_scene(kpt_context* ctx);
 
+/* New vertex positions (and optionally normals, 9 floats per triangle each,
+ * the mesh's triangle order) for a mesh of the committed scene, keeping its
+ * tree: the BLAS child boxes are refit on the GPU bottom up (each box the
+ * bounds of the triangles under it, as a build of the same tree would give),
+ * the triangle, shading and light records updated and the TLAS rebuilt on
+ * the next frame.  The reference's refitBLAS (as_builder.cuh:263-286) is
+ * not used by its renderer; a tree refit over large deformations traverses
+ * slower than a rebuild but returns the same hits.  Clears the accumulation
+ * (keeps the history in temporal mode, like a transform change). */
+kpt_status kpt_refit_mesh(kpt_context* ctx, int mesh, const float* positions, const float* normals);
+
 /* Where kpt_upload_mesh builds a BLAS.  No counterpart in the reference,
  * which builds every BLAS on the host (BLASBuilder, as_builder.cuh:181-261).
  * device = 1: on the GPU, on the context's stream -- the reference's tree

@@ -92,6 +92,7 @@ SIGNATURES = {
     "kpt_upload_mesh": (_S, [_P, C.c_int, _F, _F, _F, _I, C.POINTER(C.c_int)]),
     "kpt_add_instance": (_S, [_P, C.c_int, _F, C.c_int, C.POINTER(C.c_int)]),
     "kpt_set_blas_build": (_S, [_P, C.c_int]),
+    "kpt_refit_mesh": (_S, [_P, C.c_int, _F, _F]),
     "kpt_get_blas": (_S, [_P, C.c_int, _I, _F, _I, _F]),
     "kpt_commit_scene": (_S, [_P]),
     "kpt_clear_scene": (_S, [_P]),

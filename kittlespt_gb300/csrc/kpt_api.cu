@@ -105,7 +105,8 @@ struct kpt_context {
     DBuf<TexRec> d_textures;
     DBuf<uint8_t> d_pixels;
     SceneView view{};
-    std::vector<int> mesh_node_base, mesh_tri_base;
+    std::vector<int> mesh_node_base, mesh_tri_base;   // per mesh: first node / triangle in the device arrays
+    std::vector<LightRec> h_lights;
     std::vector<InstRec> h_inst;
 
     // camera and settings
@@ -421,6 +422,54 @@ kpt_status kpt_get_blas(kpt_context* c, int mesh, int32_t* info, float* nodes, i
     return KPT_OK;
 }
 
+kpt_status kpt_refit_mesh(kpt_context* c, int mesh, const float* positions, const float* normals) {
+    if (!c || !positions || mesh < 0 || mesh >= (int)c->meshes.size())
+        return fail(KPT_ERR_INVALID, "kpt_refit_mesh: bad mesh or null positions");
+    if (!c->committed) return fail(KPT_ERR_STATE, "kpt_refit_mesh: no committed scene");
+    HostMesh& m = c->meshes[mesh];
+    const size_t n9 = 9 * (size_t)m.ntris();
+    for (size_t i = 0; i < n9; ++i)
+        if (!std::isfinite(positions[i])) return fail(KPT_ERR_INVALID, "kpt_refit_mesh: non-finite position");
+    KPT_CUDA(cudaSetDevice(c->device));
+    m.pos.assign(positions, positions + n9);
+    if (normals) m.nrm.assign(normals, normals + n9);
+    const int tb = c->mesh_tri_base[mesh];
+    const int e = refit_blas_device(m, c->d_nodes.p, c->mesh_node_base[mesh], c->d_tris.p, tb, c->stream);
+    if (e != 0) return fail(KPT_ERR_CUDA, std::string("kpt_refit_mesh: ") + cudaGetErrorString((cudaError_t)e));
+    // shading records of the mesh's triangles (geometric normals) and its lights
+    std::vector<TriShade> shade(m.ntris());
+    KPT_CUDA(cudaMemcpy(shade.data(), c->d_shade.p + tb, shade.size() * sizeof(TriShade), cudaMemcpyDeviceToHost));
+    for (int t = 0; t < m.ntris(); ++t) {
+        float gn[3], area;
+        tri_normal_area(&m.pos[9 * (size_t)t], &m.nrm[9 * (size_t)t], gn, &area);
+        shade[t].gnx = gn[0];
+        shade[t].gny = gn[1];
+        shade[t].gnz = gn[2];
+    }
+    KPT_CUDA(cudaMemcpyAsync(c->d_shade.p + tb, shade.data(), shade.size() * sizeof(TriShade), cudaMemcpyHostToDevice,
+                             c->stream));
+    bool lights = false;
+    for (LightRec& L : c->h_lights) {
+        if (c->instances[L.inst].mesh != mesh) continue;
+        const float* p = &m.pos[9 * (size_t)L.tri];
+        L.p0 = make_float3(p[0], p[1], p[2]);
+        L.p1 = make_float3(p[3], p[4], p[5]);
+        L.p2 = make_float3(p[6], p[7], p[8]);
+        float gn[3], area;
+        tri_normal_area(p, &m.nrm[9 * (size_t)L.tri], gn, &area);
+        L.gn = make_float3(gn[0], gn[1], gn[2]);
+        L.area = area;
+        L.tri_area = area;
+        lights = true;
+    }
+    if (lights)
+        KPT_CUDA(cudaMemcpyAsync(c->d_lights.p, c->h_lights.data(), c->h_lights.size() * sizeof(LightRec),
+                                 cudaMemcpyHostToDevice, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    c->tlas_dirty = true;   // the instances' world bounds follow the mesh's
+    return c->settings.temporal_accumulation ? KPT_OK : clear_accumulation(c);
+}
+
 kpt_status kpt_add_instance(kpt_context* c, int mesh, const float* model, int material, int* out) {
     if (!c || !model || mesh < 0 || mesh >= (int)c->meshes.size())
         return fail(KPT_ERR_INVALID, "kpt_add_instance: bad mesh or matrix");
@@ -510,9 +559,13 @@ kpt_status kpt_commit_scene(kpt_context* c) {
     std::vector<float4> tris;
     std::vector<TriShade> shade;
     std::vector<MeshRec> mrec;
+    c->mesh_node_base.clear();
+    c->mesh_tri_base.clear();
     for (auto& m : c->meshes) {
         MeshRec r{};
         int nb = (int)nodes.size(), tb = (int)(tris.size() / 3);
+        c->mesh_node_base.push_back(nb);
+        c->mesh_tri_base.push_back(tb);
         for (BvhNode n : m.nodes) {
             if (n.d.y == 0) n.d.x += nb; else n.d.x += tb;
             if (n.d.w == 0) n.d.z += nb; else n.d.z += tb;
@@ -599,6 +652,7 @@ kpt_status kpt_commit_scene(kpt_context* c) {
     KPT_CUDA(c->d_shade.upload(shade.data(), shade.size(), c->stream));
     KPT_CUDA(c->d_meshes.upload(mrec.data(), mrec.size(), c->stream));
     KPT_CUDA(c->d_lights.upload(lights.data(), lights.size(), c->stream));
+    c->h_lights = lights;
     KPT_CUDA(c->d_materials.upload(mats.data(), mats.size(), c->stream));
     KPT_CUDA(c->d_textures.upload(c->textures.data(), c->textures.size(), c->stream));
     KPT_CUDA(c->d_pixels.upload(c->pixels.data(), c->pixels.size(), c->stream));

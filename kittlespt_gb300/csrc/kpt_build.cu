@@ -1149,4 +1149,153 @@ int build_blas_device(HostMesh& m, cudaStream_t st) {
     return 0;
 }
 
+// --- refit: new positions, same tree -------------------------------------
+// Every node's child boxes are recomputed bottom up from the triangles below
+// them (min / max, so each box equals the one a build of the same tree would
+// give); triangle records in leaf order are rewritten.  Nodes are the
+// device-format nodes of one mesh at node_base in the scene's node array
+// (child references global: nodes node_base + local, triangles tri_base +
+// leaf position).
+
+namespace {
+
+__global__ void k_refit_tris(const float* pos, const int* order, int n, int tri_base, float4* tris) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int t = order[k];
+    const float* p = pos + 9 * (size_t)t;
+    float4* o = tris + 3 * ((size_t)tri_base + k);
+    o[0] = make_float4(p[0], p[1], p[2], __int_as_float(t));
+    o[1] = make_float4(__fsub_rn(p[3], p[0]), __fsub_rn(p[4], p[1]), __fsub_rn(p[5], p[2]), 0.0f);
+    o[2] = make_float4(__fsub_rn(p[6], p[0]), __fsub_rn(p[7], p[1]), __fsub_rn(p[8], p[2]), 0.0f);
+}
+
+__device__ __forceinline__ void leaf_box(const float* pos, const int* order, int tri_base, int first, int count,
+                                         float* lo, float* hi) {
+    for (int q = 0; q < 3; ++q) {
+        lo[q] = FLT_MAX;
+        hi[q] = -FLT_MAX;
+    }
+    for (int k = first; k < first + count; ++k) {
+        const float* v = pos + 9 * (size_t)order[k - tri_base];
+        for (int j = 0; j < 9; ++j) {
+            lo[j % 3] = fminf(lo[j % 3], v[j]);
+            hi[j % 3] = fmaxf(hi[j % 3], v[j]);
+        }
+    }
+}
+__device__ __forceinline__ void set_child(BvhNode& n, int slot, const float* lo, const float* hi) {
+    if (slot == 0) {
+        n.a = make_float4(lo[0], lo[1], lo[2], hi[0]);
+        n.b.x = hi[1];
+        n.b.y = hi[2];
+    } else {
+        n.b.z = lo[0];
+        n.b.w = lo[1];
+        n.c = make_float4(lo[2], hi[0], hi[1], hi[2]);
+    }
+}
+
+// parents (local), interior children to wait for, and the leaf children's boxes
+__global__ void k_refit_leaves(BvhNode* nodes, int node_base, int nn, int tri_base, const float* pos,
+                               const int* order, int* parent, int* need, int* arrive) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn) return;
+    BvhNode n = nodes[node_base + v];
+    int nd = 0;
+    for (int slot = 0; slot < 2; ++slot) {
+        const int ref = slot ? n.d.z : n.d.x, cnt = slot ? n.d.w : n.d.y;
+        if (cnt == 0) {
+            parent[ref - node_base] = v;
+            ++nd;
+        } else {
+            float lo[3], hi[3];
+            leaf_box(pos, order, tri_base, ref, cnt, lo, hi);
+            set_child(n, slot, lo, hi);
+        }
+    }
+    nodes[node_base + v] = n;
+    need[v] = nd;
+    arrive[v] = 0;
+    if (v == 0) parent[0] = -1;
+}
+
+// a node whose children's boxes are final passes their union to its parent;
+// the last of a parent's interior children to arrive carries on upwards
+__global__ void k_refit_up(BvhNode* nodes, int node_base, int nn, const int* parent, const int* need, int* arrive) {
+    const int v0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v0 >= nn || need[v0] != 0) return;
+    int v = v0;
+    for (;;) {
+        const int p = parent[v];
+        if (p < 0) break;
+        // this node's child boxes, written by other threads before their arrival
+        volatile const float* f = reinterpret_cast<volatile const float*>(nodes + node_base + v);
+        const float lo[3] = {fminf(f[0], f[6]), fminf(f[1], f[7]), fminf(f[2], f[8])};
+        const float hi[3] = {fmaxf(f[3], f[9]), fmaxf(f[4], f[10]), fmaxf(f[5], f[11])};
+        BvhNode* pn = nodes + node_base + p;
+        const int slot = (pn->d.y == 0 && pn->d.x == node_base + v) ? 0 : 1;
+        if (slot == 0) {
+            pn->a = make_float4(lo[0], lo[1], lo[2], hi[0]);
+            pn->b.x = hi[1];
+            pn->b.y = hi[2];
+        } else {
+            pn->b.z = lo[0];
+            pn->b.w = lo[1];
+            pn->c = make_float4(lo[2], hi[0], hi[1], hi[2]);
+        }
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1) + 1 != need[p]) break;
+        __threadfence();
+        v = p;
+    }
+}
+
+}  // namespace
+
+int refit_blas_device(HostMesh& m, BvhNode* d_nodes, int node_base, float4* d_tris, int tri_base, cudaStream_t st) {
+    const int N = m.ntris(), nn = (int)m.nodes.size();
+    DevArray<float> pos;
+    DevArray<int> order, parent, need, arrive;
+    cudaError_t e = cudaSuccess;
+    for (cudaError_t r : {pos.alloc(9 * (size_t)N), order.alloc(N), parent.alloc(nn), need.alloc(nn), arrive.alloc(nn)})
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(pos.p, m.pos.data(), 9 * (size_t)N * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(order.p, m.order.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return (int)e;
+    k_refit_tris<<<(N + 255) / 256, 256, 0, st>>>(pos.p, order.p, N, tri_base, d_tris);
+    if (nn > 0) {
+        k_refit_leaves<<<(nn + 255) / 256, 256, 0, st>>>(d_nodes, node_base, nn, tri_base, pos.p, order.p, parent.p,
+                                                         need.p, arrive.p);
+        k_refit_up<<<(nn + 255) / 256, 256, 0, st>>>(d_nodes, node_base, nn, parent.p, need.p, arrive.p);
+        // the host copy of the nodes: boxes from the device, references local as built
+        std::vector<BvhNode> h(nn);
+        e = cudaMemcpyAsync(h.data(), d_nodes + node_base, nn * sizeof(BvhNode), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return (int)e;
+        for (int k = 0; k < nn; ++k) {
+            m.nodes[k].a = h[k].a;
+            m.nodes[k].b = h[k].b;
+            m.nodes[k].c = h[k].c;
+        }
+        const BvhNode& r = m.nodes[0];
+        m.lo[0] = fminf(r.a.x, r.b.z); m.lo[1] = fminf(r.a.y, r.b.w); m.lo[2] = fminf(r.a.z, r.c.x);
+        m.hi[0] = fmaxf(r.a.w, r.c.y); m.hi[1] = fmaxf(r.b.x, r.c.z); m.hi[2] = fmaxf(r.b.y, r.c.w);
+    } else {   // the root is a leaf: the mesh's box
+        for (int q = 0; q < 3; ++q) {
+            m.lo[q] = FLT_MAX;
+            m.hi[q] = -FLT_MAX;
+        }
+        for (size_t j = 0; j < m.pos.size(); ++j) {
+            m.lo[j % 3] = fminf(m.lo[j % 3], m.pos[j]);
+            m.hi[j % 3] = fmaxf(m.hi[j % 3], m.pos[j]);
+        }
+        e = cudaStreamSynchronize(st);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return (int)e;
+}
+
 }  // namespace kpt

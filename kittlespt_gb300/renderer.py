@@ -111,6 +111,13 @@ class Renderer:
         the host (False, the default); the trees are the same."""
         K.check(self._L.kpt_set_blas_build(self._ctx, 1 if device else 0))
 
+    def refit_mesh(self, mesh: int, positions, normals=None):
+        """New positions (and optionally normals) for an uploaded mesh of the
+        committed scene; the BLAS keeps its tree and is refit on the GPU."""
+        p = np.ascontiguousarray(positions, np.float32).reshape(-1)
+        n = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1)
+        K.check(self._L.kpt_refit_mesh(self._ctx, mesh, K.fptr(p), K.fptr(n) if n is not None else None))
+
     def get_blas(self, mesh: int) -> dict:
         """The device-format BLAS of an uploaded mesh: nodes (float32 [k, 12]
         child boxes, int32 [k, 4] child references and counts), leaf order,
