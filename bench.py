@@ -616,9 +616,31 @@ def run_blas(args):
                     best = min(best, time.perf_counter() - t0)
                     K.check(L.kpt_clear_scene(ctx))
                 times["device" if device else "host"] = best * 1e3
+            # refit (kpt_refit_mesh) of the same mesh in a committed scene,
+            # positions scaled by 1.1
+            K.check(L.kpt_set_blas_build(ctx, 1))
+            mats = (K.Material * 1)()
+            mats[0].albedo[:] = (0.5, 0.5, 0.5)
+            mats[0].roughness, mats[0].ior, mats[0].normal_scale = 0.5, 1.5, 1.0
+            mats[0].albedo_tex = mats[0].orm_tex = mats[0].transmission_tex = mats[0].emission_tex = -1
+            mats[0].normal_tex = -1
+            K.check(L.kpt_set_materials(ctx, 1, mats))
+            K.check(L.kpt_upload_mesh(ctx, n, K.fptr(pos), None, None, K.iptr(mat), C.byref(out)))
+            ident = np.eye(4, dtype=np.float32).reshape(-1)
+            inst = C.c_int()
+            K.check(L.kpt_add_instance(ctx, out.value, K.fptr(ident), -1, C.byref(inst)))
+            K.check(L.kpt_commit_scene(ctx))
+            moved = np.ascontiguousarray(pos * np.float32(1.1), np.float32)
+            refit = float("inf")
+            for _ in range(max(2, args.steps)):
+                t0 = time.perf_counter()
+                K.check(L.kpt_refit_mesh(ctx, out.value, K.fptr(moved), None))
+                refit = min(refit, time.perf_counter() - t0)
+            K.check(L.kpt_clear_scene(ctx))
             res[name] = {"triangles": n, "host_ms": times["host"], "device_ms": times["device"],
-                         "speedup": times["host"] / times["device"]}
-            print(f"[bench] {name}: host {times['host']:.1f} ms, device {times['device']:.1f} ms", file=sys.stderr)
+                         "speedup": times["host"] / times["device"], "refit_ms": refit * 1e3}
+            print(f"[bench] {name}: host {times['host']:.1f} ms, device {times['device']:.1f} ms, "
+                  f"refit {refit * 1e3:.1f} ms", file=sys.stderr)
     finally:
         L.kpt_destroy(ctx)
     big = res["random_triangles_2M"]

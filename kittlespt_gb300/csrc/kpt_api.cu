@@ -434,20 +434,9 @@ kpt_status kpt_refit_mesh(kpt_context* c, int mesh, const float* positions, cons
     m.pos.assign(positions, positions + n9);
     if (normals) m.nrm.assign(normals, normals + n9);
     const int tb = c->mesh_tri_base[mesh];
-    const int e = refit_blas_device(m, c->d_nodes.p, c->mesh_node_base[mesh], c->d_tris.p, tb, c->stream);
+    const int e = refit_blas_device(m, c->d_nodes.p, c->mesh_node_base[mesh], c->d_tris.p, tb, c->d_shade.p, c->stream);
     if (e != 0) return fail(KPT_ERR_CUDA, std::string("kpt_refit_mesh: ") + cudaGetErrorString((cudaError_t)e));
-    // shading records of the mesh's triangles (geometric normals) and its lights
-    std::vector<TriShade> shade(m.ntris());
-    KPT_CUDA(cudaMemcpy(shade.data(), c->d_shade.p + tb, shade.size() * sizeof(TriShade), cudaMemcpyDeviceToHost));
-    for (int t = 0; t < m.ntris(); ++t) {
-        float gn[3], area;
-        tri_normal_area(&m.pos[9 * (size_t)t], &m.nrm[9 * (size_t)t], gn, &area);
-        shade[t].gnx = gn[0];
-        shade[t].gny = gn[1];
-        shade[t].gnz = gn[2];
-    }
-    KPT_CUDA(cudaMemcpyAsync(c->d_shade.p + tb, shade.data(), shade.size() * sizeof(TriShade), cudaMemcpyHostToDevice,
-                             c->stream));
+    // the lights on the mesh's triangles
     bool lights = false;
     for (LightRec& L : c->h_lights) {
         if (c->instances[L.inst].mesh != mesh) continue;

@@ -1170,6 +1170,30 @@ __global__ void k_refit_tris(const float* pos, const int* order, int n, int tri_
     o[2] = make_float4(__fsub_rn(p[6], p[0]), __fsub_rn(p[7], p[1]), __fsub_rn(p[8], p[2]), 0.0f);
 }
 
+// tri_normal_area (kpt_scene.cpp) on the device, the same IEEE operations:
+// the geometric normal facing the mean vertex normal (Triangle constructor,
+// triangle.cuh:51-64)
+__global__ void k_refit_shade(const float* pos, const float* nrm, int n, TriShade* shade) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float* p = pos + 9 * (size_t)t;
+    const float* q = nrm + 9 * (size_t)t;
+    const float e0x = __fsub_rn(p[3], p[0]), e0y = __fsub_rn(p[4], p[1]), e0z = __fsub_rn(p[5], p[2]);
+    const float e1x = __fsub_rn(p[6], p[0]), e1y = __fsub_rn(p[7], p[1]), e1z = __fsub_rn(p[8], p[2]);
+    const float gx = __fsub_rn(__fmul_rn(e0y, e1z), __fmul_rn(e0z, e1y));
+    const float gy = __fsub_rn(__fmul_rn(e0z, e1x), __fmul_rn(e0x, e1z));
+    const float gz = __fsub_rn(__fmul_rn(e0x, e1y), __fmul_rn(e0y, e1x));
+    const float ax = __fdiv_rn(__fadd_rn(__fadd_rn(q[0], q[3]), q[6]), 3.0f);
+    const float ay = __fdiv_rn(__fadd_rn(__fadd_rn(q[1], q[4]), q[7]), 3.0f);
+    const float az = __fdiv_rn(__fadd_rn(__fadd_rn(q[2], q[5]), q[8]), 3.0f);
+    const float d = __fadd_rn(__fadd_rn(__fmul_rn(gx, ax), __fmul_rn(gy, ay)), __fmul_rn(gz, az));
+    const float ox = d < 0.0f ? -gx : gx, oy = d < 0.0f ? -gy : gy, oz = d < 0.0f ? -gz : gz;
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ox, ox), __fmul_rn(oy, oy)), __fmul_rn(oz, oz))));
+    shade[t].gnx = __fmul_rn(ox, inv);
+    shade[t].gny = __fmul_rn(oy, inv);
+    shade[t].gnz = __fmul_rn(oz, inv);
+}
+
 __device__ __forceinline__ void leaf_box(const float* pos, const int* order, int tri_base, int first, int count,
                                          float* lo, float* hi) {
     for (int q = 0; q < 3; ++q) {
@@ -1253,19 +1277,24 @@ __global__ void k_refit_up(BvhNode* nodes, int node_base, int nn, const int* par
 
 }  // namespace
 
-int refit_blas_device(HostMesh& m, BvhNode* d_nodes, int node_base, float4* d_tris, int tri_base, cudaStream_t st) {
+int refit_blas_device(HostMesh& m, BvhNode* d_nodes, int node_base, float4* d_tris, int tri_base, TriShade* d_shade,
+                      cudaStream_t st) {
     const int N = m.ntris(), nn = (int)m.nodes.size();
-    DevArray<float> pos;
+    DevArray<float> pos, nrm;
     DevArray<int> order, parent, need, arrive;
     cudaError_t e = cudaSuccess;
-    for (cudaError_t r : {pos.alloc(9 * (size_t)N), order.alloc(N), parent.alloc(nn), need.alloc(nn), arrive.alloc(nn)})
+    for (cudaError_t r : {pos.alloc(9 * (size_t)N), nrm.alloc(9 * (size_t)N), order.alloc(N), parent.alloc(nn),
+                          need.alloc(nn), arrive.alloc(nn)})
         if (r != cudaSuccess && e == cudaSuccess) e = r;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(pos.p, m.pos.data(), 9 * (size_t)N * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
+        e = cudaMemcpyAsync(nrm.p, m.nrm.data(), 9 * (size_t)N * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
         e = cudaMemcpyAsync(order.p, m.order.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return (int)e;
     k_refit_tris<<<(N + 255) / 256, 256, 0, st>>>(pos.p, order.p, N, tri_base, d_tris);
+    k_refit_shade<<<(N + 255) / 256, 256, 0, st>>>(pos.p, nrm.p, N, d_shade + tri_base);
     if (nn > 0) {
         k_refit_leaves<<<(nn + 255) / 256, 256, 0, st>>>(d_nodes, node_base, nn, tri_base, pos.p, order.p, parent.p,
                                                          need.p, arrive.p);

@@ -49,11 +49,13 @@ void pack_blas(HostMesh& m, const std::vector<BlasNode>& nodes, std::vector<int>
 // triangle order.  Returns a CUDA error code (0 on success).
 int build_blas_device(HostMesh& m, cudaStream_t stream);
 
-// Refit on the GPU after m.pos changed (same tree): recomputes the child
-// boxes of the mesh's nodes at node_base of the scene's device node array
-// bottom up, rewrites its triangle records at tri_base, and updates m.nodes'
-// boxes and m.lo / m.hi.  Returns a CUDA error code (0 on success).
-int refit_blas_device(HostMesh& m, BvhNode* d_nodes, int node_base, float4* d_tris, int tri_base, cudaStream_t stream);
+// Refit on the GPU after m.pos (and m.nrm) changed, same tree: recomputes
+// the child boxes of the mesh's nodes at node_base of the scene's device
+// node array bottom up, rewrites its triangle records and the geometric
+// normals of its shading records at tri_base, and updates m.nodes' boxes
+// and m.lo / m.hi.  Returns a CUDA error code (0 on success).
+int refit_blas_device(HostMesh& m, BvhNode* d_nodes, int node_base, float4* d_tris, int tri_base, TriShade* d_shade,
+                      cudaStream_t stream);
 
 // World bounds of an instance: the 8 transformed corners of the mesh bounds
 // (BLAS2::setTransform, blas.cuh:338-348).

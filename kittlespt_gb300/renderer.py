@@ -83,6 +83,10 @@ class Renderer:
         K.check(L.kpt_clear_scene(self._ctx))
         mats = (K.Material * len(scene.materials))(*[_mat(m) for m in scene.materials])
         K.check(L.kpt_set_materials(self._ctx, len(scene.materials), mats))
+        if getattr(scene, "textures", None):
+            desc, pix = scene.texture_arrays()
+            K.check(L.kpt_set_textures(self._ctx, len(scene.textures), K.iptr(desc.reshape(-1)), pix.size,
+                                       pix.ctypes.data_as(C.POINTER(C.c_uint8))))
         for m in scene.meshes:
             out = C.c_int()
             K.check(L.kpt_upload_mesh(self._ctx, m.ntris, K.fptr(m.positions.reshape(-1)),

@@ -360,6 +360,21 @@ class Scene:
     height: int
     spp: int
     name: str = ""
+    # 8-bit textures (TextureSceneEntity, pod_types.hpp): [h, w, channels] uint8 each
+    textures: List[np.ndarray] = dataclasses.field(default_factory=list)
+
+    def texture_arrays(self):
+        """(desc int32 [n, 4] = width, height, channels, byte offset; pixels
+        uint8) as kpt_set_textures takes them."""
+        desc = np.zeros((len(self.textures), 4), np.int32)
+        off = 0
+        for k, t in enumerate(self.textures):
+            h, w, ch = t.shape
+            desc[k] = (w, h, ch, off)
+            off += t.size
+        pix = (np.concatenate([np.ascontiguousarray(t, np.uint8).reshape(-1) for t in self.textures])
+               if self.textures else np.zeros(1, np.uint8))
+        return desc, pix
 
     @property
     def ntris_expanded(self):

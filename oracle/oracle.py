@@ -108,8 +108,16 @@ class Scene:
         self.h = fn(n, ex["positions"].reshape(-1), ex["normals"].reshape(-1), ex["uvs"].reshape(-1),
                     ex["material"], len(ex["mesh_offset"]), ex["mesh_offset"], ex["mesh_count"],
                     np.ascontiguousarray(np.transpose(ex["models"], (0, 2, 1))).reshape(-1),
-                    len(self.materials), _ptr(self.materials), 0, None, 0, None)
+                    len(self.materials), _ptr(self.materials), *self._textures(scene))
         self.scene = scene
+
+    def _textures(self, scene):
+        tex = getattr(scene, "textures", None)
+        if not tex:
+            return 0, None, 0, None
+        desc, pix = scene.texture_arrays()
+        self._tex = (desc, pix)
+        return len(tex), _ptr(desc), int(pix.size), _ptr(pix)
 
     def close(self):
         if self.h:
