@@ -104,7 +104,7 @@ struct ProceduralEnvironmentSettings {
     float sun_emission_factor = 1.0f;
 };
 
-// pod_types.hpp:46-57 (upscale is not supported: setting it fails)
+// pod_types.hpp:46-57
 struct RendererSettings {
     int32_t integrator_max_ray_depth = 3;
     bool integrator_use_temporal_accumulation = false;

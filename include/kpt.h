@@ -71,8 +71,13 @@ typedef struct kpt_environment {
  * postprocess_effects: the reference's lens effects on the display image
  * (computeEffects, kernels.cu:340-374, 506-527): fisheye (power 1.65) and
  * chromatic aberration.
- * upscale: the reference's render-at-1/2.5-resolution switch (not supported:
- * KPT_ERR_INVALID when set). */
+ * upscale: the reference's upscale_enable (without its compiled-out FSR path):
+ * the paths, accumulation, modulation and histogram run at the output
+ * resolution / 2.5 (truncated), the render is upscaled bilinearly
+ * (upscale.cuh:260-291) and bloom, tonemapping and effects run at the output
+ * resolution.  The render resolution follows the switch at once (the
+ * reference waits for its next resizeResolution); kpt_get_render_size
+ * gives it. */
 typedef struct kpt_settings {
     int32_t max_depth;
     int32_t bloom, karis, auto_exposure;
@@ -116,6 +121,10 @@ kpt_status kpt_destroy(kpt_context* ctx);
 
 /* Renderer::resizeResolution (renderer.cu:55-101): render size; clears the accumulation. */
 kpt_status kpt_resize(kpt_context* ctx, int width, int height);
+/* The render resolution (the output's unless upscaling); kpt_read_render,
+ * kpt_read_accumulation and kpt_read_albedo have this size, kpt_read_image
+ * the output's. */
+kpt_status kpt_get_render_size(kpt_context* ctx, int* width, int* height);
 
 /* Scene upload, Renderer::loadScene (renderer.cu:356-436).  A mesh is a
  * triangle list (positions and normals 9 floats per triangle, uvs 6, one

@@ -87,6 +87,7 @@ SIGNATURES = {
     "kpt_create": (_S, [C.c_int, C.POINTER(_P)]),
     "kpt_destroy": (_S, [_P]),
     "kpt_resize": (_S, [_P, C.c_int, C.c_int]),
+    "kpt_get_render_size": (_S, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "kpt_set_materials": (_S, [_P, C.c_int, C.POINTER(Material)]),
     "kpt_set_textures": (_S, [_P, C.c_int, _I, C.c_size_t, C.POINTER(C.c_uint8)]),
     "kpt_upload_mesh": (_S, [_P, C.c_int, _F, _F, _F, _I, C.POINTER(C.c_int)]),

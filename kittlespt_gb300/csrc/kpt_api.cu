@@ -117,8 +117,10 @@ struct kpt_context {
     kpt_settings settings;
     kpt_exposure exposure;
 
-    // frame buffers
-    int W = 0, H = 0;
+    // frame buffers: W x H is the render resolution, OW x OH the output's
+    // (smaller by 2.5 with upscaling, resizeResolution renderer.cu:55-101)
+    int W = 0, H = 0, OW = 0, OH = 0;
+    DBuf<float4> output;        // the render upscaled to the output resolution (upscale)
     int frame_index = 0;
     DBuf<float4> acc, albedo, render, image;
     // temporal accumulation: visible surface, distances of the previous frame
@@ -273,7 +275,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
-    c->vis.release(); c->tinst.release(); c->backbuf.release();
+    c->vis.release(); c->tinst.release(); c->backbuf.release(); c->output.release();
     for (int k = 0; k < 2; ++k) { c->thist[k].release(); c->tdepth[k].release(); }
     for (auto& m : c->mips) m.release();
     c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
@@ -317,18 +319,24 @@ static kpt_status ensure_temporal(kpt_context* c) {
     return KPT_OK;
 }
 
-kpt_status kpt_resize(kpt_context* c, int w, int h) {
-    if (!c || w <= 0 || h <= 0) return fail(KPT_ERR_INVALID, "kpt_resize: bad size");
-    KPT_CUDA(cudaSetDevice(c->device));
-    if (w == c->W && h == c->H) return KPT_OK;
+// Renderer::resizeResolution (renderer.cu:55-101): output w x h, render
+// resolution the output's / 2.5 with upscaling; an existing camera gets the
+// projection of its field of view at the render aspect (near 0.1, far 100).
+static kpt_status apply_resolution(kpt_context* c, int w, int h) {
+    const bool up = c->settings.upscale != 0;
+    const float scale_factor = 2.5f;
+    const int rw = up ? std::max(1, (int)((float)w / scale_factor)) : w;
+    const int rh = up ? std::max(1, (int)((float)h / scale_factor)) : h;
+    if (w == c->OW && h == c->OH && rw == c->W && rh == c->H) return KPT_OK;
     KPT_CUDA(cudaStreamSynchronize(c->stream));
-    size_t np = (size_t)w * h;
+    size_t np = (size_t)rw * rh, no = (size_t)w * h;
     KPT_CUDA(c->acc.ensure(np));
     KPT_CUDA(c->albedo.ensure(np));
     KPT_CUDA(c->render.ensure(np));
-    KPT_CUDA(c->image.ensure(np));
     KPT_CUDA(c->first_hit.ensure(np));
-    // bloom mip chain (mipchain.cuh:17-36): levels below mip 0, at most 6
+    KPT_CUDA(c->image.ensure(no));
+    if (up) KPT_CUDA(c->output.ensure(no));
+    // bloom mip chain at the output resolution (mipchain.cuh:17-36): levels below mip 0, at most 6
     int levels = std::min((int)std::log2((double)w), (int)std::log2((double)h));
     levels = std::min(levels, 6);
     for (auto& m : c->mips) m.release();
@@ -338,8 +346,26 @@ kpt_status kpt_resize(kpt_context* c, int w, int h) {
         c->mip_dims[l] = make_int2(w >> l, h >> l);
         KPT_CUDA(c->mips[l].ensure((size_t)(w >> l) * (h >> l)));
     }
-    c->W = w;
-    c->H = h;
+    c->W = rw;
+    c->H = rh;
+    c->OW = w;
+    c->OH = h;
+    if (c->has_camera) {
+        // recompute projection for new screen size (renderer.cu:77-83)
+        float proj[16];
+        inverse4(c->inv_proj, proj);
+        const float fov = 2.0f * atanf(1.0f / proj[5]);
+        const float hh = cosf(0.5f * fov) / sinf(0.5f * fov);
+        const float ww = hh * (float)rh / (float)rw;
+        const float zn = 0.1f, zf = 100.0f;
+        float p[16] = {0};
+        p[0] = ww;
+        p[5] = hh;
+        p[10] = (zf + zn) / (zf - zn);
+        p[11] = 1.0f;
+        p[14] = -(2.0f * zf * zn) / (zf - zn);
+        inverse4(p, c->inv_proj);
+    }
     c->vis.release();   // the temporal buffers are re-created (zeroed) at the new size
     for (int k = 0; k < 2; ++k) {
         c->thist[k].release();
@@ -347,6 +373,19 @@ kpt_status kpt_resize(kpt_context* c, int w, int h) {
     }
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
     return clear_accumulation(c);
+}
+
+kpt_status kpt_resize(kpt_context* c, int w, int h) {
+    if (!c || w <= 0 || h <= 0) return fail(KPT_ERR_INVALID, "kpt_resize: bad size");
+    KPT_CUDA(cudaSetDevice(c->device));
+    return apply_resolution(c, w, h);
+}
+
+kpt_status kpt_get_render_size(kpt_context* c, int* w, int* h) {
+    if (!c || !w || !h) return fail(KPT_ERR_INVALID, "kpt_get_render_size: null argument");
+    *w = c->W;
+    *h = c->H;
+    return KPT_OK;
 }
 
 kpt_status kpt_set_materials(kpt_context* c, int n, const kpt_material* m) {
@@ -753,8 +792,13 @@ kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
         return fail(KPT_ERR_INVALID, "kpt_set_settings: temporal_accumulation must be 0 or 1");
     if (s->postprocess_effects != 0 && s->postprocess_effects != 1)
         return fail(KPT_ERR_INVALID, "kpt_set_settings: postprocess_effects must be 0 or 1");
-    if (s->upscale != 0) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscaling is not supported");
+    if (s->upscale != 0 && s->upscale != 1) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscale must be 0 or 1");
+    const bool resize = s->upscale != c->settings.upscale && c->OW > 0;
     c->settings = *s;
+    if (resize) {   // the render resolution follows the switch at once
+        kpt_status st = apply_resolution(c, c->OW, c->OH);
+        if (st != KPT_OK) return st;
+    }
     return clear_accumulation(c);
 }
 kpt_status kpt_get_settings(kpt_context* c, kpt_settings* s) {
@@ -1028,18 +1072,26 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
         k_exposure<<<1, 32, 0, s>>>(c->hist.p, c->expo_state.p, in);
         c->launches += 2;
     }
+    // launchUpscaleComputeKernel (kernels.cu:84-104): bilinear without FSR
+    const bool up = c->settings.upscale != 0;
+    const float4* out = up ? c->output.p : c->render.p;
+    if (up) {
+        k_upscale<<<dim3((c->OW + 15) / 16, (c->OH + 15) / 16), dim3(16, 16), 0, s>>>(c->render.p, c->W, c->H,
+                                                                                 c->output.p, c->OW, c->OH);
+        c->launches += 1;
+    }
     const float4* bloom0 = nullptr;
     int levels = (int)c->mips.size() - 1;
     if (c->settings.bloom && levels > 0) {
         dim3 b(16, 16);
         for (int l = 0; l < levels; ++l) {
             int2 sd = c->mip_dims[l], dd = c->mip_dims[l + 1];
-            const float4* src = l == 0 ? c->render.p : c->mips[l].p;
+            const float4* src = l == 0 ? out : c->mips[l].p;
             k_bloom_down<<<dim3((dd.x + 15) / 16, (dd.y + 15) / 16), b, 0, s>>>(src, sd.x, sd.y, c->mips[l + 1].p, dd.x, dd.y,
                                                                                c->settings.karis && l == 0);
         }
-        // mip 0 starts as a copy of the render (renderer.cu:446-451)
-        cudaMemcpyAsync(c->mips[0].p, c->render.p, sizeof(float4) * (size_t)np, cudaMemcpyDeviceToDevice, s);
+        // mip 0 starts as a copy of the output (renderer.cu:446-451)
+        cudaMemcpyAsync(c->mips[0].p, out, sizeof(float4) * (size_t)c->OW * c->OH, cudaMemcpyDeviceToDevice, s);
         for (int l = levels; l > 0; --l) {
             int2 sd = c->mip_dims[l], dd = c->mip_dims[l - 1];
             k_bloom_up<<<dim3((dd.x + 15) / 16, (dd.y + 15) / 16), b, 0, s>>>(c->mips[l].p, sd.x, sd.y, c->mips[l - 1].p,
@@ -1052,12 +1104,13 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
     double lavg = (10.0 / 0.65) * ((N * N) / ((double)c->exposure.iso * (double)c->exposure.shutter));
     float fixed_scalar = (float)(0.18 / lavg);
     const bool fx = c->settings.postprocess_effects != 0;
-    k_tonemap<<<dim3((c->W + 15) / 16, (c->H + 15) / 16), dim3(16, 16), 0, s>>>(
-        c->W, c->H, c->render.p, bloom0, bloom0 != nullptr, c->settings.bloom_final_blend, c->expo_state.p, fixed_scalar,
+    k_tonemap<<<dim3((c->OW + 15) / 16, (c->OH + 15) / 16), dim3(16, 16), 0, s>>>(
+        c->OW, c->OH, out, bloom0, bloom0 != nullptr, c->settings.bloom_final_blend, c->expo_state.p, fixed_scalar,
         c->settings.auto_exposure, c->exposure.white_ev, c->exposure.black_ev, fx ? c->backbuf.p : c->image.p);
     c->launches += 1;
     if (fx) {   // launchFxComputeKernel (renderer.cu:162-167)
-        k_effects<<<dim3((c->W + 15) / 16, (c->H + 15) / 16), dim3(16, 16), 0, s>>>(c->W, c->H, c->backbuf.p, c->image.p);
+        k_effects<<<dim3((c->OW + 15) / 16, (c->OH + 15) / 16), dim3(16, 16), 0, s>>>(c->OW, c->OH, c->backbuf.p,
+                                                                                    c->image.p);
         c->launches += 1;
     }
     stage_mark(c, KPT_STAGE_COUNT);   // end of the last interval
@@ -1120,7 +1173,7 @@ static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     F->acc = c->acc.p;
     F->albedo = c->albedo.p;
     F->first_hit = c->first_hit.p;
-    if (c->settings.postprocess_effects) KPT_CUDA(c->backbuf.ensure((size_t)c->W * c->H));
+    if (c->settings.postprocess_effects) KPT_CUDA(c->backbuf.ensure((size_t)c->OW * c->OH));
     if (c->settings.temporal_accumulation) {
         st = ensure_temporal(c);
         if (st != KPT_OK) return st;
@@ -1248,7 +1301,7 @@ static kpt_status read_buf(kpt_context* c, const void* src, void* dst, size_t by
     KPT_CUDA(cudaStreamSynchronize(c->stream));
     return KPT_OK;
 }
-kpt_status kpt_read_image(kpt_context* c, float* rgba) { return read_buf(c, c ? c->image.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
+kpt_status kpt_read_image(kpt_context* c, float* rgba) { return read_buf(c, c ? c->image.p : nullptr, rgba, c ? 16 * (size_t)c->OW * c->OH : 0); }
 kpt_status kpt_read_render(kpt_context* c, float* rgba) { return read_buf(c, c ? c->render.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
 kpt_status kpt_read_accumulation(kpt_context* c, float* rgba) { return read_buf(c, c ? c->acc.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
 kpt_status kpt_read_albedo(kpt_context* c, float* rgba) { return read_buf(c, c ? c->albedo.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }

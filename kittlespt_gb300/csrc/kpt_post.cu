@@ -426,3 +426,22 @@ __global__ void k_effects(int W, int H, const float4* src, float4* dst) {
 }
 
 }  // namespace kpt
+
+namespace kpt {
+
+// upscale (upscale.cuh:260-291, USE_FSR undefined): destination pixel
+// (x, y) / destination size * source size, read with textureReadBilinear
+// (device_texture_buffer.cuh:42-80) filtering all four channels.
+__global__ void k_upscale(const float4* src, int sw, int sh, float4* dst, int dw, int dh) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= dw || y >= dh) return;
+    const float px = __fmul_rn(__fdiv_rn((float)x, (float)dw), (float)sw);
+    const float py = __fmul_rn(__fdiv_rn((float)y, (float)dh), (float)sh);
+    const int ix = (int)px, iy = (int)py;
+    const float ws = __fsub_rn(px, (float)ix), wt = __fsub_rn(py, (float)iy);
+    const float4 c0 = tex_nearest(src, sw, sh, ix, iy), c1 = tex_nearest(src, sw, sh, ix + 1, iy);
+    const float4 c2 = tex_nearest(src, sw, sh, ix, iy + 1), c3 = tex_nearest(src, sw, sh, ix + 1, iy + 1);
+    dst[(size_t)y * dw + x] = lerp4(lerp4(c0, c1, ws), lerp4(c2, c3, ws), wt);
+}
+
+}  // namespace kpt

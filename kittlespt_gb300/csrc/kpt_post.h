@@ -28,5 +28,8 @@ __global__ void k_tonemap(int W, int H, const float4* render, const float4* bloo
 // computeEffects (kernels.cu:506-527): fisheye and chromatic aberration of
 // the tonemapped image
 __global__ void k_effects(int W, int H, const float4* src, float4* dst);
+// upscale without FSR (upscale.cuh:260-291): bilinear read of the render at
+// the output pixel's position
+__global__ void k_upscale(const float4* src, int sw, int sh, float4* dst, int dw, int dh);
 
 }  // namespace kpt

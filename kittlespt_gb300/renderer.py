@@ -257,14 +257,24 @@ class Renderer:
         """Display image (AgX, non-linear sRGB), [H][W][4] float."""
         return self._read(self._L.kpt_read_image)
 
+    def render_size(self):
+        """(width, height) of the render resolution (the output's unless upscaling)."""
+        w, h = C.c_int(), C.c_int()
+        K.check(self._L.kpt_get_render_size(self._ctx, C.byref(w), C.byref(h)))
+        return w.value, h.value
+
+    def _read_render_res(self, fn):
+        w, h = self.render_size()
+        return self._read(fn, (h, w, 4))
+
     def read_render(self) -> np.ndarray:
-        return self._read(self._L.kpt_read_render)
+        return self._read_render_res(self._L.kpt_read_render)
 
     def read_accumulation(self) -> np.ndarray:
-        return self._read(self._L.kpt_read_accumulation)
+        return self._read_render_res(self._L.kpt_read_accumulation)
 
     def read_albedo(self) -> np.ndarray:
-        return self._read(self._L.kpt_read_albedo)
+        return self._read_render_res(self._L.kpt_read_albedo)
 
     def read_histogram(self) -> np.ndarray:
         out = np.zeros(256, np.uint64)

@@ -2171,4 +2171,25 @@ void orc_effects(int W, int H, const float* src, float* dst) {
         }
 }
 
+// upscale without FSR (upscale.cuh:260-291): every output pixel reads the
+// render [sh][sw][4] bilinearly (textureReadBilinear, all channels) at
+// (x / dw * sw, y / dh * sh).
+void orc_upscale(int sw, int sh, const float* src, int dw, int dh, float* dst) {
+    auto tex = [&](int x, int y) {
+        x = std::min(std::max(x, 0), sw - 1);
+        y = std::min(std::max(y, 0), sh - 1);
+        const float* q = src + 4 * ((size_t)y * sw + x);
+        return F4(q[0], q[1], q[2], q[3]);
+    };
+    for (int y = 0; y < dh; ++y)
+        for (int x = 0; x < dw; ++x) {
+            const float px = (float)x / (float)dw * (float)sw, py = (float)y / (float)dh * (float)sh;
+            const int ix = (int)px, iy = (int)py;
+            const float ws = px - (float)ix, wt = py - (float)iy;
+            const f4 c = lerp4(lerp4(tex(ix, iy), tex(ix + 1, iy), ws), lerp4(tex(ix, iy + 1), tex(ix + 1, iy + 1), ws), wt);
+            float* o = dst + 4 * ((size_t)y * dw + x);
+            o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
+        }
+}
+
 }  // extern "C"

@@ -82,6 +82,7 @@ def lib(prefix: str = "orc"):
         g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
         g("temporal_frame").argtypes = [C.c_int, C.c_int, _f, _f, _f, _f, C.c_int, _f, _f, _i, _f, _f, _f, _f, _f]
         g("effects").argtypes = [C.c_int, C.c_int, _f, _f]
+        g("upscale").argtypes = [C.c_int, C.c_int, _f, C.c_int, C.c_int, _f]
     else:
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _f]
         g("exposure").argtypes = [_f] + [C.c_float] * 12 + [_f]
@@ -256,6 +257,15 @@ def effects(image):
     H, W = image.shape[:2]
     out = np.zeros((H, W, 4), np.float32)
     lib().orc_effects(W, H, np.ascontiguousarray(image, np.float32).reshape(-1), out.reshape(-1))
+    return out
+
+
+def upscale(render, width, height):
+    """upscale without FSR (upscale.cuh:260-291) of a render [h, w, 4] to
+    [height, width, 4]."""
+    sh, sw = render.shape[:2]
+    out = np.zeros((height, width, 4), np.float32)
+    lib().orc_upscale(sw, sh, np.ascontiguousarray(render, np.float32).reshape(-1), width, height, out.reshape(-1))
     return out
 
 

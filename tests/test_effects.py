@@ -36,3 +36,30 @@ def test_effects_match_oracle(w, h):
     same = (imgs[1] == ref).all(-1)
     assert same.mean() >= 0.995, f"{same.mean():.4f} of pixels equal"
     assert not np.array_equal(imgs[0], imgs[1])   # the effects changed the image
+
+
+@pytest.mark.parametrize("bloom", [0, 1])
+def test_upscale_matches_oracle(bloom):
+    """kpt_settings.upscale (the reference's upscale_enable without FSR): the
+    render at the output resolution / 2.5, upscaled bilinearly, then bloom and
+    tonemapping at the output resolution."""
+    from kittlespt_gb300.renderer import Renderer
+    sc = S.scene_small(80, 60, 1, 3)
+    sc.settings["bloom"] = bloom
+    r = Renderer(0)
+    r.initialize()
+    try:
+        r.load_scene(sc)
+        r.set_renderer_settings(upscale=1)
+        assert r.render_size() == (32, 24)
+        r.execute_rendering(16.0, 2)
+        r.synchronize()
+        render = r.read_render()
+        img = r.get_render_target()
+    finally:
+        r.shutdown()
+    assert render.shape == (24, 32, 4) and img.shape == (60, 80, 4)
+    out = O.upscale(render, 80, 60)
+    bl = O.bloom(out, False, float(sc.settings["bloom_internal_blend"])) if bloom else None
+    ref = O.post_image(out, bl, float(sc.settings["bloom_final_blend"]), O.exposure_scalar(sc.exposure))
+    assert np.abs(img - ref).max() <= 2e-5
