@@ -100,6 +100,23 @@ __global__ void k_sky_grad(SkyParams P, int n, const float3* dirs, float3* out) 
     for (int k = 0; k < SKY_PARAMS; ++k) out[7 * (size_t)i + 1 + k] = J[k];
 }
 
+// The double-precision sky Jacobian where the single-precision march is
+// ill-conditioned: near the horizon and the sun.
+__device__ __forceinline__ bool sky_in_band(const SkyParams& P, float3 d) {
+    return fabsf(d.y) < 0.05f || dot(d, P.sun_dir) > 0.995f;
+}
+
+// Queues an escape's double-precision Jacobian with its gradient weight;
+// false when the queue is full (the caller evaluates it at once).
+__device__ __forceinline__ bool sky_defer(const AdjParams& A, float3 d, float3 w) {
+    if (!A.skyq) return false;
+    const int q = atomicAdd(A.skyq_count, 1);
+    if (q >= A.skyq_cap) return false;
+    A.skyq[2 * (size_t)q] = make_float4(d.x, d.y, d.z, 0.0f);
+    A.skyq[2 * (size_t)q + 1] = make_float4(w.x, w.y, w.z, 0.0f);
+    return true;
+}
+
 // Pixels whose camera ray misses: every sample is sky(d) * LeSun(d).
 __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjParams A) {
     extern __shared__ double sg[];
@@ -115,12 +132,17 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjP
         float3 J[SKY_PARAMS];
         const float ls = le_sun(P, r.d);
         float3 L = nishita_grad(P, obs, r.d, J) * ls;
-        if (fabsf(r.d.y) < 0.05f || dot(r.d, P.sun_dir) > 0.995f) nishita_jacobian_d(P, obs, r.d, J);
         float3 m;
         float3 Lc = make_float3(clamp_out(L.x, &m.x), clamp_out(L.y, &m.y), clamp_out(L.z, &m.z));
         const float4 a = A.adjoint[p];
         const float3 g = make_float3(a.x, a.y, a.z) * m * ls;   // mean over identical samples
-        for (int k = 0; k < SKY_PARAMS; ++k) acc.add(4 * A.nmat + k, wdot(g, J[k]));
+        bool done = false;
+        if (sky_in_band(P, r.d)) {
+            done = sky_defer(A, r.d, g);
+            if (!done) nishita_jacobian_d(P, obs, r.d, J);
+        }
+        if (!done)
+            for (int k = 0; k < SKY_PARAMS; ++k) acc.add(4 * A.nmat + k, wdot(g, J[k]));
         if (A.image) A.image[p] = make_float4(Lc.x, Lc.y, Lc.z, 0.0f);
     }
     grad_end(sg, ng, A.grad);
@@ -165,6 +187,7 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
         bool escaped = false;
         float3 s_end = make_float3(0.0f, 0.0f, 0.0f), b_end = s_end, d_end = s_end;
         float3 J_end[SKY_PARAMS];
+        bool d_band = false;
         for (int level = 0;; ++level) {
             if (level > 0) {
                 Hit hh = trace_closest(s, make_xray(o, d), 0.0f, __int_as_float(0x7f800000), st, stack);
@@ -175,8 +198,10 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
                 s_end = nishita_grad(P, obs, d, J_end);
                 // near the sun (Mie forward peak) and the horizon the
                 // single-precision march's derivatives are ill-conditioned:
-                // there the Jacobian is evaluated in double
-                if (fabsf(d.y) < 0.05f || dot(d, P.sun_dir) > 0.995f) nishita_jacobian_d(P, obs, d, J_end);
+                // there the Jacobian is evaluated in double, deferred to
+                // k_adjoint_sky_d (the FP64 march then runs on full warps)
+                d_band = sky_in_band(P, d);
+                if (d_band && !A.skyq) nishita_jacobian_d(P, obs, d, J_end);
                 b_end = beta;
                 d_end = d;
                 break;
@@ -399,7 +424,13 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
         if (nonzero(g)) {
             if (escaped) {
                 const float3 gb = wmul(g, b_end);
-                for (int i = 0; i < SKY_PARAMS; ++i) gsky[i] += wdot(gb, J_end[i]);
+                bool done = false;
+                if (d_band && A.skyq) {
+                    done = sky_defer(A, d_end, gb);
+                    if (!done) nishita_jacobian_d(P, obs, d_end, J_end);
+                }
+                if (!done)
+                    for (int i = 0; i < SKY_PARAMS; ++i) gsky[i] += wdot(gb, J_end[i]);
             }
             for (int k = nv - 1; k >= 0; --k) {
                 const float3 gb = wmul(g, vb[k]);
@@ -450,6 +481,32 @@ __device__ __forceinline__ void adjoint_block(const FrameParams& F, const AdjPar
 }
 
 __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint(FrameParams F, AdjParams A) { adjoint_block<false>(F, A); }
+
+// The deferred double-precision sky Jacobians: weight . J(d) per queued
+// escape, summed into the sky parameters' gradients.
+__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_sky_d(FrameParams F, AdjParams A) {
+    __shared__ double sg[SKY_PARAMS];
+    if (threadIdx.x < SKY_PARAMS) sg[threadIdx.x] = 0.0;
+    __syncthreads();
+    const SkyParams& P = F.sky;
+    const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
+    const int n = min(*A.skyq_count, A.skyq_cap);
+    double gsky[SKY_PARAMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = A.skyq[2 * (size_t)i], b = A.skyq[2 * (size_t)i + 1];
+        float3 J[SKY_PARAMS];
+        nishita_jacobian_d(P, obs, make_float3(a.x, a.y, a.z), J);
+        const float3 w = make_float3(b.x, b.y, b.z);
+        for (int k = 0; k < SKY_PARAMS; ++k) gsky[k] += wdot(w, J[k]);
+    }
+    for (int k = 0; k < SKY_PARAMS; ++k) {
+        double v = gsky[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sg + k, v);
+    }
+    __syncthreads();
+    if (threadIdx.x < SKY_PARAMS && sg[threadIdx.x] != 0.0) atomicAdd(A.grad + 4 * A.nmat + threadIdx.x, sg[threadIdx.x]);
+}
 __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_rec(FrameParams F, AdjParams A) { adjoint_block<true>(F, A); }
 
 }  // namespace kpt

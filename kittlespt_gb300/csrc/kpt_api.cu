@@ -151,6 +151,8 @@ struct kpt_context {
     DBuf<float> adj_in, adj_image;
     DBuf<double> adj_grad;
     DBuf<int> rec_count;
+    DBuf<float4> adj_skyq;      // deferred double-precision sky Jacobians: (direction, weight)
+    DBuf<int> adj_skyq_count;
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2], unsorted;
     DBuf<int> octants;
@@ -286,6 +288,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->unsorted.release(); c->octants.release();
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
+    c->adj_skyq.release(); c->adj_skyq_count.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
     if (c->ev_sky) cudaEventDestroy(c->ev_sky);
@@ -1560,6 +1563,12 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     if (st != KPT_OK) return st;
     KPT_CUDA(c->sun_J.ensure(ADJ_SKY_PARAMS));
     KPT_CUDA(c->rec_count.ensure(1));
+    // room for every sample's escape and every missing pixel
+    const size_t qcap = (size_t)c->W * c->H * ((size_t)nsamples + 1);
+    if (!rec) {
+        KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
+        KPT_CUDA(c->adj_skyq_count.ensure(1));
+    }
     FrameParams F = frame_params(c, sample0, nsamples);
     AdjParams A{};
     A.adjoint = reinterpret_cast<const float4*>(adjoint);
@@ -1570,11 +1579,17 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     A.rec_count = c->rec_count.p;
     A.max_rec = max_rec;
     A.nmat = (int)c->materials.size();
+    if (!rec) {   // the records' test path keeps the double Jacobians where they occur
+        A.skyq = c->adj_skyq.p;
+        A.skyq_count = c->adj_skyq_count.p;
+        A.skyq_cap = (int)(c->adj_skyq.n / 2);
+    }
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
     KPT_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * ng, s));
     if (image) KPT_CUDA(cudaMemsetAsync(image, 0, sizeof(float4) * (size_t)np, s));
     KPT_CUDA(cudaMemsetAsync(c->rec_count.p, 0, sizeof(int), s));
+    if (A.skyq) KPT_CUDA(cudaMemsetAsync(A.skyq_count, 0, sizeof(int), s));
     KPT_CUDA(cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s));
     const void* kern = rec ? (const void*)k_adjoint_rec : (const void*)k_adjoint;
     for (const void* k : {kern, (const void*)k_adjoint_miss})
@@ -1589,6 +1604,10 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     if (rec) k_adjoint_rec<<<grid, PATH_BLOCK, smem, s>>>(F, A);
     else k_adjoint<<<grid, PATH_BLOCK, smem, s>>>(F, A);
     c->launches += 5;
+    if (A.skyq) {
+        k_adjoint_sky_d<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
+        c->launches += 1;
+    }
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;
 }

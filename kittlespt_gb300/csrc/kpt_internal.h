@@ -116,6 +116,12 @@ struct AdjParams {
     int* rec_count;
     int max_rec;
     int nmat;
+    // escapes whose sky Jacobian is evaluated in double (near the horizon or
+    // the sun): (direction, gradient weight) pairs for k_adjoint_sky_d; null:
+    // evaluated where they occur
+    float4* skyq;
+    int* skyq_count;
+    int skyq_cap;
 };
 
 // Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
@@ -153,6 +159,7 @@ __global__ void k_sky_grad(SkyParams P, int n, const float3* dirs, float3* out);
 __global__ void k_adjoint_miss(FrameParams F, AdjParams A);
 __global__ void k_adjoint(FrameParams F, AdjParams A);
 __global__ void k_adjoint_rec(FrameParams F, AdjParams A);   // also writes the frozen-path records
+__global__ void k_adjoint_sky_d(FrameParams F, AdjParams A);
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
 // Temporal accumulation (kernels.cu:164-327): per instance, the matrices of
 // computeVelocity and testReprojection for one frame, rows of column-major
