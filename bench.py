@@ -652,6 +652,66 @@ def run_blas(args):
     print(json.dumps(out))
 
 
+def run_upscale(args):
+    """Upscaling (kpt_settings.upscale): the full-frame scene displayed at
+    1920x1080 and rendered at 768x432 (output / 2.5), 16 spp, depth 8, the
+    render upscaled bilinearly (1) or by the FSR path, EASU + RCAS (2), with
+    bloom, exposure and tonemapping at the output size; native 1080p frames
+    (0) beside them.  Device time per frame over K frames (CUDA events on the
+    library's stream, L2 flushed between frames) and the post chain's own time
+    (event nodes around it in the frame's graph)."""
+    import torch
+    from kittlespt_gb300 import _lib as K
+    from kittlespt_gb300 import scenes as S
+    from kittlespt_gb300.renderer import Renderer
+    r = Renderer(0)
+    r.initialize()
+    r.load_scene(S.scene_full(W, H, SPP, DEPTH))
+    stream = torch.cuda.ExternalStream(r.stream(), device=0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=0)
+    res = {}
+    try:
+        for mode, name in ((0, "native"), (1, "bilinear"), (2, "fsr")):
+            r.set_renderer_settings(upscale=mode)
+            for _ in range(args.warmup):
+                r.execute_rendering(16.0, SPP)
+                with torch.cuda.stream(stream):
+                    flush.add_(1.0)
+            r.synchronize()
+            torch.cuda.synchronize()
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                start.record(stream)
+                for k in range(args.steps):
+                    r.execute_rendering(16.0, SPP)
+                    if k + 1 < args.steps:
+                        flush.add_(1.0)
+                stop.record(stream)
+            r.synchronize()
+            torch.cuda.synchronize()
+            ms = start.elapsed_time(stop) / args.steps
+            K.check(r._L.kpt_enable_timing(r.ctx, 1))
+            for _ in range(4):
+                r.execute_rendering(16.0, SPP)
+            sms = (C.c_float * len(K.STAGES))()
+            K.check(r._L.kpt_stage_ms(r.ctx, 3, sms))
+            K.check(r._L.kpt_enable_timing(r.ctx, 0))
+            rw, rh = r.render_size()
+            res[name] = {"render": f"{rw}x{rh}", "ms_per_frame": ms, "post_ms": sms[K.STAGES.index("post")] / 3}
+            print(f"[bench] {name}: render {rw}x{rh}, {ms:.2f} ms/frame, post chain "
+                  f"{res[name]['post_ms']:.3f} ms", file=sys.stderr)
+    finally:
+        r.shutdown()
+    f = res["fsr"]
+    out = {"metric": "frames/s, 1920x1080 output upscaled by FSR 1.0 from 768x432 (16 spp, depth 8)",
+           "value": 1e3 / f["ms_per_frame"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": f["ms_per_frame"], "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded procedural scene)",
+           "config": {"workload": "upscale_1080p_from_768x432", "output": f"{W}x{H}", "spp": SPP,
+                      "max_depth": DEPTH, "l2": "flushed between frames"}, "modes": res}
+    print(json.dumps(out))
+
+
 def run_profile_case(spec):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
     small case that ncu captures of single kernels run on."""
@@ -675,10 +735,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "adjoint", "traversal", "blas"],
+    ap.add_argument("--workload", default="frame",
+                    choices=["frame", "batch", "adjoint", "traversal", "blas", "upscale"],
                     help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one; "
                          "adjoint: gradient evaluations/s of the path-replay adjoint; "
-                         "traversal: rays/s on 2M random triangles; blas: BLAS build on upload, host vs device")
+                         "traversal: rays/s on 2M random triangles; blas: BLAS build on upload, host vs device; "
+                         "upscale: 1080p output rendered at 1/2.5 and upscaled, bilinear and FSR")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
     args = ap.parse_args()
@@ -695,6 +757,8 @@ def main():
         run_traversal(args)
     elif args.workload == "blas":
         run_blas(args)
+    elif args.workload == "upscale":
+        run_upscale(args)
     else:
         run_gpu(args)
 

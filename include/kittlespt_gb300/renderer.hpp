@@ -115,6 +115,9 @@ struct RendererSettings {
     bool tonemapper_enable_auto_exposure = false;
     bool postprocess_enable_effects = false;
     bool upscale_enable = false;
+    // the reference's build-time USE_FSR (kernels.cuh:3) as a setting: with
+    // upscale_enable, FSR 1.0 (EASU + RCAS) instead of the bilinear upscale
+    bool upscale_fsr = false;
 };
 
 // pod_types.hpp:60-123 (glTF 2.0 metallic-roughness material)
@@ -383,7 +386,7 @@ public:
         s.bloom_internal_blend = r.bloom_internal_blend;
         s.temporal_accumulation = r.integrator_use_temporal_accumulation;
         s.postprocess_effects = r.postprocess_enable_effects;
-        s.upscale = r.upscale_enable;
+        s.upscale = r.upscale_enable ? (r.upscale_fsr ? 2 : 1) : 0;
         detail::check(kpt_set_settings(ctx(), &s));
     }
     RendererSettings getRendererSettings() const {
@@ -399,6 +402,7 @@ public:
         r.integrator_use_temporal_accumulation = s.temporal_accumulation != 0;
         r.postprocess_enable_effects = s.postprocess_effects != 0;
         r.upscale_enable = s.upscale != 0;
+        r.upscale_fsr = s.upscale == 2;
         return r;
     }
 

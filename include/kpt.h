@@ -71,11 +71,13 @@ typedef struct kpt_environment {
  * postprocess_effects: the reference's lens effects on the display image
  * (computeEffects, kernels.cu:340-374, 506-527): fisheye (power 1.65) and
  * chromatic aberration.
- * upscale: the reference's upscale_enable (without its compiled-out FSR path):
- * the paths, accumulation, modulation and histogram run at the output
- * resolution / 2.5 (truncated), the render is upscaled bilinearly
- * (upscale.cuh:260-291) and bloom, tonemapping and effects run at the output
- * resolution.  The render resolution follows the switch at once (the
+ * upscale: the reference's upscale_enable.  0 off; 1 and 2: the paths,
+ * accumulation, modulation and histogram run at the output resolution / 2.5
+ * (truncated), the render is upscaled to the output resolution, and bloom,
+ * tonemapping and effects run there.  1 upscales bilinearly as the reference
+ * builds it (upscale.cuh:260-291); 2 runs the FSR 1.0 path the reference
+ * compiles with USE_FSR (kernels.cuh:3, kernels.cu:84-104): EASU
+ * (upscale.cuh:13-258) then RCAS sharpening (upscale.cuh:300-433).  The render resolution follows the switch at once (the
  * reference waits for its next resizeResolution); kpt_get_render_size
  * gives it. */
 typedef struct kpt_settings {

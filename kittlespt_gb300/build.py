@@ -1,11 +1,12 @@
 """Builds libkpt.so (the CUDA path tracer behind include/kpt.h) in-tree.
 
-Six translation units, compiled in parallel with nvcc for sm_103a only:
+Seven translation units, compiled in parallel with nvcc for sm_103a only:
 kpt_path.cu (path and ray kernels, fast maths like the reference's GPU
 build), kpt_adjoint.cu (path-replay adjoint, fast maths), kpt_post.cu (post
 chain, IEEE), kpt_api.cu (C ABI), kpt_scene.cpp (host
-acceleration-structure build) and kpt_build.cu (the same BLAS build on the
-GPU, IEEE without contraction).  Host code is compiled without
+acceleration-structure build), kpt_build.cu (the same BLAS build on the
+GPU, IEEE without contraction) and kpt_fsr.cu (the FSR upscale path, IEEE
+without contraction).  Host code is compiled without
 floating-point contraction so x86-64 and aarch64 builds agree.
 """
 
@@ -34,6 +35,7 @@ UNITS = {
     "kpt_api.cu": [],
     "kpt_scene.cpp": [],
     "kpt_build.cu": ["-fmad=false"],
+    "kpt_fsr.cu": ["-fmad=false"],
 }
 
 

@@ -127,6 +127,7 @@ struct kpt_context {
     // and this one, history images (color, frames), per-instance matrices
     DBuf<float4> vis, thist[2];
     DBuf<float4> backbuf;       // the tonemapped image before the effects (postprocess_effects)
+    DBuf<float4> easu;          // the EASU image before sharpening (upscale = 2)
     DBuf<float> tdepth[2];
     int tdepth_prev = 0;
     DBuf<TemporalInst> tinst;
@@ -277,7 +278,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
-    c->vis.release(); c->tinst.release(); c->backbuf.release(); c->output.release();
+    c->vis.release(); c->tinst.release(); c->backbuf.release(); c->output.release(); c->easu.release();
     for (int k = 0; k < 2; ++k) { c->thist[k].release(); c->tdepth[k].release(); }
     for (auto& m : c->mips) m.release();
     c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
@@ -795,8 +796,8 @@ kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
         return fail(KPT_ERR_INVALID, "kpt_set_settings: temporal_accumulation must be 0 or 1");
     if (s->postprocess_effects != 0 && s->postprocess_effects != 1)
         return fail(KPT_ERR_INVALID, "kpt_set_settings: postprocess_effects must be 0 or 1");
-    if (s->upscale != 0 && s->upscale != 1) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscale must be 0 or 1");
-    const bool resize = s->upscale != c->settings.upscale && c->OW > 0;
+    if (s->upscale < 0 || s->upscale > 2) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscale must be 0, 1 or 2");
+    const bool resize = (s->upscale != 0) != (c->settings.upscale != 0) && c->OW > 0;
     c->settings = *s;
     if (resize) {   // the render resolution follows the switch at once
         kpt_status st = apply_resolution(c, c->OW, c->OH);
@@ -1075,13 +1076,18 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
         k_exposure<<<1, 32, 0, s>>>(c->hist.p, c->expo_state.p, in);
         c->launches += 2;
     }
-    // launchUpscaleComputeKernel (kernels.cu:84-104): bilinear without FSR
+    // launchUpscaleComputeKernel (kernels.cu:84-104): bilinear, or with FSR
+    // (upscale = 2) EASU into a scratch image and RCAS from it into the output
     const bool up = c->settings.upscale != 0;
     const float4* out = up ? c->output.p : c->render.p;
-    if (up) {
-        k_upscale<<<dim3((c->OW + 15) / 16, (c->OH + 15) / 16), dim3(16, 16), 0, s>>>(c->render.p, c->W, c->H,
-                                                                                 c->output.p, c->OW, c->OH);
+    const dim3 ob(16, 16), og((c->OW + 15) / 16, (c->OH + 15) / 16);
+    if (c->settings.upscale == 1) {
+        k_upscale<<<og, ob, 0, s>>>(c->render.p, c->W, c->H, c->output.p, c->OW, c->OH);
         c->launches += 1;
+    } else if (c->settings.upscale == 2) {
+        k_easu<<<og, ob, 0, s>>>(c->render.p, c->W, c->H, c->easu.p, c->OW, c->OH);
+        k_rcas<<<og, ob, 0, s>>>(c->easu.p, c->OW, c->OH, c->output.p);
+        c->launches += 2;
     }
     const float4* bloom0 = nullptr;
     int levels = (int)c->mips.size() - 1;
@@ -1177,6 +1183,7 @@ static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     F->albedo = c->albedo.p;
     F->first_hit = c->first_hit.p;
     if (c->settings.postprocess_effects) KPT_CUDA(c->backbuf.ensure((size_t)c->OW * c->OH));
+    if (c->settings.upscale == 2) KPT_CUDA(c->easu.ensure((size_t)c->OW * c->OH));
     if (c->settings.temporal_accumulation) {
         st = ensure_temporal(c);
         if (st != KPT_OK) return st;

@@ -31,5 +31,9 @@ __global__ void k_effects(int W, int H, const float4* src, float4* dst);
 // upscale without FSR (upscale.cuh:260-291): bilinear read of the render at
 // the output pixel's position
 __global__ void k_upscale(const float4* src, int sw, int sh, float4* dst, int dw, int dh);
+// the FSR 1.0 path (kpt_fsr.cu): EASU of the render to the output size, then
+// RCAS of that image
+__global__ void k_easu(const float4* src, int sw, int sh, float4* dst, int dw, int dh);
+__global__ void k_rcas(const float4* src, int w, int h, float4* dst);
 
 }  // namespace kpt

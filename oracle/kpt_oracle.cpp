@@ -2192,4 +2192,147 @@ void orc_upscale(int sw, int sh, const float* src, int dw, int dh, float* dst) {
         }
 }
 
+// FSR 1.0 as the reference compiles it when USE_FSR is defined
+// (kernels.cuh:3; launchUpscaleComputeKernel, kernels.cu:84-104).
+// EASU (upscale.cuh:13-258) reads the render [sh][sw][4] with 12 taps, each a
+// textureReadBilinearUV (device_texture_buffer.cuh:42-86: truncated pixel
+// position, clamped texels, lerps with the remainder, even when it is
+// negative) at a position of the FsrEasuCon constants; RCAS (upscale.cuh:
+// 300-433, sharpness 0, FSR_RCAS_DENOISE undefined) sharpens the EASU image
+// from its plus-shaped neighbourhood, read the same way at (p / size) * size.
+// The reference's double-precision literals (0.5, .4, 1.5625, .29, 1. / lob,
+// 4. * lobe + 1., the RCAS limit) keep their double arithmetic here.  The
+// EASU image goes to easu_out, the sharpened one to dst ([dh][dw][4], alpha 1).
+void orc_fsr(int sw, int sh, const float* src, int dw, int dh, float* easu_out, float* dst) {
+    auto bilinear = [](const float* img, int w, int h, float px, float py) {
+        auto tex = [&](int x, int y) {
+            x = std::min(std::max(x, 0), w - 1);
+            y = std::min(std::max(y, 0), h - 1);
+            const float* q = img + 4 * ((size_t)y * w + x);
+            return F4(q[0], q[1], q[2], q[3]);
+        };
+        const int ix = (int)px, iy = (int)py;
+        const float ws = px - (float)ix, wt = py - (float)iy;
+        return lerp4(lerp4(tex(ix, iy), tex(ix + 1, iy), ws), lerp4(tex(ix, iy + 1), tex(ix + 1, iy + 1), ws), wt);
+    };
+    // FsrEasuCon (upscale.cuh:18-62) with the render size as viewport and input
+    const float inw = (float)sw, inh = (float)sh, ow = (float)dw, oh = (float)dh;
+    const f4 con0 = F4(inw / ow, inh / oh, (float)(0.5 * (double)inw / (double)ow - 0.5),
+                       (float)(0.5 * (double)inh / (double)oh - 0.5));
+    const f4 con1 = F4(1.0f / inw, 1.0f / inh, 1.0f / inw, -1.0f / inh);
+    const f4 con2 = F4(-1.0f / inw, 2.0f / inh, 1.0f / inw, 2.0f / inh);
+    const f2 con3 = F2(0.0f / inw, 4.0f / inh);
+    const f4 off = F4(-0.5f * con1.x, 0.5f * con1.x, -0.5f * con1.y, 0.5f * con1.y);
+    // FsrEasuSetF (upscale.cuh:101-130): direction and edge length of one
+    // bilinear corner from its '+' of lumas
+    auto setf = [](f2& dir, float& len, float w, float lA, float lB, float lC, float lD, float lE) {
+        float lenX = fmaxf(fabsf(lD - lC), fabsf(lC - lB));
+        const float dirX = lD - lB;
+        dir.x += dirX * w;
+        lenX = clampf(fabsf(dirX) / lenX, 0.0f, 1.0f);
+        lenX *= lenX;
+        len += lenX * w;
+        float lenY = fmaxf(fabsf(lE - lC), fabsf(lC - lA));
+        const float dirY = lE - lA;
+        dir.y += dirY * w;
+        lenY = clampf(fabsf(dirY) / lenY, 0.0f, 1.0f);
+        lenY *= lenY;
+        len += lenY * w;
+    };
+    for (int y = 0; y < dh; ++y)
+        for (int x = 0; x < dw; ++x) {
+            // FsrEasuF (upscale.cuh:133-254)
+            float ppx = (float)x * con0.x + con0.z, ppy = (float)y * con0.y + con0.w;
+            const float fpx = floorf(ppx), fpy = floorf(ppy);
+            ppx -= fpx;
+            ppy -= fpy;
+            const f2 p0 = F2(fpx * con1.x + con1.z, fpy * con1.y + con1.w);
+            const f2 p1 = p0 + F2(con2.x, con2.y), p2 = p0 + F2(con2.z, con2.w), p3 = p0 + F2(con3.x, con3.y);
+            auto tap = [&](f2 p, float ox, float oy) {
+                const f2 q = p + F2(ox, oy);
+                return xyz(bilinear(src, sw, sh, q.x * (float)sw, q.y * (float)sh));
+            };
+            auto luma = [](f3 c) { return (float)((double)c.y + 0.5 * (double)(c.x + c.z)); };
+            const f3 bC = tap(p0, off.x, off.w), cC = tap(p0, off.y, off.w);
+            const f3 iC = tap(p1, off.x, off.w), jC = tap(p1, off.y, off.w);
+            const f3 fC = tap(p1, off.y, off.z), eC = tap(p1, off.x, off.z);
+            const f3 kC = tap(p2, off.x, off.w), lC = tap(p2, off.y, off.w);
+            const f3 hC = tap(p2, off.y, off.z), gC = tap(p2, off.x, off.z);
+            const f3 oC = tap(p3, off.y, off.z), nC = tap(p3, off.x, off.z);
+            const float bL = luma(bC), cL = luma(cC), iL = luma(iC), jL = luma(jC), fL = luma(fC), eL = luma(eC);
+            const float kL = luma(kC), lL = luma(lC), hL = luma(hC), gL = luma(gC), oL = luma(oC), nL = luma(nC);
+            f2 dir = F2(0.0f, 0.0f);
+            float len = 0.0f;
+            setf(dir, len, (float)((1.0 - (double)ppx) * (1.0 - (double)ppy)), bL, eL, fL, gL, jL);
+            setf(dir, len, (float)((double)ppx * (1.0 - (double)ppy)), cL, fL, gL, hL, kL);
+            setf(dir, len, (float)((1.0 - (double)ppx) * (double)ppy), fL, iL, jL, kL, nL);
+            setf(dir, len, ppx * ppy, gL, jL, kL, lL, oL);
+            // normalise the direction, shape the length (upscale.cuh:203-225)
+            const float d2x = dir.x * dir.x, d2y = dir.y * dir.y;
+            float dirR = d2x + d2y;
+            const bool zro = dirR < 1.0f / 32768.0f;
+            dirR = 1.0f / sqrtf(dirR);
+            dirR = zro ? 1.0f : dirR;
+            dir.x = zro ? 1.0f : dir.x;
+            dir.x *= dirR;
+            dir.y *= dirR;
+            len = (float)((double)len * 0.5);
+            len *= len;
+            const float stretch = (dir.x * dir.x + dir.y * dir.y) / fmaxf(fabsf(dir.x), fabsf(dir.y));
+            const f2 len2 = F2((float)(1.0 + ((double)stretch - 1.0) * (double)len), (float)(1.0 - 0.5 * (double)len));
+            const float lob = (float)(0.5 - 0.29 * (double)len);
+            const float clp = (float)(1.0 / (double)lob);
+            const f3 min4 = fmin3(fmin3(fC, gC), fmin3(jC, kC));
+            const f3 max4 = fmax3(fmax3(fC, gC), fmax3(jC, kC));
+            f3 aC = F3(0.0f);
+            float aW = 0.0f;
+            // FsrEasuTapF (upscale.cuh:65-98): windowed Lanczos-2 approximation
+            // along the rotated, stretched offset
+            auto tapf = [&](float tx, float ty, f3 c) {
+                const float ox = tx - ppx, oy = ty - ppy;
+                float vx = ox * dir.x + oy * dir.y;
+                float vy = ox * -dir.y + oy * dir.x;
+                vx *= len2.x;
+                vy *= len2.y;
+                const float d2 = fminf(vx * vx + vy * vy, clp);
+                float wB = (float)(0.4 * (double)d2 - 1.0);
+                float wA = (float)((double)(lob * d2) - 1.0);
+                wB *= wB;
+                wA *= wA;
+                wB = (float)(1.5625 * (double)wB - 0.5625);
+                const float w = wB * wA;
+                aC = aC + c * w;
+                aW += w;
+            };
+            tapf(0, -1, bC); tapf(1, -1, cC); tapf(-1, 1, iC); tapf(0, 1, jC);
+            tapf(0, 0, fC); tapf(-1, 0, eC); tapf(1, 1, kC); tapf(2, 1, lC);
+            tapf(2, 0, hC); tapf(1, 0, gC); tapf(1, 2, oC); tapf(0, 2, nC);
+            const f3 pix = fmin3(max4, fmax3(min4, aC / aW));
+            float* o = easu_out + 4 * ((size_t)y * dw + x);
+            o[0] = pix.x; o[1] = pix.y; o[2] = pix.z; o[3] = 1.0f;
+        }
+    // sharpen / FsrRcasF (upscale.cuh:316-375, 415-433)
+    const float fw = (float)dw, fh = (float)dh;
+    for (int y = 0; y < dh; ++y)
+        for (int x = 0; x < dw; ++x) {
+            auto load = [&](float px, float py) {
+                return xyz(bilinear(easu_out, dw, dh, (px / fw) * fw, (py / fh) * fh));
+            };
+            const float sx = (float)x, sy = (float)y;
+            const f3 b = load(sx + 0.0f, sy + -1.0f), d = load(sx + -1.0f, sy + 0.0f), e = load(sx, sy);
+            const f3 f = load(sx + 1.0f, sy + 0.0f), h = load(sx + 0.0f, sy + 1.0f);
+            const f3 mn4 = fmin3(b, fmin3(f, h)), mx4 = fmax3(b, fmax3(f, h));
+            const f3 hitMin = mn4 / (4.0f * mx4);
+            const f3 hitMax = (F3(1.0f) - mx4) / (4.0f * mn4 + -4.0f);
+            const f3 lobeRGB = fmax3(-hitMin, hitMax);
+            const float con = 1.0f;   // FsrRcasCon: exp2(-sharpness), sharpness 0
+            const float lobe = (float)(fmax(-(0.25 - (1.0 / 16.0)),
+                                            fmin((double)fmaxf(lobeRGB.x, fmaxf(lobeRGB.y, lobeRGB.z)), 0.0)) *
+                                       (double)con);
+            const f3 col = (lobe * (((b + d) + h) + f) + e) / (float)(4.0 * (double)lobe + 1.0);
+            float* o = dst + 4 * ((size_t)y * dw + x);
+            o[0] = col.x; o[1] = col.y; o[2] = col.z; o[3] = 1.0f;
+        }
+}
+
 }  // extern "C"

@@ -73,6 +73,8 @@ def lib(prefix: str = "orc"):
     g("post_image").argtypes = [C.c_int, C.c_int, _f, _v, C.c_int, C.c_float, C.c_float, C.c_float,
                                 C.c_float, _f]
     g("metering_weights").argtypes = [C.c_int, C.c_int, _f]
+    g("upscale").argtypes = [C.c_int, C.c_int, _f, C.c_int, C.c_int, _f]
+    g("fsr").argtypes = [C.c_int, C.c_int, _f, C.c_int, C.c_int, _f, _f]
     if prefix == "orc":
         g("sky_double").argtypes = [C.c_int, _v, _v, _v, _v]
         g("adjoint_estimate").restype = C.c_int
@@ -82,7 +84,6 @@ def lib(prefix: str = "orc"):
         g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
         g("temporal_frame").argtypes = [C.c_int, C.c_int, _f, _f, _f, _f, C.c_int, _f, _f, _i, _f, _f, _f, _f, _f]
         g("effects").argtypes = [C.c_int, C.c_int, _f, _f]
-        g("upscale").argtypes = [C.c_int, C.c_int, _f, C.c_int, C.c_int, _f]
     else:
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _f]
         g("exposure").argtypes = [_f] + [C.c_float] * 12 + [_f]
@@ -260,13 +261,26 @@ def effects(image):
     return out
 
 
-def upscale(render, width, height):
+def upscale(render, width, height, prefix="orc"):
     """upscale without FSR (upscale.cuh:260-291) of a render [h, w, 4] to
     [height, width, 4]."""
     sh, sw = render.shape[:2]
     out = np.zeros((height, width, 4), np.float32)
-    lib().orc_upscale(sw, sh, np.ascontiguousarray(render, np.float32).reshape(-1), width, height, out.reshape(-1))
+    getattr(lib(prefix), prefix + "_upscale")(sw, sh, np.ascontiguousarray(render, np.float32).reshape(-1),
+                                              width, height, out.reshape(-1))
     return out
+
+
+def fsr(render, width, height, prefix="orc"):
+    """The reference's FSR 1.0 upscale (EASU, upscale.cuh:13-258) and sharpen
+    (RCAS, upscale.cuh:300-433) of a render [h, w, 4] to [height, width, 4]:
+    returns (EASU image, sharpened image)."""
+    sh, sw = render.shape[:2]
+    easu = np.zeros((height, width, 4), np.float32)
+    out = np.zeros((height, width, 4), np.float32)
+    getattr(lib(prefix), prefix + "_fsr")(sw, sh, np.ascontiguousarray(render, np.float32).reshape(-1),
+                                          width, height, easu.reshape(-1), out.reshape(-1))
+    return easu, out
 
 
 def modulate(acc_sum, nsamples, albedo, prefix="orc"):

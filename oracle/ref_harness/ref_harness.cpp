@@ -22,6 +22,7 @@
 #include "shaders/texture.cu"
 #include "shaders/histogram.cu"
 #include "shaders/bloom.cu"
+#include "shaders/upscale.cuh"
 #include "shaders/integrator.cuh"
 #include "shaders/film.cuh"
 #include "shaders/filter.cuh"
@@ -533,6 +534,76 @@ void ref_post_image(int W, int H, const float* render, const float* bloom, int u
             float4 f = make_float4(frag, 1.0f);
             std::memcpy(image_out + 4 * ((size_t)y * W + x), &f, 16);
         }
+    surfs.resize(1);
+}
+
+// The upscale kernel (upscale.cuh:260-291) as the reference builds it
+// (USE_FSR undefined, kernels.cuh:3): every output pixel reads the render
+// bilinearly.  src: [sh][sw][4], dst: [dh][dw][4].
+void ref_upscale(int sw, int sh, const float* src, int dw, int dh, float* dst) {
+    auto& surfs = host_surfaces();
+    surfs.resize(1);
+    std::vector<float4> s((size_t)sw * sh), d((size_t)dw * dh, make_float4(0, 0, 0, 0));
+    std::memcpy(s.data(), src, sizeof(float4) * s.size());
+    surfs.push_back({s.data(), sw, sh});
+    surfs.push_back({d.data(), dw, dh});
+    DeviceTextureBuffer ts, td;
+    ts.dimensions = make_int2(sw, sh);
+    ts.m_surface_object = 1;
+    td.dimensions = make_int2(dw, dh);
+    td.m_surface_object = 2;
+    blockDim = dim3(8, 8, 1);
+    for (int y = 0; y < dh; ++y)
+        for (int x = 0; x < dw; ++x) {
+            blockIdx = make_uint3(x / 8, y / 8, 0);
+            threadIdx = make_uint3(x % 8, y % 8, 0);
+            upscale(ts, td);
+        }
+    std::memcpy(dst, d.data(), sizeof(float4) * d.size());
+    surfs.resize(1);
+}
+
+// The reference's FSR 1.0 path, compiled out of its build by default
+// (USE_FSR, kernels.cuh:3): launchUpscaleComputeKernel (kernels.cu:84-104)
+// runs the upscale kernel's USE_FSR branch (upscale.cuh:271-283: FsrEasuCon +
+// FsrEasuF of the render into the output) and then the sharpen kernel
+// (upscale.cuh:415-433, RCAS of the output); renderer.cu:142-147 copies the
+// sharpened image back into the output.  This driver runs that branch's body
+// per output pixel with the reference's own FsrEasuCon/FsrEasuF, then the
+// unmodified sharpen kernel one thread at a time.
+void ref_fsr(int sw, int sh, const float* src, int dw, int dh, float* easu_out, float* dst) {
+    auto& surfs = host_surfaces();
+    surfs.resize(1);
+    std::vector<float4> s((size_t)sw * sh), e((size_t)dw * dh, make_float4(0, 0, 0, 0)), d(e);
+    std::memcpy(s.data(), src, sizeof(float4) * s.size());
+    surfs.push_back({s.data(), sw, sh});
+    surfs.push_back({e.data(), dw, dh});
+    surfs.push_back({d.data(), dw, dh});
+    DeviceTextureBuffer ts, te, td;
+    ts.dimensions = make_int2(sw, sh);
+    ts.m_surface_object = 1;
+    te.dimensions = make_int2(dw, dh);
+    te.m_surface_object = 2;
+    td.dimensions = make_int2(dw, dh);
+    td.m_surface_object = 3;
+    for (int y = 0; y < dh; ++y)
+        for (int x = 0; x < dw; ++x) {
+            float3 c;
+            float4 con0, con1, con2, con3;
+            float2 rendersize = make_float2(ts.dimensions);
+            FsrEasuCon(con0, con1, con2, con3, rendersize, rendersize, make_float2(te.dimensions));
+            FsrEasuF(c, make_float2(make_int2(x, y)), con0, con1, con2, con3, ts);
+            te.textureWrite(make_float4(c, 1), make_int2(x, y));
+        }
+    blockDim = dim3(8, 8, 1);
+    for (int y = 0; y < dh; ++y)
+        for (int x = 0; x < dw; ++x) {
+            blockIdx = make_uint3(x / 8, y / 8, 0);
+            threadIdx = make_uint3(x % 8, y % 8, 0);
+            sharpen(te, td);
+        }
+    std::memcpy(easu_out, e.data(), sizeof(float4) * e.size());
+    std::memcpy(dst, d.data(), sizeof(float4) * d.size());
     surfs.resize(1);
 }
 

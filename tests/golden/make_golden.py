@@ -121,6 +121,17 @@ def main():
                post_image=img, post_hist_float=hist, post_exposure=expo, lum=Y,
                lum_bins=O.lum_bins(Y, prefix="ref"), meter_96x54=O.metering_weights(96, 54, "ref"),
                meter_100x37=O.metering_weights(100, 37, "ref"))
+
+    # upscaling of the same render to the output size it is rendered for
+    # (64x36 = 160x90 / 2.5): bilinear, and the FSR path (EASU + RCAS) also on
+    # a high-dynamic-range image with zero patches and an odd ratio
+    hdr = np.exp(rng.normal(0.0, 3.0, (27, 48, 4))).astype(np.float32)
+    hdr[::3, ::5] = 0.0
+    hdr[10:16, 20:30] = 0.25
+    easu, sharp = O.fsr(render, 160, 90, "ref")
+    easu_hdr, sharp_hdr = O.fsr(hdr, 121, 67, "ref")
+    out.update(up_bilinear=O.upscale(render, 160, 90, "ref"), up_easu=easu, up_fsr=sharp, up_hdr=hdr,
+               up_hdr_easu=easu_hdr, up_hdr_fsr=sharp_hdr)
     np.savez_compressed(os.path.join(OUT, "reference_host.npz"), **out)
     print("wrote", os.path.join(OUT, "reference_host.npz"))
 

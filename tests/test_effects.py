@@ -38,11 +38,12 @@ def test_effects_match_oracle(w, h):
     assert not np.array_equal(imgs[0], imgs[1])   # the effects changed the image
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("bloom", [0, 1])
-def test_upscale_matches_oracle(bloom):
-    """kpt_settings.upscale (the reference's upscale_enable without FSR): the
-    render at the output resolution / 2.5, upscaled bilinearly, then bloom and
-    tonemapping at the output resolution."""
+def test_upscale_matches_oracle(bloom, mode):
+    """kpt_settings.upscale (the reference's upscale_enable): the render at the
+    output resolution / 2.5, upscaled bilinearly (1) or by the FSR path, EASU
+    then RCAS (2), then bloom and tonemapping at the output resolution."""
     from kittlespt_gb300.renderer import Renderer
     sc = S.scene_small(80, 60, 1, 3)
     sc.settings["bloom"] = bloom
@@ -50,8 +51,11 @@ def test_upscale_matches_oracle(bloom):
     r.initialize()
     try:
         r.load_scene(sc)
-        r.set_renderer_settings(upscale=1)
+        r.set_renderer_settings(upscale=mode)
         assert r.render_size() == (32, 24)
+        with pytest.raises(Exception):
+            r.set_renderer_settings(upscale=3)
+        assert r.get_renderer_settings().upscale == mode
         r.execute_rendering(16.0, 2)
         r.synchronize()
         render = r.read_render()
@@ -59,7 +63,10 @@ def test_upscale_matches_oracle(bloom):
     finally:
         r.shutdown()
     assert render.shape == (24, 32, 4) and img.shape == (60, 80, 4)
-    out = O.upscale(render, 80, 60)
+    out = O.upscale(render, 80, 60) if mode == 1 else O.fsr(render, 80, 60)[1]
+    if mode == 2:   # the sharpened image is not the bilinear one
+        assert np.abs(out - O.upscale(render, 80, 60)).max() > 1e-3
     bl = O.bloom(out, False, float(sc.settings["bloom_internal_blend"])) if bloom else None
     ref = O.post_image(out, bl, float(sc.settings["bloom_final_blend"]), O.exposure_scalar(sc.exposure))
-    assert np.abs(img - ref).max() <= 2e-5
+    err = np.abs(img - ref).max(-1)
+    assert err.max() <= 2e-5, f"{(err > 2e-5).mean():.4f} of pixels off, worst {err.max()} at {np.argwhere(err > 2e-5)[:8]}"

@@ -92,6 +92,23 @@ def test_post_chain(golden):
     np.testing.assert_array_equal(bits(img), bits(golden["post_image"]))
 
 
+def test_upscale_bilinear_and_fsr(golden):
+    """upscale (upscale.cuh:260-291) and the FSR path (EASU + RCAS, compiled in
+    with USE_FSR), bit for bit, on the post-chain render and on a
+    high-dynamic-range image with zero patches at an odd ratio."""
+    render = golden["post_render"]
+    np.testing.assert_array_equal(bits(O.upscale(render, 160, 90)), bits(golden["up_bilinear"]))
+    easu, sharp = O.fsr(render, 160, 90)
+    np.testing.assert_array_equal(bits(easu), bits(golden["up_easu"]))
+    np.testing.assert_array_equal(bits(sharp), bits(golden["up_fsr"]))
+    easu, sharp = O.fsr(golden["up_hdr"], 121, 67)
+    np.testing.assert_array_equal(bits(easu), bits(golden["up_hdr_easu"]))
+    np.testing.assert_array_equal(bits(sharp), bits(golden["up_hdr_fsr"]))
+    # a constant image stays that constant through EASU and RCAS
+    flat = np.full((20, 24, 4), 0.3, np.float32)
+    assert (O.fsr(flat, 60, 50)[1][..., :3] == np.float32(0.3)).all()
+
+
 def test_histogram_bins_and_weights(golden):
     np.testing.assert_array_equal(O.lum_bins(golden["lum"]), golden["lum_bins"])
     np.testing.assert_array_equal(bits(O.metering_weights(96, 54)), bits(golden["meter_96x54"]))
