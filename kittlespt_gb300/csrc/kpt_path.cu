@@ -225,10 +225,23 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
         if (!first && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
         const float3 wo = -d;
         if (!(bsdf.alpha < 0.001f)) {
-            if (S.get1D() < 0.5f) {
+            // The light sample: each branch draws its numbers and sets up its
+            // direction; the BSDF is then evaluated once for all lanes (the
+            // sun / area-light choice is random per lane, so both branches
+            // run in every warp), and each branch finishes its own sample.
+            const bool sun = S.get1D() < 0.5f;
+            const float dsun = 149.597e9f;
+            // the sun's centre at 1 AU, each product rounded on its own:
+            // target - sun_pos below cancels two values near 1.5e11, which a
+            // fused multiply-add would shift by up to half their ulp (~1e-5
+            // of the difference)
+            const float3 sun_pos = make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
+                                               __fmul_rn(P.sun_dir.z, dsun));
+            float3 wi = P.sun_dir, target, Lem;
+            float pdf = 0.0f, prob = 0.0f;
+            bool eval;
+            if (sun) {
                 // sampleLdSun: jittered point on the sun disc at 1 AU
-                const float dsun = 149.597e9f;
-                float3 sun_pos = P.sun_dir * dsun;
                 float3 off;
                 if (order == 0) {
                     float2 a = S.get2D(0);
@@ -239,26 +252,18 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
                     float2 a = S.get2D(1);
                     off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                 }
-                float3 target = sun_pos + (off * P.sun_radius_m);
-                float3 fcos = bsdf.f(wo, P.sun_dir) * fmaxf(0.0f, dot(P.sun_dir, (si.backface ? -1.0f : 1.0f) * si.ng));
-                const float3 sun_rad = *F.sun_radiance;
-                if (nonzero(fcos) && nonzero(sun_rad)) {
-                    float area = PI_F * Sqr(P.sun_radius_m);
-                    float3 sn = normalize(target - sun_pos), wi = normalize(target - si.pos);
-                    float th = AbsDot(sn, -wi);
-                    float pdf = (1.0f / area) / (th / Sqr(dsun));
-                    float3 Ld = (fcos * sun_rad * 6.0e5f) / pdf;
-                    float3 c = Ld * beta / 0.5f;
-                    if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
-                        emit_shadow(F, si, target, c, item, here + 1, false);
-                }
+                target = make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
+                                     __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
+                                     __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
+                eval = true;
             } else {
                 // sampleLd: uniform light pick, uniform point on the triangle
                 float X = S.get1D();
+                eval = false;
                 if (nl >= 1) {
                     int li = min((int)(X * (float)nl), nl - 1);
                     const LightRec& lt = s.lights[li];
-                    float prob = 1.0f / (float)nl;
+                    prob = 1.0f / (float)nl;
                     float2 uu = S.get2D(order);
                     const InstRec& lir = s.inst[lt.inst];
                     float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
@@ -271,24 +276,37 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
                     float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
                     p = row3(model, p, 1.0f);
                     float3 gn = row3(model, lt.gn, 0.0f);
-                    float pdf = 1.0f / lt.tri_area;
+                    pdf = 1.0f / lt.tri_area;
                     pdf *= Sqr(length(p - si.pos));
                     pdf /= AbsDot(normalize(p - si.pos), gn);
-                    float3 wi = normalize(p - si.pos);
-                    float3 Lem = emission_of(s, lt.material, luv);
-                    if (!(pdf <= 0.0f || !nonzero(Lem))) {
-                        float3 fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
-                        if (nonzero(fcos)) {
-                            float p_l = prob * pdf;
-                            float pb = bsdf.pdf(wo, wi);
-                            float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
-                            float3 Ld = (Lem * fcos * w_l) / p_l;
-                            float3 c = Ld * beta / (1.0f - 0.5f);
-                            if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
-                                emit_shadow(F, si, p, c, item, here + 2, true);
-                        }
-                    }
+                    wi = normalize(p - si.pos);
+                    Lem = emission_of(s, lt.material, luv);
+                    target = p;
+                    eval = !(pdf <= 0.0f || !nonzero(Lem));
                 }
+            }
+            float3 fcos = make_float3(0.0f, 0.0f, 0.0f);
+            if (eval) fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
+            if (sun) {
+                const float3 sun_rad = *F.sun_radiance;
+                if (nonzero(fcos) && nonzero(sun_rad)) {
+                    float area = PI_F * Sqr(P.sun_radius_m);
+                    float3 sn = normalize(target - sun_pos), wt = normalize(target - si.pos);
+                    float th = AbsDot(sn, -wt);
+                    float spdf = (1.0f / area) / (th / Sqr(dsun));
+                    float3 Ld = (fcos * sun_rad * 6.0e5f) / spdf;
+                    float3 c = Ld * beta / 0.5f;
+                    if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                        emit_shadow(F, si, target, c, item, here + 1, false);
+                }
+            } else if (eval && nonzero(fcos)) {
+                float p_l = prob * pdf;
+                float pb = bsdf.pdf(wo, wi);
+                float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
+                float3 Ld = (Lem * fcos * w_l) / p_l;
+                float3 c = Ld * beta / (1.0f - 0.5f);
+                if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                    emit_shadow(F, si, target, c, item, here + 2, true);
             }
         }
         F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
