@@ -248,7 +248,9 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
                 if (S.get1D() < 0.5f) {
                     // sampleLdSun
                     const float dsun = 149.597e9f;
-                    float3 sun_pos = P.sun_dir * dsun;
+                    // rounded product by product, as the forward's shading does
+                    const float3 sun_pos = make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
+                                                       __fmul_rn(P.sun_dir.z, dsun));
                     float3 off;
                     if (order == 0) {
                         float2 a = S.get2D(0);
@@ -259,7 +261,9 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
                         float2 a = S.get2D(1);
                         off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                     }
-                    float3 target = sun_pos + (off * P.sun_radius_m);
+                    const float3 target = make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
+                                                      __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
+                                                      __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
                     const float cf = fmaxf(0.0f, dot(P.sun_dir, (si.backface ? -1.0f : 1.0f) * si.ng));
                     FGrad fg;
                     float3 fcos = bsdf_f_grad(bsdf, wo, P.sun_dir, fg) * cf;
