@@ -50,6 +50,51 @@ def traversal_scene():
     return S.scene_traversal(20000)
 
 
+def tricky_scene():
+    """Random triangles plus exact duplicates of a third of them, triangles
+    with two equal vertices, collinear vertices and slivers, in one mesh
+    placed three times: instances 0 and 1 coincide, instance 2 is moved and
+    turned.  Equal hit distances are frequent, so the hit that wins depends
+    on the traversal order."""
+    rng = np.random.default_rng(5)
+    n = 3000
+    c = rng.uniform(-2.0, 2.0, (n, 1, 3))
+    p = (c + rng.normal(0.0, 0.3, (n, 3, 3))).astype(np.float32)
+    dup = p[rng.choice(n, n // 3, replace=False)]
+    deg = p[:200].copy()
+    deg[:100, 2] = deg[:100, 1]                                                    # two equal vertices
+    deg[100:, 2] = deg[100:, 0] + np.float32(2.0) * (deg[100:, 1] - deg[100:, 0])  # collinear
+    sliver = p[200:400].copy()
+    sliver[:, 2] = sliver[:, 0] + (sliver[:, 1] - sliver[:, 0]) * np.float32(0.5) + np.float32(1e-6)
+    pos = np.concatenate([p, dup, deg, sliver]).astype(np.float32)
+    pos = pos[rng.permutation(pos.shape[0])]
+    nrm = np.repeat(np.cross(pos[:, 1] - pos[:, 0], pos[:, 2] - pos[:, 0])[:, None, :], 3, 1)
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=-1, keepdims=True), 1e-12)
+    mesh = S.Mesh(pos, nrm.astype(np.float32), np.zeros((pos.shape[0], 3, 2), np.float32),
+                  np.zeros(pos.shape[0], np.int32))
+    base = S.scene_small(8, 8, 1, 2)
+    ident = np.eye(4, dtype=np.float32)
+    inst = [S.Instance(0, ident, 0), S.Instance(0, ident, 1),
+            S.Instance(0, (S.translate(0.5, 0.25, -0.5) @ S.rot_y(0.7)).astype(np.float32), 2)]
+    return S.Scene([mesh], inst, base.materials, base.camera, base.env, base.settings, base.exposure, 8, 8, 1)
+
+
+def tricky_rays(sc, m=60000):
+    """Rays aimed at points inside random triangles of the tricky scene's mesh
+    (a tenth of them on an edge), from points around the cloud."""
+    pos = sc.meshes[0].positions
+    rng = np.random.default_rng(9)
+    k = rng.integers(0, pos.shape[0], m)
+    b = rng.dirichlet((1.0, 1.0, 1.0), m).astype(np.float32)
+    b[: m // 10, 2] = 0.0
+    b[: m // 10] /= b[: m // 10].sum(1, keepdims=True)
+    target = np.einsum("nk,nkj->nj", b, pos[k]).astype(np.float32)
+    o = (target + rng.normal(0.0, 1.0, (m, 3)) * np.float32(4.0)).astype(np.float32)
+    d = target - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o, d.astype(np.float32)
+
+
 def main():
     if not O.available("ref"):
         O.build(ref=True)
@@ -132,6 +177,12 @@ def main():
     easu_hdr, sharp_hdr = O.fsr(hdr, 121, 67, "ref")
     out.update(up_bilinear=O.upscale(render, 160, 90, "ref"), up_easu=easu, up_fsr=sharp, up_hdr=hdr,
                up_hdr_easu=easu_hdr, up_hdr_fsr=sharp_hdr)
+    # closest hits where equal distances are common (duplicated and
+    # coincident triangles): which one wins is the reference's traversal order
+    r = O.Scene(tricky_scene(), "ref")
+    o, d = tricky_rays(tricky_scene(), 8192)
+    h = r.trace(o, d)
+    out.update(tricky_prim=h["prim"], tricky_t=h["t"], tricky_bvh=np.array(bvh_digest(r)))
     np.savez_compressed(os.path.join(OUT, "reference_host.npz"), **out)
     print("wrote", os.path.join(OUT, "reference_host.npz"))
 

@@ -12,7 +12,7 @@ import pytest
 from kittlespt_gb300 import scenes as S
 from oracle import oracle as O
 
-from tests.golden.make_golden import bvh_digest, full_scene, small_scene, traversal_scene
+from tests.golden.make_golden import bvh_digest, full_scene, small_scene, traversal_scene, tricky_rays, tricky_scene
 
 
 def bits(a):
@@ -90,6 +90,21 @@ def test_post_chain(golden):
     np.testing.assert_array_equal(bits(O.bloom(render, True, 0.65)), bits(golden["post_bloom_karis"]))
     img = O.post_image(render, golden["post_bloom"], 0.175, float(golden["post_expo_scalar"]))
     np.testing.assert_array_equal(bits(img), bits(golden["post_image"]))
+
+
+def test_ties_are_broken_in_the_reference_order(golden):
+    """Duplicated, coincident, degenerate and sliver triangles: trees, hit
+    distances and the winning triangle among equal distances are the
+    reference's; brute force (lowest index) disagrees on many of them."""
+    r = O.Scene(tricky_scene())
+    assert bvh_digest(r) == str(golden["tricky_bvh"])
+    o, d = tricky_rays(tricky_scene(), 8192)
+    h = r.trace(o, d)
+    np.testing.assert_array_equal(h["prim"], golden["tricky_prim"])
+    np.testing.assert_array_equal(bits(h["t"]), bits(golden["tricky_t"]))
+    brute = r.trace(o, d, brute=True)
+    np.testing.assert_array_equal(bits(brute["t"]), bits(golden["tricky_t"]))
+    assert (brute["prim"] != h["prim"]).mean() > 0.05
 
 
 def test_upscale_bilinear_and_fsr(golden):
