@@ -1085,7 +1085,8 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
         k_upscale<<<og, ob, 0, s>>>(c->render.p, c->W, c->H, c->output.p, c->OW, c->OH);
         c->launches += 1;
     } else if (c->settings.upscale == 2) {
-        k_easu<<<og, ob, 0, s>>>(c->render.p, c->W, c->H, c->easu.p, c->OW, c->OH);
+        k_easu<<<og, ob, 0, s>>>(c->render.p, c->W, c->H, c->easu.p, c->OW, c->OH,
+                                 easu_constants(c->W, c->H, c->OW, c->OH));
         k_rcas<<<og, ob, 0, s>>>(c->easu.p, c->OW, c->OH, c->output.p);
         c->launches += 2;
     }

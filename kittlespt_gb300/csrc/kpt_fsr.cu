@@ -79,6 +79,9 @@ __device__ __forceinline__ void easu_set(float2& dir, float& len, float w, float
     len += lenY * w;
 }
 
+// 0.4 (double) - 0.4f, rounded to float: the low part of 0.4
+constexpr float CL4 = -0x1.99999ap-28f;
+
 struct EasuKernel {
     float2 dir, len2;
     float lob, clp, ppx, ppy;
@@ -94,7 +97,16 @@ struct EasuKernel {
         vx *= len2.x;
         vy *= len2.y;
         const float d2 = fminf(vx * vx + vy * vy, clp);
-        float wB = (float)(0.4 * (double)d2 - 1.0);
+        // 0.4 * d2 - 1.0 in double rounded to float, from floats: the
+        // product with 0.4 split as 0.4f + CL4 (an exact product and its
+        // error by fma), then a two-sum with -1.  After the squaring and
+        // the fused step below it gives the double form's wB for every float
+        // d2 in [0, 4.8] (d2 <= clp <= 1 / 0.21), checked exhaustively; the
+        // one input where the two differ before squaring is 2.5 (0 against
+        // -2^-52).
+        const float ph = 0.4f * d2, pl = fmaf(0.4f, d2, -ph), tt = fmaf(CL4, d2, pl);
+        const float sm = ph + -1.0f, bb = sm - ph, er = (ph - (sm - bb)) + (-1.0f - bb);
+        float wB = sm + (er + tt);
         // (double)(lob * d2) - 1.0 rounded to float: p = lob * d2 lies in
         // [0, 2] (d2 <= clp = 1 / lob); for p >= 2^-29 the difference is
         // exact in double, so one float subtraction rounds it the same, and
@@ -116,19 +128,39 @@ struct EasuKernel {
 
 }  // namespace
 
-// EASU (FsrEasuCon + FsrEasuF, upscale.cuh:18-254) of the render [sh][sw]
-// into dst [dh][dw], one thread per output pixel
-__global__ void k_easu(const float4* src, int sw, int sh, float4* dst, int dw, int dh) {
+// FsrEasuCon (upscale.cuh:18-62) with the render size as viewport and
+// input size, on the host (IEEE float divisions and the reference's double
+// expressions, the same on every host this builds for)
+EasuCon easu_constants(int sw, int sh, int dw, int dh) {
+    const float inw = (float)sw, inh = (float)sh, ow = (float)dw, oh = (float)dh;
+    EasuCon c;
+    c.c0x = inw / ow;
+    c.c0y = inh / oh;
+    c.c0z = (float)(0.5 * (double)inw / (double)ow - 0.5);
+    c.c0w = (float)(0.5 * (double)inh / (double)oh - 0.5);
+    c.c1x = 1.0f / inw;
+    c.c1y = 1.0f / inh;
+    c.c1z = 1.0f / inw;
+    c.c1w = -1.0f / inh;
+    c.c2x = -1.0f / inw;
+    c.c2y = 2.0f / inh;
+    c.c2z = 1.0f / inw;
+    c.c2w = 2.0f / inh;
+    c.c3x = 0.0f / inw;
+    c.c3y = 4.0f / inh;
+    return c;
+}
+
+// EASU (FsrEasuF, upscale.cuh:133-254) of the render [sh][sw] into dst
+// [dh][dw], one thread per output pixel
+__global__ void k_easu(const float4* src, int sw, int sh, float4* dst, int dw, int dh, EasuCon con) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dw || y >= dh) return;
-    // FsrEasuCon with the render size as viewport and input size
-    const float inw = (float)sw, inh = (float)sh, ow = (float)dw, oh = (float)dh;
-    const float c0x = inw / ow, c0y = inh / oh;
-    const float c0z = (float)(0.5 * (double)inw / (double)ow - 0.5);
-    const float c0w = (float)(0.5 * (double)inh / (double)oh - 0.5);
-    const float c1x = 1.0f / inw, c1y = 1.0f / inh, c1z = 1.0f / inw, c1w = -1.0f / inh;
-    const float c2x = -1.0f / inw, c2y = 2.0f / inh, c2z = 1.0f / inw, c2w = 2.0f / inh;
-    const float c3x = 0.0f / inw, c3y = 4.0f / inh;
+    const float inw = (float)sw, inh = (float)sh;
+    const float c0x = con.c0x, c0y = con.c0y, c0z = con.c0z, c0w = con.c0w;
+    const float c1x = con.c1x, c1y = con.c1y, c1z = con.c1z, c1w = con.c1w;
+    const float c2x = con.c2x, c2y = con.c2y, c2z = con.c2z, c2w = con.c2w;
+    const float c3x = con.c3x, c3y = con.c3y;
     const float offx = -0.5f * c1x, offy = 0.5f * c1x, offz = -0.5f * c1y, offw = 0.5f * c1y;
 
     float ppx = (float)x * c0x + c0z, ppy = (float)y * c0y + c0w;
@@ -175,9 +207,12 @@ __global__ void k_easu(const float4* src, int sw, int sh, float4* dst, int dw, i
     const float stretch = (dir.x * dir.x + dir.y * dir.y) / fmaxf(fabsf(dir.x), fabsf(dir.y));
     EasuKernel K;
     K.dir = dir;
-    K.len2 = make_float2((float)(1.0 + ((double)stretch - 1.0) * (double)len), (float)(1.0 - 0.5 * (double)len));
+    // 1. - .5 * len and 1. / lob in double give the float forms' results for
+    // every float len in [0, 1] and lob in [0.2, 0.51] (checked
+    // exhaustively); .29 * len and the stretch term stay in double
+    K.len2 = make_float2((float)(1.0 + ((double)stretch - 1.0) * (double)len), 1.0f - 0.5f * len);
     K.lob = (float)(0.5 - 0.29 * (double)len);
-    K.clp = (float)(1.0 / (double)K.lob);
+    K.clp = 1.0f / K.lob;
     K.ppx = ppx;
     K.ppy = ppy;
     K.aC = make_float3(0.0f, 0.0f, 0.0f);

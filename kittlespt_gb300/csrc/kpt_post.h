@@ -32,8 +32,13 @@ __global__ void k_effects(int W, int H, const float4* src, float4* dst);
 // the output pixel's position
 __global__ void k_upscale(const float4* src, int sw, int sh, float4* dst, int dw, int dh);
 // the FSR 1.0 path (kpt_fsr.cu): EASU of the render to the output size, then
-// RCAS of that image
-__global__ void k_easu(const float4* src, int sw, int sh, float4* dst, int dw, int dh);
+// RCAS of that image.  EasuCon holds FsrEasuCon's constants for one pair of
+// sizes (upscale.cuh:18-62), computed on the host by easu_constants.
+struct EasuCon {
+    float c0x, c0y, c0z, c0w, c1x, c1y, c1z, c1w, c2x, c2y, c2z, c2w, c3x, c3y;
+};
+EasuCon easu_constants(int sw, int sh, int dw, int dh);
+__global__ void k_easu(const float4* src, int sw, int sh, float4* dst, int dw, int dh, EasuCon con);
 __global__ void k_rcas(const float4* src, int w, int h, float4* dst);
 
 }  // namespace kpt
