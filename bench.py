@@ -47,6 +47,19 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(x, world, device=None):
+    """The largest x over the ranks of a replicas run (all-reduce MAX over the
+    default process group); x itself with one rank.  Timings are reduced this
+    way, so a run's time is its slowest replica's."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -228,10 +241,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
     barrier()
     ms = start.elapsed_time(stop)
-    t = torch.tensor([ms], device=local)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, world, device=local)
     st1 = r.stats()
     launches = r.launch_count() - l0
     print(f"[bench] {args.steps} frames in {ms_max:.2f} ms ({ms_max / args.steps:.2f} ms/frame)", file=sys.stderr)
@@ -283,8 +293,8 @@ def run_gpu(args):
         K.check(r._L.kpt_set_camera_inverse(r.ctx, K.fptr(ip), K.fptr(iv)))
         r.execute_rendering(16.0, SPP)
         K.check(r._L.kpt_read_image(r.ctx, img_ptr))
-    e2e_s = (time.perf_counter() - t0) / n_e2e
-    e2e = samples_step / e2e_s / 1e6
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, world, device=local)
+    e2e = samples_step * world / e2e_s / 1e6
     overflow = st1.overflows - st0.overflows
     r.shutdown()
 
