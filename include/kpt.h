@@ -223,6 +223,14 @@ kpt_status kpt_read_accumulation(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_albedo(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_histogram(kpt_context* ctx, uint64_t* bins256);
 kpt_status kpt_get_stats(kpt_context* ctx, kpt_stats* st);
+/* Diagnostics, no reference counterpart: for each level 0 .. min(max_levels,
+ * max_depth + 1) - 1 of the last wave of the last frame rendered on this
+ * context, counts[3 l] = paths shaded at level l (level >= 1: extension rays
+ * traced into it), counts[3 l + 1] = sun shadow rays and counts[3 l + 2] =
+ * area-light shadow rays it sent; *levels = the number of levels written.  A
+ * frame has one wave unless width x height x spp exceeds the wave capacity
+ * (kpt_tuning.wave_cap).  After kpt_submit_batch, call kpt_wait_batch first. */
+kpt_status kpt_get_level_counts(kpt_context* ctx, int max_levels, int32_t* counts, int32_t* levels);
 
 /* Per-sample radiance of the plain method (the megakernel body,
  * shaders/kernels.cu:385-413), for parity checks: samples sample0 ..

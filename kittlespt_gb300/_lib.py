@@ -119,6 +119,7 @@ SIGNATURES = {
     "kpt_read_albedo": (_S, [_P, _F]),
     "kpt_read_histogram": (_S, [_P, C.POINTER(C.c_uint64)]),
     "kpt_get_stats": (_S, [_P, C.POINTER(Stats)]),
+    "kpt_get_level_counts": (_S, [_P, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "kpt_render_samples_device": (_S, [_P, C.c_int, C.c_int, _P, _P, _P]),
     "kpt_trace_device": (_S, [_P, C.c_int, _P, _P, C.c_float, C.c_float, _P, _P, _P, _P]),
     "kpt_occluded_device": (_S, [_P, C.c_int, _P, _P, C.c_float, _P, _P]),

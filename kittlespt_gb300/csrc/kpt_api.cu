@@ -122,6 +122,7 @@ struct kpt_context {
     int W = 0, H = 0, OW = 0, OH = 0;
     DBuf<float4> output;        // the render upscaled to the output resolution (upscale)
     int frame_index = 0;
+    int levels_depth = -1;      // max depth of the last wave whose level counts are kept (-1: none)
     DBuf<float4> acc, albedo, render, image;
     // temporal accumulation: visible surface, distances of the previous frame
     // and this one, history images (color, frames), per-instance matrices
@@ -938,6 +939,7 @@ static void stage_mark(kpt_context* c, int stage) {
 // The path stage: camera rays and their sky, then the wave(s) of paths level
 // by level, the queued sky and the ordered accumulation of every sample.
 static void enqueue_paths(kpt_context* c, const FrameParams& F) {
+    c->levels_depth = F.max_depth;
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
     const int D = F.max_depth;
@@ -1317,6 +1319,20 @@ kpt_status kpt_read_render(kpt_context* c, float* rgba) { return read_buf(c, c ?
 kpt_status kpt_read_accumulation(kpt_context* c, float* rgba) { return read_buf(c, c ? c->acc.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
 kpt_status kpt_read_albedo(kpt_context* c, float* rgba) { return read_buf(c, c ? c->albedo.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
 kpt_status kpt_read_histogram(kpt_context* c, uint64_t* bins) { return read_buf(c, c ? c->hist.p : nullptr, bins, 256 * sizeof(uint64_t)); }
+
+kpt_status kpt_get_level_counts(kpt_context* c, int max_levels, int32_t* counts, int32_t* levels) {
+    if (!c || !counts || !levels || max_levels < 1) return fail(KPT_ERR_INVALID, "kpt_get_level_counts: invalid argument");
+    const int D = c->levels_depth;
+    if (D < 0 || !c->level_counts.p) return fail(KPT_ERR_STATE, "kpt_get_level_counts: no frame rendered");
+    std::vector<int> h((size_t)LEVEL_WORDS * (D + 2));
+    KPT_CUDA(cudaMemcpyAsync(h.data(), c->level_counts.p, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    const int n = std::min(max_levels, D + 1);
+    for (int l = 0; l < n; ++l)
+        for (int k = 0; k < 3; ++k) counts[3 * l + k] = h[(size_t)LEVEL_WORDS * l + k];
+    *levels = n;
+    return KPT_OK;
+}
 
 kpt_status kpt_get_stats(kpt_context* c, kpt_stats* st) {
     if (!c || !st) return fail(KPT_ERR_INVALID, "null argument");

@@ -158,6 +158,9 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
     PathRec* out = F.unsorted ? F.unsorted : F.paths[(level + 1) & 1];
     int* here = F.level_counts + LEVEL_WORDS * level;
     int* next = F.level_counts + LEVEL_WORDS * (level + 1);
+    // the wave's paths entering level 0 (levels >= 1 count theirs as they
+    // are appended); read back by kpt_get_level_counts
+    if (first && blockIdx.x == 0 && threadIdx.x == 0) here[0] = n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float3 o, d, beta, prev, L;
         float p_b;

@@ -286,6 +286,14 @@ class Renderer:
         K.check(self._L.kpt_get_stats(self._ctx, C.byref(s)))
         return s
 
+    def level_counts(self, max_levels: int = 65) -> np.ndarray:
+        """[levels, 3]: paths shaded, sun shadow rays and area-light shadow
+        rays per level of the last wave of the last frame (kpt_get_level_counts)."""
+        buf = (C.c_int32 * (3 * max_levels))()
+        n = C.c_int32()
+        K.check(self._L.kpt_get_level_counts(self._ctx, max_levels, buf, C.byref(n)))
+        return np.array(buf[:3 * n.value], np.int64).reshape(n.value, 3)
+
     def launch_count(self) -> int:
         n = C.c_uint64()
         K.check(self._L.kpt_launch_count(self._ctx, C.byref(n)))

@@ -54,4 +54,5 @@ def test_errors_without_context(lib):
     assert lib.kpt_resize(None, 4, 4) == -1
     assert lib.kpt_last_error()
     assert lib.kpt_render_frame(None, 1, 16.0) == -1
+    assert lib.kpt_get_level_counts(None, 4, None, None) == -1
     assert lib.kpt_destroy(None) == 0

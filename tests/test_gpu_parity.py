@@ -195,6 +195,32 @@ def test_accumulation_is_sample_order_sum():
     np.testing.assert_array_equal(bits(acc), bits(s))
 
 
+def test_level_counts_agree_with_the_ray_counts():
+    """kpt_get_level_counts: level 0 shades every camera-ray hit of every
+    sample, each level's paths and shadow rays add up to the frame's ray
+    counters, and fewer paths continue than enter."""
+    from kittlespt_gb300 import _lib as K
+    sc = S.scene_full(64, 36, 3, 6, n_variants=2, subdiv=3, grid=3, n_lights=4)
+    r = make_renderer(sc)
+    try:
+        with pytest.raises(K.KptError):
+            r.level_counts()        # no frame yet
+        st0 = r.stats()
+        r.execute_rendering(16.0, 3)
+        r.synchronize()
+        st1 = r.stats()
+        lc = r.level_counts()
+        hits = int((render_samples(r, sc, 1)[1][..., 0] >= 0).sum())
+    finally:
+        r.shutdown()
+    assert lc.shape == (7, 3)
+    assert lc[0, 0] == hits * 3
+    assert (np.diff(lc[:, 0]) <= 0).all() and lc[1, 0] > 0
+    assert (lc[:, 1] + lc[:, 2] <= lc[:, 0]).all()
+    assert lc[1:, 0].sum() == st1.path_rays - st0.path_rays
+    assert lc[:, 1:].sum() == st1.shadow_rays - st0.shadow_rays
+
+
 def test_api_errors_and_state():
     sc = S.scene_small(16, 16, 1, 2)
     r = make_renderer(sc)
