@@ -106,15 +106,19 @@ __device__ __forceinline__ bool sky_in_band(const SkyParams& P, float3 d) {
     return fabsf(d.y) < 0.05f || dot(d, P.sun_dir) > 0.995f;
 }
 
-// Queues an escape's double-precision Jacobian with its gradient weight;
-// false when the queue is full (the caller evaluates it at once).
-__device__ __forceinline__ bool sky_defer(const AdjParams& A, float3 d, float3 w) {
-    if (!A.skyq) return false;
-    const int q = atomicAdd(A.skyq_count, 1);
-    if (q >= A.skyq_cap) return false;
-    A.skyq[2 * (size_t)q] = make_float4(d.x, d.y, d.z, 0.0f);
-    A.skyq[2 * (size_t)q + 1] = make_float4(w.x, w.y, w.z, 0.0f);
+// Queues an escape's sky Jacobian (direction d) with its gradient weight w
+// in queue q (count, capacity cap); false when there is no queue or it is
+// full (the caller evaluates the Jacobian at once).
+__device__ __forceinline__ bool sky_push(float4* q, int* count, int cap, float3 d, float3 w) {
+    if (!q) return false;
+    const int i = atomicAdd(count, 1);
+    if (i >= cap) return false;
+    q[2 * (size_t)i] = make_float4(d.x, d.y, d.z, 0.0f);
+    q[2 * (size_t)i + 1] = make_float4(w.x, w.y, w.z, 0.0f);
     return true;
+}
+__device__ __forceinline__ bool sky_defer(const AdjParams& A, float3 d, float3 w) {
+    return sky_push(A.skyq, A.skyq_count, A.skyq_cap, d, w);
 }
 
 // Pixels whose camera ray misses: every sample is sky(d) * LeSun(d).
@@ -186,22 +190,16 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
         int nv = 0;
         bool escaped = false;
         float3 s_end = make_float3(0.0f, 0.0f, 0.0f), b_end = s_end, d_end = s_end;
-        float3 J_end[SKY_PARAMS];
-        bool d_band = false;
         for (int level = 0;; ++level) {
             if (level > 0) {
                 Hit hh = trace_closest(s, make_xray(o, d), 0.0f, __int_as_float(0x7f800000), st, stack);
                 h.t = hh.t; h.u = hh.u; h.v = hh.v; h.inst = hh.inst; h.tri = hh.tri;
             }
             if (h.inst < 0) {
+                // the sky the path escapes to, by the forward's march; its
+                // Jacobian is needed only in the reverse sweep
                 escaped = true;
-                s_end = nishita_grad(P, obs, d, J_end);
-                // near the sun (Mie forward peak) and the horizon the
-                // single-precision march's derivatives are ill-conditioned:
-                // there the Jacobian is evaluated in double, deferred to
-                // k_adjoint_sky_d (the FP64 march then runs on full warps)
-                d_band = sky_in_band(P, d);
-                if (d_band && !A.skyq) nishita_jacobian_d(P, obs, d, J_end);
+                s_end = nishita(P, obs, d);
                 b_end = beta;
                 d_end = d;
                 break;
@@ -427,14 +425,22 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
         float3 R = escaped ? s_end : make_float3(0.0f, 0.0f, 0.0f);
         if (nonzero(g)) {
             if (escaped) {
+                // The sky Jacobian at the escape: near the sun (Mie forward
+                // peak) and the horizon the single-precision march's
+                // derivatives are ill-conditioned, so there it is evaluated
+                // in double.  Both kinds are queued for batched kernels
+                // (k_adjoint_sky_d / _f), which march on full warps instead
+                // of the few lanes of a warp that escape together here.
                 const float3 gb = wmul(g, b_end);
-                bool done = false;
-                if (d_band && A.skyq) {
-                    done = sky_defer(A, d_end, gb);
-                    if (!done) nishita_jacobian_d(P, obs, d_end, J_end);
-                }
-                if (!done)
+                const bool band = sky_in_band(P, d_end);
+                const bool done = band ? sky_defer(A, d_end, gb)
+                                       : sky_push(A.skyqf, A.skyqf_count, A.skyqf_cap, d_end, gb);
+                if (!done) {
+                    float3 J_end[SKY_PARAMS];
+                    if (band) nishita_jacobian_d(P, obs, d_end, J_end);
+                    else nishita_grad(P, obs, d_end, J_end);
                     for (int i = 0; i < SKY_PARAMS; ++i) gsky[i] += wdot(gb, J_end[i]);
+                }
             }
             for (int k = nv - 1; k >= 0; --k) {
                 const float3 gb = wmul(g, vb[k]);
@@ -486,20 +492,24 @@ __device__ __forceinline__ void adjoint_block(const FrameParams& F, const AdjPar
 
 __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint(FrameParams F, AdjParams A) { adjoint_block<false>(F, A); }
 
-// The deferred double-precision sky Jacobians: weight . J(d) per queued
-// escape, summed into the sky parameters' gradients.
-__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_sky_d(FrameParams F, AdjParams A) {
+// The deferred sky Jacobians: weight . J(d) per queued escape, summed into
+// the sky parameters' gradients; in double (DBL, the band near the horizon
+// and the sun) or single precision.
+template <bool DBL>
+__device__ __forceinline__ void sky_jacobians(const FrameParams& F, const float4* q, const int* count, int cap,
+                                              double* grad) {
     __shared__ double sg[SKY_PARAMS];
     if (threadIdx.x < SKY_PARAMS) sg[threadIdx.x] = 0.0;
     __syncthreads();
     const SkyParams& P = F.sky;
     const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
-    const int n = min(*A.skyq_count, A.skyq_cap);
+    const int n = min(*count, cap);
     double gsky[SKY_PARAMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 a = A.skyq[2 * (size_t)i], b = A.skyq[2 * (size_t)i + 1];
+        const float4 a = q[2 * (size_t)i], b = q[2 * (size_t)i + 1];
         float3 J[SKY_PARAMS];
-        nishita_jacobian_d(P, obs, make_float3(a.x, a.y, a.z), J);
+        if (DBL) nishita_jacobian_d(P, obs, make_float3(a.x, a.y, a.z), J);
+        else nishita_grad(P, obs, make_float3(a.x, a.y, a.z), J);
         const float3 w = make_float3(b.x, b.y, b.z);
         for (int k = 0; k < SKY_PARAMS; ++k) gsky[k] += wdot(w, J[k]);
     }
@@ -509,7 +519,14 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_sky_d(FrameParams F, Adj
         if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sg + k, v);
     }
     __syncthreads();
-    if (threadIdx.x < SKY_PARAMS && sg[threadIdx.x] != 0.0) atomicAdd(A.grad + 4 * A.nmat + threadIdx.x, sg[threadIdx.x]);
+    if (threadIdx.x < SKY_PARAMS && sg[threadIdx.x] != 0.0) atomicAdd(grad + threadIdx.x, sg[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_sky_d(FrameParams F, AdjParams A) {
+    sky_jacobians<true>(F, A.skyq, A.skyq_count, A.skyq_cap, A.grad + 4 * A.nmat);
+}
+__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_sky_f(FrameParams F, AdjParams A) {
+    sky_jacobians<false>(F, A.skyqf, A.skyqf_count, A.skyqf_cap, A.grad + 4 * A.nmat);
 }
 __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_rec(FrameParams F, AdjParams A) { adjoint_block<true>(F, A); }
 

@@ -155,6 +155,8 @@ struct kpt_context {
     DBuf<int> rec_count;
     DBuf<float4> adj_skyq;      // deferred double-precision sky Jacobians: (direction, weight)
     DBuf<int> adj_skyq_count;
+    DBuf<float4> adj_skyqf;     // deferred single-precision sky Jacobians
+    DBuf<int> adj_skyqf_count;
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2], unsorted;
     DBuf<int> octants;
@@ -290,7 +292,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->unsorted.release(); c->octants.release();
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
-    c->adj_skyq.release(); c->adj_skyq_count.release();
+    c->adj_skyq.release(); c->adj_skyq_count.release(); c->adj_skyqf.release(); c->adj_skyqf_count.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
     if (c->ev_sky) cudaEventDestroy(c->ev_sky);
@@ -1592,6 +1594,8 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     if (!rec) {
         KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
         KPT_CUDA(c->adj_skyq_count.ensure(1));
+        KPT_CUDA(c->adj_skyqf.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
+        KPT_CUDA(c->adj_skyqf_count.ensure(1));
     }
     FrameParams F = frame_params(c, sample0, nsamples);
     AdjParams A{};
@@ -1607,6 +1611,9 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         A.skyq = c->adj_skyq.p;
         A.skyq_count = c->adj_skyq_count.p;
         A.skyq_cap = (int)(c->adj_skyq.n / 2);
+        A.skyqf = c->adj_skyqf.p;
+        A.skyqf_count = c->adj_skyqf_count.p;
+        A.skyqf_cap = (int)(c->adj_skyqf.n / 2);
     }
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
@@ -1614,6 +1621,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     if (image) KPT_CUDA(cudaMemsetAsync(image, 0, sizeof(float4) * (size_t)np, s));
     KPT_CUDA(cudaMemsetAsync(c->rec_count.p, 0, sizeof(int), s));
     if (A.skyq) KPT_CUDA(cudaMemsetAsync(A.skyq_count, 0, sizeof(int), s));
+    if (A.skyqf) KPT_CUDA(cudaMemsetAsync(A.skyqf_count, 0, sizeof(int), s));
     KPT_CUDA(cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s));
     const void* kern = rec ? (const void*)k_adjoint_rec : (const void*)k_adjoint;
     for (const void* k : {kern, (const void*)k_adjoint_miss})
@@ -1630,7 +1638,8 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     c->launches += 5;
     if (A.skyq) {
         k_adjoint_sky_d<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
-        c->launches += 1;
+        k_adjoint_sky_f<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
+        c->launches += 2;
     }
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;

@@ -122,6 +122,11 @@ struct AdjParams {
     float4* skyq;
     int* skyq_count;
     int skyq_cap;
+    // the other escapes' single-precision Jacobians, the same way, for
+    // k_adjoint_sky_f
+    float4* skyqf;
+    int* skyqf_count;
+    int skyqf_cap;
 };
 
 // Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
@@ -160,6 +165,7 @@ __global__ void k_adjoint_miss(FrameParams F, AdjParams A);
 __global__ void k_adjoint(FrameParams F, AdjParams A);
 __global__ void k_adjoint_rec(FrameParams F, AdjParams A);   // also writes the frozen-path records
 __global__ void k_adjoint_sky_d(FrameParams F, AdjParams A);
+__global__ void k_adjoint_sky_f(FrameParams F, AdjParams A);
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
 // Temporal accumulation (kernels.cu:164-327): per instance, the matrices of
 // computeVelocity and testReprojection for one frame, rows of column-major
