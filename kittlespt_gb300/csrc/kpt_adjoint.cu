@@ -3,19 +3,22 @@
 //
 // The differentiated image is, per pixel, the mean over samples of the
 // clamped path radiance (what the accumulation adds per frame, before the
-// post chain).  For dLoss/dimage given per pixel, k_adjoint replays every
+// post chain).  For dLoss/dimage given per pixel, the adjoint replays every
 // sample's path with the forward's random numbers -- the same camera ray,
-// traversal, light sample and BSDF sample as k_shade, in one thread -- and
-// keeps, per vertex, the throughput beta_k, the radiance the vertex adds c_k,
-// the weight to the next vertex w_k and their derivatives.  With
+// traversal, light sample and BSDF sample as k_shade -- and keeps, per
+// vertex, the throughput beta_k, the radiance the vertex adds c_k, the weight
+// to the next vertex w_k and their derivatives.  With
 // R_k = c_k + w_k R_{k+1} (R after the last vertex: the sky if the path
 // escaped), the gradient is sum_k beta_k (dc_k + dw_k R_{k+1}) plus the sky
 // terms.  Sampled directions, lobe / light / sun choices, Russian roulette,
 // pdfs and MIS weights are held fixed (detached sampling), so the result is
 // the derivative of the estimator with respect to the BSDF values (per
 // material albedo and roughness) and the sky radiance (Rayleigh r, g, b, Mie,
-// both scale heights).  Nothing is stored between passes: each sample is
-// recomputed from its RNG stream.
+// both scale heights).  Nothing is stored between the forward and the
+// adjoint: each sample is recomputed from its RNG stream.  The replay runs as
+// a wavefront (k_adj_shade / k_adj_shadow per level with the forward's
+// k_extend, then k_adj_sweep); adjoint_items replays one sample per thread
+// and writes the frozen-path records (kpt_adjoint_records_device).
 #include "kpt_adjoint.cuh"
 #include "kpt_pathfn.cuh"
 
@@ -152,8 +155,8 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjP
     grad_end(sg, ng, A.grad);
 }
 
-// Replay of every (sample, hit pixel) item; REC also writes each vertex's
-// frozen quantities to A.rec.
+// Replay of every (sample, hit pixel) item, one per thread; REC also writes
+// each vertex's frozen quantities to A.rec (the records path).
 template <bool REC>
 __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjParams& A, GradAcc& acc, int* stack,
                                               double* gsky) {
@@ -490,7 +493,6 @@ __device__ __forceinline__ void adjoint_block(const FrameParams& F, const AdjPar
     grad_end(sg, ng, A.grad);
 }
 
-__global__ void __launch_bounds__(PATH_BLOCK) k_adjoint(FrameParams F, AdjParams A) { adjoint_block<false>(F, A); }
 
 // The deferred sky Jacobians: weight . J(d) per queued escape, summed into
 // the sky parameters' gradients; in double (DBL, the band near the horizon
@@ -529,5 +531,407 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_sky_f(FrameParams F, Adj
     sky_jacobians<false>(F, A.skyqf, A.skyqf_count, A.skyqf_cap, A.grad + 4 * A.nmat);
 }
 __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_rec(FrameParams F, AdjParams A) { adjoint_block<true>(F, A); }
+
+// ---------------------------------------------------------------------------
+// The wavefront replay (kpt_adjoint_device): the estimator of adjoint_items
+// with its rays traced by the forward's queue kernels.  Per level,
+// k_adj_shade runs the replay's vertex for every path of the wave (emission
+// with its MIS weight, the light sample and its derivatives, the BSDF sample
+// and its derivatives, Russian roulette) and stores the vertex record; the
+// light sample's shadow ray goes to k_adj_shadow, which marks the sample
+// visible; k_extend traces the continuations.  After the last level
+// k_adj_sweep sums each sample's radiance and runs its reverse sweep.  The
+// arithmetic of every vertex is adjoint_items' (the records megakernel, kept
+// for the frozen-path records).
+
+__device__ __forceinline__ float3 xyz3(float4 v) { return make_float3(v.x, v.y, v.z); }
+
+__global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjParams A, int level, long long wave0) {
+    constexpr int MV = ADJ_MAX_VERTICES;
+    const SceneView& s = F.scene;
+    const SkyParams& P = F.sky;
+    const int order = F.rng_order;
+    const int nl = s.nlights;
+    const bool first = level == 0;
+    const float3 sun_rad = *F.sun_radiance;
+    const int cap = F.cap;
+    int n;
+    if (first) {
+        const long long left = (long long)F.counts[0] * F.nsamples - wave0;
+        n = (int)(left < 0 ? 0 : (left < cap ? left : cap));
+    } else {
+        n = F.level_counts[LEVEL_WORDS * level];
+    }
+    const PathRec* in = F.paths[level & 1];
+    PathRec* out = F.paths[(level + 1) & 1];
+    int* here = F.level_counts + LEVEL_WORDS * level;
+    int* next = F.level_counts + LEVEL_WORDS * (level + 1);
+    float4* vr = A.vr + (size_t)level * cap;
+    const size_t vs = A.vstride;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float3 o, d, beta, prev;
+        float p_b;
+        uint32_t seed;
+        int loc;   // the path's slot in the wave
+        PrimaryRec h;
+        if (first) {
+            const int nhit = F.counts[0];
+            const long long item = wave0 + i;
+            const int k = (int)(item / nhit);
+            const int p = F.hit_list[item - (long long)k * nhit];
+            const int x = p % F.W, y = p / F.W;
+            Sampler S0;
+            S0.init(x, y, F.W, F.sample0 + k);
+            S0.get1D();   // BoxFilter::sample, result discarded (kernels.cu:397-402)
+            S0.get1D();
+            const XRay cam = camera_ray(F, x, y);
+            o = cam.o;
+            d = cam.d;
+            beta = make_float3(1.0f, 1.0f, 1.0f);
+            prev = make_float3(0.0f, 0.0f, 0.0f);
+            p_b = 1.0f;
+            seed = S0.seed;
+            h = F.primary[p];
+            loc = i;
+        } else {
+            const PathRec pr = in[i];
+            o = make_float3(pr.o_pb.x, pr.o_pb.y, pr.o_pb.z);
+            p_b = pr.o_pb.w;
+            d = make_float3(pr.d_seed.x, pr.d_seed.y, pr.d_seed.z);
+            seed = __float_as_uint(pr.d_seed.w);
+            beta = make_float3(pr.beta_item.x, pr.beta_item.y, pr.beta_item.z);
+            loc = __float_as_int(pr.beta_item.w);
+            prev = make_float3(pr.prev.x, pr.prev.y, pr.prev.z);
+            h = F.hits[i];
+        }
+        auto end_path = [&](bool escaped, int nv, float3 de, float3 be) {
+            A.vend[2 * (size_t)loc] = make_float4(de.x, de.y, de.z, __int_as_float(nv));
+            A.vend[2 * (size_t)loc + 1] = make_float4(be.x, be.y, be.z, __int_as_float(escaped ? 1 : 0));
+        };
+        if (h.inst < 0) {   // the path leaves the scene: the sweep evaluates the sky
+            end_path(true, level, d, beta);
+            continue;
+        }
+        Sampler S;
+        S.seed = seed + (uint32_t)level;
+        Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
+        float3 c = make_float3(0.0f, 0.0f, 0.0f);
+        float3 Le = make_float3(0.0f, 0.0f, 0.0f);
+        if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
+        if (nonzero(Le)) {
+            float w_l = 1.0f;
+            if (si.light >= 0 && !first) {
+                const LightRec& lt = s.lights[si.light];
+                float pmf = 1.0f / (float)nl;
+                float dist = length(si.pos - prev);
+                float cosl = AbsDot(normalize(si.pos - prev), si.ng);
+                float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
+                w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
+            }
+            c = Le * w_l;
+        }
+        Bsdf bsdf = bsdf_at(s, si);
+        const MatFactors mf = mat_factors(s, si);
+        const float3 dalb = first ? make_float3(0.0f, 0.0f, 0.0f) : mf.alb_tex;
+        if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);
+        float dal = 2.0f * mf.rough_eff * mf.rough_tex;
+        if (!first && bsdf.alpha < 0.3f) {
+            float a2 = 2.0f * bsdf.alpha;
+            dal *= (a2 > 0.1f && a2 < 0.3f) ? 2.0f : 0.0f;
+            bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
+        }
+        const float3 wo = -d;
+        const float3 zero = make_float3(0.0f, 0.0f, 0.0f);
+        float3 fcos = zero, kk = zero, dat = zero, dalt = zero;
+        int nee = 0;   // 1: sun, 2: area light, with a shadow ray sent
+        if (!(bsdf.alpha < 0.001f)) {
+            // the light sample: each branch sets up its direction, the BSDF
+            // and its derivatives are evaluated once for the warp
+            const bool sun = S.get1D() < 0.5f;
+            const float dsun = 149.597e9f;
+            const float3 sun_pos = make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
+                                               __fmul_rn(P.sun_dir.z, dsun));
+            float3 wi = P.sun_dir, target = sun_pos, Lem = zero;
+            float pdf = 0.0f, prob = 0.0f;
+            bool eval = false;
+            if (sun) {
+                float3 off;
+                if (order == 0) {
+                    float2 a = S.get2D(0);
+                    float b = S.get1D();
+                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                } else {
+                    float b = S.get1D();
+                    float2 a = S.get2D(1);
+                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                }
+                target = make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
+                                     __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
+                                     __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
+                eval = true;
+            } else {
+                float X = S.get1D();
+                if (nl >= 1) {
+                    int li = min((int)(X * (float)nl), nl - 1);
+                    const LightRec& lt = s.lights[li];
+                    prob = 1.0f / (float)nl;
+                    float2 uu = S.get2D(order);
+                    const InstRec& lir = s.inst[lt.inst];
+                    float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
+                    float bx, by;
+                    if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
+                    else { by = uu.y / 2.0f; bx = uu.x - by; }
+                    float bz = 1.0f - bx - by;
+                    float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
+                                             bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
+                    float3 lp = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
+                    lp = row3(model, lp, 1.0f);
+                    float3 gn = row3(model, lt.gn, 0.0f);
+                    pdf = 1.0f / lt.tri_area;
+                    pdf *= Sqr(length(lp - si.pos));
+                    pdf /= AbsDot(normalize(lp - si.pos), gn);
+                    wi = normalize(lp - si.pos);
+                    Lem = emission_of(s, lt.material, luv);
+                    target = lp;
+                    eval = !(pdf <= 0.0f || !nonzero(Lem));
+                }
+            }
+            float cf = 0.0f;
+            FGrad fg;
+            float3 fc = zero;
+            if (eval) {
+                cf = fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
+                fc = bsdf_f_grad(bsdf, wo, wi, fg) * cf;
+            }
+            if (eval && nonzero(fc) && (!sun || nonzero(sun_rad))) {
+                if (sun) {
+                    float area = PI_F * Sqr(P.sun_radius_m);
+                    float3 sn = normalize(target - sun_pos), wt = normalize(target - si.pos);
+                    float th = AbsDot(sn, -wt);
+                    float spdf = (1.0f / area) / (th / Sqr(dsun));
+                    const float k = 6.0e5f / spdf / 0.5f;
+                    kk = make_float3(k, k, k);
+                    nee = 1;
+                } else {
+                    float p_l = prob * pdf;
+                    float pb = bsdf.pdf(wo, wi);
+                    float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
+                    kk = Lem * (w_l / p_l / (1.0f - 0.5f));
+                    nee = 2;
+                }
+                fcos = fc;
+                dat = fg.da * dalb * cf;
+                dalt = fg.dal * dal * cf;
+                // the shadow ray of Integrator::unoccluded (integrator.cuh:124-131)
+                const float3 so = si.backface ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+                const float3 sd = normalize(target - so);
+                const float tmax = length(target - so) - 0.11f;
+                // sun rays from the front of the buffer, light rays from the
+                // back (one append per kind: the group shares one counter)
+                int j;
+                if (nee == 1) j = group_append(here + 1);
+                else j = cap - 1 - group_append(here + 2);
+                ShadowRec r;
+                r.o_tmax = make_float4(so.x, so.y, so.z, tmax);
+                r.d_item = make_float4(sd.x, sd.y, sd.z, __int_as_float(loc));
+                r.contrib = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                F.shadow[j] = r;
+            }
+        }
+        vr[AV_BETA * vs + loc] = make_float4(beta.x, beta.y, beta.z, __int_as_float(si.material));
+        vr[AV_EMIT * vs + loc] = make_float4(c.x, c.y, c.z, __int_as_float(nee));
+        vr[AV_FCOS * vs + loc] = make_float4(fcos.x, fcos.y, fcos.z, 0.0f);
+        vr[AV_K * vs + loc] = make_float4(kk.x, kk.y, kk.z, 0.0f);
+        vr[AV_DA * vs + loc] = make_float4(dat.x, dat.y, dat.z, 0.0f);
+        vr[AV_DAL * vs + loc] = make_float4(dalt.x, dalt.y, dalt.z, 0.0f);
+        const int nv = level + 1;
+        float3 w = zero, dwa = zero, dwr = zero;
+        bool go = false;
+        if (level < F.max_depth && nv < MV) {
+            float2 uu, X;
+            if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
+            else { X = S.get2D(1); uu = S.get2D(1); }
+            FGrad sg;
+            SampleInfo sinfo;
+            BsdfSample bs = bsdf_sample_grad(bsdf, wo, uu, X, sg, sinfo);
+            if (!(bs.scatter == SC_ABSORBED || !nonzero(bs.f))) {
+                const float cw = AbsDot(si.ng, bs.wi);
+                w = bs.f * cw / bs.pdf;
+                dwa = sg.da * dalb * cw / bs.pdf;
+                dwr = sg.dal * dal * cw / bs.pdf;
+                beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
+                p_b = bsdf.pdf(wo, bs.wi);
+                o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+                float rr = 1.0f;
+                bool killed = false;
+                float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
+                if (mx < 1.0f && level >= 1) {
+                    float q = fmaxf(0.0f, 1.0f - mx);
+                    if (S.get1D() < q) killed = true;
+                    else {
+                        beta = beta / (1.0f - q);
+                        rr = 1.0f / (1.0f - q);
+                    }
+                }
+                w = w * rr;
+                dwa = dwa * rr;
+                dwr = dwr * rr;
+                go = !(killed || !nonzero(beta));
+                d = bs.wi;
+            }
+        }
+        vr[AV_W * vs + loc] = make_float4(w.x, w.y, w.z, 0.0f);
+        vr[AV_DWA * vs + loc] = make_float4(dwa.x, dwa.y, dwa.z, 0.0f);
+        vr[AV_DWR * vs + loc] = make_float4(dwr.x, dwr.y, dwr.z, 0.0f);
+        if (!go) {
+            end_path(false, nv, zero, zero);
+            continue;
+        }
+        const int j = group_append(next);
+        PathRec pr;
+        pr.o_pb = make_float4(o.x, o.y, o.z, p_b);
+        pr.d_seed = make_float4(d.x, d.y, d.z, __uint_as_float(S.seed));
+        pr.beta_item = make_float4(beta.x, beta.y, beta.z, __int_as_float(loc));
+        pr.prev = make_float4(si.pos.x, si.pos.y, si.pos.z, 0.0f);
+        out[j] = pr;
+    }
+}
+
+// The replay's shadow rays of `level`: an unoccluded ray marks its vertex's
+// light sample visible.
+struct AdjShadowQueue {
+    const ShadowRec* rec;
+    unsigned char* vis;
+    int nsun, cap;
+    __device__ __forceinline__ int slot(int i) const { return i < nsun ? i : cap - 1 - (i - nsun); }
+    __device__ __forceinline__ void ray(int i, float3& o, float3& d, float& tmin, float& tmax) const {
+        const int j = slot(i);
+        const float4 a = rec[j].o_tmax, b = rec[j].d_item;
+        o = make_float3(a.x, a.y, a.z);
+        d = make_float3(b.x, b.y, b.z);
+        tmin = 0.0f;
+        tmax = a.w;
+    }
+    __device__ __forceinline__ bool closest(int, const Hit&, float3&, float3&) const { return false; }
+    __device__ __forceinline__ void any(int i, bool occluded) const {
+        if (!occluded) vis[__float_as_int(rec[slot(i)].d_item.w)] = 1;
+    }
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_adj_shadow(FrameParams F, AdjParams A, int level) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    int* lc = F.level_counts + LEVEL_WORDS * level;
+    AdjShadowQueue q{F.shadow, A.vis + (size_t)level * F.cap, lc[1], F.cap};
+    trace_queue<true>(F.scene, lc[1] + lc[2], lc + 4, q, st, stack);
+}
+
+// Every sample of the wave: its radiance from the vertex records (the
+// forward's sum), clamp, image, and the reverse sweep into the gradients.
+__global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjParams A, long long wave0) {
+    extern __shared__ double sg[];
+    const int ng = 4 * A.nmat + ADJ_SKY_PARAMS;
+    grad_begin(sg, ng);
+    GradAcc acc{sg};
+    double gsky[SKY_PARAMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const SkyParams& P = F.sky;
+    const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
+    const float3 sun_rad = *F.sun_radiance;
+    const int cap = F.cap;
+    const size_t vs = A.vstride;
+    const int nhit = F.counts[0];
+    const long long left = (long long)nhit * F.nsamples - wave0;
+    const int n = (int)(left < 0 ? 0 : (left < cap ? left : cap));
+    const float inv_n = 1.0f / (float)F.nsamples;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long item = wave0 + i;
+        const int ks = (int)(item / nhit);
+        const int p = F.hit_list[item - (long long)ks * nhit];
+        const float4 e0 = A.vend[2 * (size_t)i], e1 = A.vend[2 * (size_t)i + 1];
+        const int nv = __float_as_int(e0.w);
+        const bool escaped = __float_as_int(e1.w) != 0;
+        const float3 d_end = xyz3(e0), b_end = xyz3(e1);
+        const float3 s_end = escaped ? nishita(P, obs, d_end) : make_float3(0.0f, 0.0f, 0.0f);
+        // c of vertex k: its emission, plus its light sample where visible
+        auto vertex_c = [&](int k, float4 emit, bool* vis_nee) {
+            const float3 c = xyz3(emit);
+            const int nee = __float_as_int(emit.w);
+            *vis_nee = nee != 0 && A.vis[(size_t)k * cap + i] != 0;
+            if (!*vis_nee) return c;
+            const float3 fcos = xyz3(A.vr[AV_FCOS * vs + (size_t)k * cap + i]);
+            const float3 kk = xyz3(A.vr[AV_K * vs + (size_t)k * cap + i]);
+            return nee == 1 ? c + fcos * sun_rad * kk.x : c + fcos * kk;
+        };
+        float3 L = make_float3(0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < nv; ++k) {
+            bool v;
+            const float3 b = xyz3(A.vr[AV_BETA * vs + (size_t)k * cap + i]);
+            L = L + b * vertex_c(k, A.vr[AV_EMIT * vs + (size_t)k * cap + i], &v);
+        }
+        if (escaped) L = L + b_end * s_end;
+        float3 msk;
+        const float3 Lc = make_float3(clamp_out(L.x, &msk.x), clamp_out(L.y, &msk.y), clamp_out(L.z, &msk.z));
+        const float4 a = A.adjoint[p];
+        const float3 g = make_float3(a.x, a.y, a.z) * msk * inv_n;
+        if (A.image) {
+            atomicAdd(&A.image[p].x, Lc.x * inv_n);
+            atomicAdd(&A.image[p].y, Lc.y * inv_n);
+            atomicAdd(&A.image[p].z, Lc.z * inv_n);
+        }
+        if (!nonzero(g)) continue;
+        float3 R = escaped ? s_end : make_float3(0.0f, 0.0f, 0.0f);
+        if (escaped) {
+            const float3 gb = wmul(g, b_end);
+            const bool band = sky_in_band(P, d_end);
+            const bool done = band ? sky_defer(A, d_end, gb)
+                                   : sky_push(A.skyqf, A.skyqf_count, A.skyqf_cap, d_end, gb);
+            if (!done) {
+                float3 J_end[SKY_PARAMS];
+                if (band) nishita_jacobian_d(P, obs, d_end, J_end);
+                else nishita_grad(P, obs, d_end, J_end);
+                for (int q = 0; q < SKY_PARAMS; ++q) gsky[q] += wdot(gb, J_end[q]);
+            }
+        }
+        for (int k = nv - 1; k >= 0; --k) {
+            const size_t o = (size_t)k * cap + i;
+            const float4 b4 = A.vr[AV_BETA * vs + o];
+            bool v;
+            const float3 ck = vertex_c(k, A.vr[AV_EMIT * vs + o], &v);
+            float3 dca = make_float3(0.0f, 0.0f, 0.0f), dcr = dca, cs = dca;
+            if (v) {
+                const int nee = __float_as_int(A.vr[AV_EMIT * vs + o].w);
+                const float3 kk = xyz3(A.vr[AV_K * vs + o]);
+                const float3 da = xyz3(A.vr[AV_DA * vs + o]), dl = xyz3(A.vr[AV_DAL * vs + o]);
+                if (nee == 1) {
+                    dca = da * sun_rad * kk.x;
+                    dcr = dl * sun_rad * kk.x;
+                    cs = xyz3(A.vr[AV_FCOS * vs + o]) * kk.x;
+                } else {
+                    dca = da * kk;
+                    dcr = dl * kk;
+                }
+            }
+            const float3 gb = wmul(g, xyz3(b4));
+            const float3 dwa = xyz3(A.vr[AV_DWA * vs + o]), dwr = xyz3(A.vr[AV_DWR * vs + o]);
+            const float3 ta = wmul(gb, dca + wmul(dwa, R));
+            const int m4 = 4 * __float_as_int(b4.w);
+            acc.add(m4 + 0, ta.x);
+            acc.add(m4 + 1, ta.y);
+            acc.add(m4 + 2, ta.z);
+            acc.add(m4 + 3, wdot(gb, dcr + wmul(dwr, R)));
+            if (nonzero(cs)) {
+                const float3 gs = wmul(gb, cs);
+                for (int q = 0; q < SKY_PARAMS; ++q) gsky[q] += wdot(gs, A.sun_J[q]);
+            }
+            R = ck + xyz3(A.vr[AV_W * vs + o]) * R;
+        }
+    }
+    for (int q = 0; q < SKY_PARAMS; ++q) {   // one shared add per warp per sky parameter
+        double v = gsky[q];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sg + 4 * A.nmat + q, v);
+    }
+    grad_end(sg, ng, A.grad);
+}
 
 }  // namespace kpt

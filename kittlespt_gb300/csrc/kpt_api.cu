@@ -157,6 +157,8 @@ struct kpt_context {
     DBuf<int> adj_skyq_count;
     DBuf<float4> adj_skyqf;     // deferred single-precision sky Jacobians
     DBuf<int> adj_skyqf_count;
+    DBuf<float4> adj_vr, adj_vend;   // the wavefront replay's vertex and end records
+    DBuf<unsigned char> adj_vis;     // the wavefront replay's light-sample visibility
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2], unsorted;
     DBuf<int> octants;
@@ -182,6 +184,8 @@ struct kpt_context {
 // Wave capacity: paths advanced together, level by level (208 B of work
 // buffers each; 2^25 paths hold a 1080p frame of 16 samples in one wave).
 static constexpr long long WAVE_CAP = 1LL << 25;
+// device memory for one wave of the wavefront adjoint's vertex records
+static constexpr size_t ADJ_WAVE_BYTES = (size_t)12 << 30;
 // finished lanes of a warp that store results and fetch rays together
 // (kpt_tuning.fetch_batch): 8 measured best on the 1080p16 frame (4..12 within 1.5%)
 static constexpr int FETCH_BATCH = 8;
@@ -293,6 +297,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     c->adj_skyq.release(); c->adj_skyq_count.release(); c->adj_skyqf.release(); c->adj_skyqf_count.release();
+    c->adj_vr.release(); c->adj_vend.release(); c->adj_vis.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
     if (c->ev_sky) cudaEventDestroy(c->ev_sky);
@@ -1591,13 +1596,21 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     KPT_CUDA(c->rec_count.ensure(1));
     // room for every sample's escape and every missing pixel
     const size_t qcap = (size_t)c->W * c->H * ((size_t)nsamples + 1);
+    FrameParams F = frame_params(c, sample0, nsamples);
+    // the wavefront replay's records: a wave of at most ADJ_WAVE_BYTES of them
+    const int D = F.max_depth;
+    const size_t per_path = sizeof(float4) * ((size_t)AV_FIELDS * (D + 1) + 2) + (size_t)(D + 1);
     if (!rec) {
+        const size_t fit = std::max<size_t>(1 << 16, ADJ_WAVE_BYTES / per_path);
+        F.cap = (int)std::min<size_t>((size_t)F.cap, fit);
+        KPT_CUDA(c->adj_vr.ensure((size_t)AV_FIELDS * (D + 1) * F.cap));
+        KPT_CUDA(c->adj_vend.ensure(2 * (size_t)F.cap));
+        KPT_CUDA(c->adj_vis.ensure((size_t)(D + 1) * F.cap));
         KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
         KPT_CUDA(c->adj_skyq_count.ensure(1));
         KPT_CUDA(c->adj_skyqf.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
         KPT_CUDA(c->adj_skyqf_count.ensure(1));
     }
-    FrameParams F = frame_params(c, sample0, nsamples);
     AdjParams A{};
     A.adjoint = reinterpret_cast<const float4*>(adjoint);
     A.grad = grad;
@@ -1614,6 +1627,10 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         A.skyqf = c->adj_skyqf.p;
         A.skyqf_count = c->adj_skyqf_count.p;
         A.skyqf_cap = (int)(c->adj_skyqf.n / 2);
+        A.vr = c->adj_vr.p;
+        A.vend = c->adj_vend.p;
+        A.vis = c->adj_vis.p;
+        A.vstride = (size_t)(D + 1) * F.cap;
     }
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
@@ -1623,7 +1640,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     if (A.skyq) KPT_CUDA(cudaMemsetAsync(A.skyq_count, 0, sizeof(int), s));
     if (A.skyqf) KPT_CUDA(cudaMemsetAsync(A.skyqf_count, 0, sizeof(int), s));
     KPT_CUDA(cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s));
-    const void* kern = rec ? (const void*)k_adjoint_rec : (const void*)k_adjoint;
+    const void* kern = rec ? (const void*)k_adjoint_rec : (const void*)k_adj_sweep;
     for (const void* k : {kern, (const void*)k_adjoint_miss})
         KPT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -1633,9 +1650,32 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
     k_adjoint_constants<<<1, 32, 0, s>>>(F, A);
     k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);
-    if (rec) k_adjoint_rec<<<grid, PATH_BLOCK, smem, s>>>(F, A);
-    else k_adjoint<<<grid, PATH_BLOCK, smem, s>>>(F, A);
-    c->launches += 5;
+    c->launches += 4;
+    if (rec) {
+        // the frozen-path records: one thread replays one sample
+        k_adjoint_rec<<<grid, PATH_BLOCK, smem, s>>>(F, A);
+        c->launches += 1;
+    } else {
+        // the wavefront replay, wave by wave (every pixel may hit: the last
+        // waves find no work when fewer do): per level the vertices, their
+        // shadow rays and the continuations, then every sample's sweep
+        const long long items = (long long)np * nsamples;
+        const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
+        const int g_shd = persistent_grid(c, (const void*)k_adj_shadow, TRACE_BLOCK);
+        const int g_vtx = persistent_grid(c, (const void*)k_adj_shade, PATH_BLOCK);
+        for (long long w0 = 0; w0 < items; w0 += F.cap) {
+            KPT_CUDA(cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s));
+            KPT_CUDA(cudaMemsetAsync(A.vis, 0, (size_t)(D + 1) * F.cap, s));
+            for (int l = 0; l <= D; ++l) {
+                if (l > 0) k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
+                k_adj_shade<<<g_vtx, PATH_BLOCK, 0, s>>>(F, A, l, w0);
+                k_adj_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, A, l);
+                c->launches += l > 0 ? 3 : 2;
+            }
+            k_adj_sweep<<<grid, PATH_BLOCK, smem, s>>>(F, A, w0);
+            c->launches += 1;
+        }
+    }
     if (A.skyq) {
         k_adjoint_sky_d<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
         k_adjoint_sky_f<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);

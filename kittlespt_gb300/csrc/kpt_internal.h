@@ -127,7 +127,19 @@ struct AdjParams {
     float4* skyqf;
     int* skyqf_count;
     int skyqf_cap;
+    // the wavefront replay: per vertex AV_FIELDS float4 fields, field f of
+    // level l, path slot i at vr[f * vstride + l * cap + i]; per path slot
+    // its end (direction, vertex count; throughput, escaped) at vend[2 i],
+    // vend[2 i + 1]; vis[l * cap + i] = 1 when the light sample of vertex l
+    // is unoccluded
+    float4* vr;
+    float4* vend;
+    unsigned char* vis;
+    size_t vstride;
 };
+
+// fields of the wavefront replay's vertex record
+enum AdjVField { AV_BETA, AV_EMIT, AV_FCOS, AV_K, AV_DA, AV_DAL, AV_W, AV_DWA, AV_DWR, AV_FIELDS };
 
 // Frisvad basis applied to l, IEEE arithmetic (maths/matrix_maths.cuh:375-396).
 __device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
@@ -162,10 +174,12 @@ __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
 __global__ void k_adjoint_constants(FrameParams F, AdjParams A);
 __global__ void k_sky_grad(SkyParams P, int n, const float3* dirs, float3* out);
 __global__ void k_adjoint_miss(FrameParams F, AdjParams A);
-__global__ void k_adjoint(FrameParams F, AdjParams A);
 __global__ void k_adjoint_rec(FrameParams F, AdjParams A);   // also writes the frozen-path records
 __global__ void k_adjoint_sky_d(FrameParams F, AdjParams A);
 __global__ void k_adjoint_sky_f(FrameParams F, AdjParams A);
+__global__ void k_adj_shade(FrameParams F, AdjParams A, int level, long long wave0);
+__global__ void k_adj_shadow(FrameParams F, AdjParams A, int level);
+__global__ void k_adj_sweep(FrameParams F, AdjParams A, long long wave0);
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
 // Temporal accumulation (kernels.cu:164-327): per instance, the matrices of
 // computeVelocity and testReprojection for one frame, rows of column-major

@@ -106,15 +106,6 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary_sky(FrameParams F) {
 // ---------------------------------------------------------------------------
 // paths: one wave of work items advanced level by level
 
-// Appends the lanes of a (possibly divergent) warp that reach this call to a
-// list with one atomic; returns each lane's slot.
-__device__ __forceinline__ int group_append(int* counter) {
-    cg::coalesced_group g = cg::coalesced_threads();
-    int base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
-    return g.shfl(base, 0) + (int)g.thread_rank();
-}
-
 // Shadow ray of Integrator::unoccluded (integrator.cuh:124-131): from the
 // offset surface point towards `target`, stopping 0.11 short of it.
 __device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si, float3 target, float3 contrib,

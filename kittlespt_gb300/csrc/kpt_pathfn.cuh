@@ -130,6 +130,15 @@ __device__ __forceinline__ void flush_stats(const TraceStats& st, unsigned long 
     }
 }
 
+// Appends the lanes of a (possibly divergent) warp that reach this call to a
+// list with one atomic; returns each lane's slot.
+__device__ __forceinline__ int group_append(int* counter) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+    return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
 // Appends `want` lanes of the warp to a list: returns each lane's slot.
 __device__ __forceinline__ int warp_append(bool want, int* counter) {
     unsigned mask = __ballot_sync(0xffffffffu, want);
