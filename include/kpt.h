@@ -367,7 +367,10 @@ kpt_status kpt_autotune_batch(kpt_batch* b, int n, kpt_context* const* jobs, con
  * respect to the BSDF values and the sky radiance.  image (may be null)
  * receives the image itself.  Requires max_depth <= 16.
  * kpt_adjoint_device takes device pointers (grad: doubles) and does not
- * synchronise; kpt_adjoint takes host arrays. */
+ * synchronise; kpt_adjoint takes host arrays.  The replay runs in waves whose
+ * per-vertex records take at most 12 GiB of device memory, plus two sky
+ * queues of 32 B per pixel and sample; the context keeps these buffers for
+ * the next call until kpt_destroy. */
 kpt_status kpt_adjoint_param_count(kpt_context* ctx, int* n);
 kpt_status kpt_adjoint_device(kpt_context* ctx, int sample0, int nsamples, const float* adjoint, double* grad,
                               float* image);
