@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_trace_chains(
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
     BounceQueue q{o, d, n, nbounces, inst, tri, t, &s, 0, make_float3(0.0f, 0.0f, 0.0f), make_float3(0.0f, 0.0f, 0.0f)};
-    trace_queue<false>(s, n, next, q, st, stack);
+    trace_queue<false, BounceQueue, 2>(s, n, next, q, st, stack);
     flush_stats(st, counters);
 }
 
