@@ -17,6 +17,7 @@
 //     matrices indexed m[column][row]).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -238,6 +239,14 @@ public:
         getRenderTarget(img.data());
         return img;
     }
+
+    // getDebugRenderTargetTexture (renderer.cu:202-205): the reference's debug
+    // texture, whose only write is commented out (kernels.cu:436-448), holds
+    // zeros
+    void getDebugRenderTarget(float* rgba) const {
+        std::fill(rgba, rgba + (size_t)m_width * m_height * 4, 0.0f);
+    }
+    std::vector<float> getDebugRenderTarget() const { return std::vector<float>((size_t)m_width * m_height * 4, 0.0f); }
 
     size_t getMaterialsCount() const { return (size_t)counts()[0]; }
     size_t getMeshCount() const { return (size_t)counts()[2]; }   // the reference's meshes are instances here

@@ -257,6 +257,12 @@ class Renderer:
         """Display image (AgX, non-linear sRGB), [H][W][4] float."""
         return self._read(self._L.kpt_read_image)
 
+    def get_debug_render_target(self) -> np.ndarray:
+        """getDebugRenderTargetTexture (renderer.cu:202-205): the reference's
+        debug texture, whose only write is commented out (kernels.cu:436-448),
+        so it holds zeros; [H][W][4] float at the output size."""
+        return np.zeros((self.height, self.width, 4), np.float32)
+
     def render_size(self):
         """(width, height) of the render resolution (the output's unless upscaling)."""
         w, h = C.c_int(), C.c_int()

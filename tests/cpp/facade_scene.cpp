@@ -6,6 +6,7 @@
 // through the C ABI and compare the images.  Exits 3 when no GPU context can be created.
 //
 // usage: facade_scene <out.bin> <width> <height> <frames>
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -119,6 +120,11 @@ int main(int argc, char** argv) {
         }
         for (int f = 0; f < frames; ++f) r.executeRendering(16.0f, 2);
         std::vector<float> img = r.getRenderTarget();
+        const std::vector<float> dbg = r.getDebugRenderTarget();   // nothing writes it: zeros
+        if (dbg.size() != img.size() || std::any_of(dbg.begin(), dbg.end(), [](float v) { return v != 0.0f; })) {
+            std::printf("debug render target is not a zero image of the output size\n");
+            return 1;
+        }
         // arrays of the scene as the facade passed them, then the image
         FILE* fp = std::fopen(argv[1], "wb");
         if (!fp) return 1;
