@@ -224,8 +224,9 @@ kpt_status kpt_read_albedo(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_histogram(kpt_context* ctx, uint64_t* bins256);
 kpt_status kpt_get_stats(kpt_context* ctx, kpt_stats* st);
 /* Diagnostics, no reference counterpart: for each level 0 .. min(max_levels,
- * max_depth + 1) - 1 of the last wave of the last frame rendered on this
- * context, counts[3 l] = paths shaded at level l (level >= 1: extension rays
+ * max_depth + 1) - 1 of the last wave of the last frame rendered (or adjoint
+ * replayed) on this context, counts[3 l] = paths shaded at level l (level
+ * >= 1: extension rays
  * traced into it), counts[3 l + 1] = sun shadow rays and counts[3 l + 2] =
  * area-light shadow rays it sent; *levels = the number of levels written.  A
  * frame has one wave unless width x height x spp exceeds the wave capacity

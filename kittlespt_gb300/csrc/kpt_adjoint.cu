@@ -566,6 +566,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
     PathRec* out = F.paths[(level + 1) & 1];
     int* here = F.level_counts + LEVEL_WORDS * level;
     int* next = F.level_counts + LEVEL_WORDS * (level + 1);
+    if (first && blockIdx.x == 0 && threadIdx.x == 0) here[0] = n;   // read back by kpt_get_level_counts
     float4* vr = A.vr + (size_t)level * cap;
     const size_t vs = A.vstride;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

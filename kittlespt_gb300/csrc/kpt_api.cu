@@ -1663,6 +1663,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
         const int g_shd = persistent_grid(c, (const void*)k_adj_shadow, TRACE_BLOCK);
         const int g_vtx = persistent_grid(c, (const void*)k_adj_shade, PATH_BLOCK);
+        c->levels_depth = D;   // kpt_get_level_counts then reports the replay's last wave
         for (long long w0 = 0; w0 < items; w0 += F.cap) {
             KPT_CUDA(cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s));
             KPT_CUDA(cudaMemsetAsync(A.vis, 0, (size_t)(D + 1) * F.cap, s));
