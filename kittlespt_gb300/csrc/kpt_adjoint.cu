@@ -827,6 +827,30 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_adj_shadow(Fr
     trace_queue<true>(F.scene, lc[1] + lc[2], lc + 4, q, st, stack);
 }
 
+// An escape's sky Jacobian evaluated where it occurs (its queue is full):
+// weight . J added to the block's sky gradient slots.
+static __device__ __noinline__ void sky_jacobian_now(const SkyParams& P, float3 obs, float3 d, bool band, float3 w,
+                                                     double* slots) {
+    float3 J[SKY_PARAMS];
+    if (band) nishita_jacobian_d(P, obs, d, J);
+    else nishita_grad(P, obs, d, J);
+    for (int q = 0; q < SKY_PARAMS; ++q) atomicAdd(slots + q, (double)wdot(w, J[q]));
+}
+
+// The sky radiance at the end of every escaped path of the wave (the
+// forward's march), for k_adj_sweep.
+__global__ void __launch_bounds__(PATH_BLOCK) k_adj_sky(FrameParams F, AdjParams A, long long wave0) {
+    const SkyParams& P = F.sky;
+    const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
+    const long long left = (long long)F.counts[0] * F.nsamples - wave0;
+    const int n = (int)(left < 0 ? 0 : (left < F.cap ? left : F.cap));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (__float_as_int(A.vend[2 * (size_t)i + 1].w) == 0) continue;
+        const float3 s = nishita(P, obs, xyz3(A.vend[2 * (size_t)i]));
+        A.vsky[i] = make_float4(s.x, s.y, s.z, 0.0f);
+    }
+}
+
 // Every sample of the wave: its radiance from the vertex records (the
 // forward's sum), clamp, image, and the reverse sweep into the gradients.
 __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjParams A, long long wave0) {
@@ -852,7 +876,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
         const int nv = __float_as_int(e0.w);
         const bool escaped = __float_as_int(e1.w) != 0;
         const float3 d_end = xyz3(e0), b_end = xyz3(e1);
-        const float3 s_end = escaped ? nishita(P, obs, d_end) : make_float3(0.0f, 0.0f, 0.0f);
+        const float3 s_end = escaped ? xyz3(A.vsky[i]) : make_float3(0.0f, 0.0f, 0.0f);
         // c of vertex k: its emission, plus its light sample where visible
         auto vertex_c = [&](int k, float4 emit, bool* vis_nee) {
             const float3 c = xyz3(emit);
@@ -886,12 +910,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
             const bool band = sky_in_band(P, d_end);
             const bool done = band ? sky_defer(A, d_end, gb)
                                    : sky_push(A.skyqf, A.skyqf_count, A.skyqf_cap, d_end, gb);
-            if (!done) {
-                float3 J_end[SKY_PARAMS];
-                if (band) nishita_jacobian_d(P, obs, d_end, J_end);
-                else nishita_grad(P, obs, d_end, J_end);
-                for (int q = 0; q < SKY_PARAMS; ++q) gsky[q] += wdot(gb, J_end[q]);
-            }
+            if (!done) sky_jacobian_now(P, obs, d_end, band, gb, sg + 4 * A.nmat);
         }
         for (int k = nv - 1; k >= 0; --k) {
             const size_t o = (size_t)k * cap + i;

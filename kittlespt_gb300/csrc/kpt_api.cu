@@ -157,7 +157,7 @@ struct kpt_context {
     DBuf<int> adj_skyq_count;
     DBuf<float4> adj_skyqf;     // deferred single-precision sky Jacobians
     DBuf<int> adj_skyqf_count;
-    DBuf<float4> adj_vr, adj_vend;   // the wavefront replay's vertex and end records
+    DBuf<float4> adj_vr, adj_vend, adj_vsky;   // the wavefront replay's vertex and end records, escape skies
     DBuf<unsigned char> adj_vis;     // the wavefront replay's light-sample visibility
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2], unsorted;
@@ -297,7 +297,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     c->adj_skyq.release(); c->adj_skyq_count.release(); c->adj_skyqf.release(); c->adj_skyqf_count.release();
-    c->adj_vr.release(); c->adj_vend.release(); c->adj_vis.release();
+    c->adj_vr.release(); c->adj_vend.release(); c->adj_vsky.release(); c->adj_vis.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
     if (c->ev_sky) cudaEventDestroy(c->ev_sky);
@@ -1605,6 +1605,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         F.cap = (int)std::min<size_t>((size_t)F.cap, fit);
         KPT_CUDA(c->adj_vr.ensure((size_t)AV_FIELDS * (D + 1) * F.cap));
         KPT_CUDA(c->adj_vend.ensure(2 * (size_t)F.cap));
+        KPT_CUDA(c->adj_vsky.ensure((size_t)F.cap));
         KPT_CUDA(c->adj_vis.ensure((size_t)(D + 1) * F.cap));
         KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
         KPT_CUDA(c->adj_skyq_count.ensure(1));
@@ -1629,6 +1630,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         A.skyqf_cap = (int)(c->adj_skyqf.n / 2);
         A.vr = c->adj_vr.p;
         A.vend = c->adj_vend.p;
+        A.vsky = c->adj_vsky.p;
         A.vis = c->adj_vis.p;
         A.vstride = (size_t)(D + 1) * F.cap;
     }
@@ -1647,12 +1649,18 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     KPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PATH_BLOCK, smem));
     const int grid = std::max(1, per_sm) * c->sm_count;
     k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
+    // the sun's double-precision Jacobian (one thread) on the side stream: only
+    // the replay's sweep (or the records kernel) reads it
+    KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
+    KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
+    k_adjoint_constants<<<1, 32, 0, c->side>>>(F, A);
+    KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
     k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
-    k_adjoint_constants<<<1, 32, 0, s>>>(F, A);
     k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);
     c->launches += 4;
     if (rec) {
         // the frozen-path records: one thread replays one sample
+        KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
         k_adjoint_rec<<<grid, PATH_BLOCK, smem, s>>>(F, A);
         c->launches += 1;
     } else {
@@ -1673,8 +1681,10 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
                 k_adj_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, A, l);
                 c->launches += l > 0 ? 3 : 2;
             }
+            k_adj_sky<<<g_vtx, PATH_BLOCK, 0, s>>>(F, A, w0);
+            KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
             k_adj_sweep<<<grid, PATH_BLOCK, smem, s>>>(F, A, w0);
-            c->launches += 1;
+            c->launches += 2;
         }
     }
     if (A.skyq) {

@@ -134,6 +134,7 @@ struct AdjParams {
     // is unoccluded
     float4* vr;
     float4* vend;
+    float4* vsky;              // [cap] the sky radiance of an escaped path's last ray
     unsigned char* vis;
     size_t vstride;
 };
@@ -180,6 +181,7 @@ __global__ void k_adjoint_sky_f(FrameParams F, AdjParams A);
 __global__ void k_adj_shade(FrameParams F, AdjParams A, int level, long long wave0);
 __global__ void k_adj_shadow(FrameParams F, AdjParams A, int level);
 __global__ void k_adj_sweep(FrameParams F, AdjParams A, long long wave0);
+__global__ void k_adj_sky(FrameParams F, AdjParams A, long long wave0);
 // kpt_post.cu (IEEE): clamp and add the samples of each pixel in sample order
 // Temporal accumulation (kernels.cu:164-327): per instance, the matrices of
 // computeVelocity and testReprojection for one frame, rows of column-major
