@@ -1688,8 +1688,13 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         }
     }
     if (A.skyq) {
+        // the double (FP64 pipe) and single-precision (FP32) Jacobians side by side
+        KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
+        KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
+        k_adjoint_sky_f<<<c->sm_count * 4, PATH_BLOCK, 0, c->side>>>(F, A);
+        KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
         k_adjoint_sky_d<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
-        k_adjoint_sky_f<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
+        KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
         c->launches += 2;
     }
     KPT_CUDA(cudaGetLastError());
