@@ -567,8 +567,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
     int* here = F.level_counts + LEVEL_WORDS * level;
     int* next = F.level_counts + LEVEL_WORDS * (level + 1);
     if (first && blockIdx.x == 0 && threadIdx.x == 0) here[0] = n;   // read back by kpt_get_level_counts
-    float4* vr = A.vr + (size_t)level * cap;
-    const size_t vs = A.vstride;
+    float4* const vr0 = A.vr + (size_t)level * cap * AV_FIELDS;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float3 o, d, beta, prev;
         float p_b;
@@ -739,12 +738,12 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
                 F.shadow[j] = r;
             }
         }
-        vr[AV_BETA * vs + loc] = make_float4(beta.x, beta.y, beta.z, __int_as_float(si.material));
-        vr[AV_EMIT * vs + loc] = make_float4(c.x, c.y, c.z, __int_as_float(nee));
-        vr[AV_FCOS * vs + loc] = make_float4(fcos.x, fcos.y, fcos.z, 0.0f);
-        vr[AV_K * vs + loc] = make_float4(kk.x, kk.y, kk.z, 0.0f);
-        vr[AV_DA * vs + loc] = make_float4(dat.x, dat.y, dat.z, 0.0f);
-        vr[AV_DAL * vs + loc] = make_float4(dalt.x, dalt.y, dalt.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_BETA] = make_float4(beta.x, beta.y, beta.z, __int_as_float(si.material));
+        vr0[(size_t)loc * AV_FIELDS + AV_EMIT] = make_float4(c.x, c.y, c.z, __int_as_float(nee));
+        vr0[(size_t)loc * AV_FIELDS + AV_FCOS] = make_float4(fcos.x, fcos.y, fcos.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_K] = make_float4(kk.x, kk.y, kk.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_DA] = make_float4(dat.x, dat.y, dat.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_DAL] = make_float4(dalt.x, dalt.y, dalt.z, 0.0f);
         const int nv = level + 1;
         float3 w = zero, dwa = zero, dwr = zero;
         bool go = false;
@@ -781,9 +780,9 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
                 d = bs.wi;
             }
         }
-        vr[AV_W * vs + loc] = make_float4(w.x, w.y, w.z, 0.0f);
-        vr[AV_DWA * vs + loc] = make_float4(dwa.x, dwa.y, dwa.z, 0.0f);
-        vr[AV_DWR * vs + loc] = make_float4(dwr.x, dwr.y, dwr.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_W] = make_float4(w.x, w.y, w.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_DWA] = make_float4(dwa.x, dwa.y, dwa.z, 0.0f);
+        vr0[(size_t)loc * AV_FIELDS + AV_DWR] = make_float4(dwr.x, dwr.y, dwr.z, 0.0f);
         if (!go) {
             end_path(false, nv, zero, zero);
             continue;
@@ -859,11 +858,13 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
     grad_begin(sg, ng);
     GradAcc acc{sg};
     double gsky[SKY_PARAMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    // the sun light samples' weights, summed: their sky gradient is linear in
+    // the sun's Jacobian, applied once at the end
+    double cs0 = 0.0, cs1 = 0.0, cs2 = 0.0;
     const SkyParams& P = F.sky;
     const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
     const float3 sun_rad = *F.sun_radiance;
     const int cap = F.cap;
-    const size_t vs = A.vstride;
     const int nhit = F.counts[0];
     const long long left = (long long)nhit * F.nsamples - wave0;
     const int n = (int)(left < 0 ? 0 : (left < cap ? left : cap));
@@ -883,15 +884,16 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
             const int nee = __float_as_int(emit.w);
             *vis_nee = nee != 0 && A.vis[(size_t)k * cap + i] != 0;
             if (!*vis_nee) return c;
-            const float3 fcos = xyz3(A.vr[AV_FCOS * vs + (size_t)k * cap + i]);
-            const float3 kk = xyz3(A.vr[AV_K * vs + (size_t)k * cap + i]);
+            const float3 fcos = xyz3(A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_FCOS]);
+            const float3 kk = xyz3(A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_K]);
             return nee == 1 ? c + fcos * sun_rad * kk.x : c + fcos * kk;
         };
         float3 L = make_float3(0.0f, 0.0f, 0.0f);
+#pragma unroll 1
         for (int k = 0; k < nv; ++k) {
             bool v;
-            const float3 b = xyz3(A.vr[AV_BETA * vs + (size_t)k * cap + i]);
-            L = L + b * vertex_c(k, A.vr[AV_EMIT * vs + (size_t)k * cap + i], &v);
+            const float3 b = xyz3(A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_BETA]);
+            L = L + b * vertex_c(k, A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_EMIT], &v);
         }
         if (escaped) L = L + b_end * s_end;
         float3 msk;
@@ -912,27 +914,28 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
                                    : sky_push(A.skyqf, A.skyqf_count, A.skyqf_cap, d_end, gb);
             if (!done) sky_jacobian_now(P, obs, d_end, band, gb, sg + 4 * A.nmat);
         }
+#pragma unroll 1
         for (int k = nv - 1; k >= 0; --k) {
             const size_t o = (size_t)k * cap + i;
-            const float4 b4 = A.vr[AV_BETA * vs + o];
+            const float4 b4 = A.vr[o * AV_FIELDS + AV_BETA];
             bool v;
-            const float3 ck = vertex_c(k, A.vr[AV_EMIT * vs + o], &v);
+            const float3 ck = vertex_c(k, A.vr[o * AV_FIELDS + AV_EMIT], &v);
             float3 dca = make_float3(0.0f, 0.0f, 0.0f), dcr = dca, cs = dca;
             if (v) {
-                const int nee = __float_as_int(A.vr[AV_EMIT * vs + o].w);
-                const float3 kk = xyz3(A.vr[AV_K * vs + o]);
-                const float3 da = xyz3(A.vr[AV_DA * vs + o]), dl = xyz3(A.vr[AV_DAL * vs + o]);
+                const int nee = __float_as_int(A.vr[o * AV_FIELDS + AV_EMIT].w);
+                const float3 kk = xyz3(A.vr[o * AV_FIELDS + AV_K]);
+                const float3 da = xyz3(A.vr[o * AV_FIELDS + AV_DA]), dl = xyz3(A.vr[o * AV_FIELDS + AV_DAL]);
                 if (nee == 1) {
                     dca = da * sun_rad * kk.x;
                     dcr = dl * sun_rad * kk.x;
-                    cs = xyz3(A.vr[AV_FCOS * vs + o]) * kk.x;
+                    cs = xyz3(A.vr[o * AV_FIELDS + AV_FCOS]) * kk.x;
                 } else {
                     dca = da * kk;
                     dcr = dl * kk;
                 }
             }
             const float3 gb = wmul(g, xyz3(b4));
-            const float3 dwa = xyz3(A.vr[AV_DWA * vs + o]), dwr = xyz3(A.vr[AV_DWR * vs + o]);
+            const float3 dwa = xyz3(A.vr[o * AV_FIELDS + AV_DWA]), dwr = xyz3(A.vr[o * AV_FIELDS + AV_DWR]);
             const float3 ta = wmul(gb, dca + wmul(dwa, R));
             const int m4 = 4 * __float_as_int(b4.w);
             acc.add(m4 + 0, ta.x);
@@ -941,13 +944,16 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
             acc.add(m4 + 3, wdot(gb, dcr + wmul(dwr, R)));
             if (nonzero(cs)) {
                 const float3 gs = wmul(gb, cs);
-                for (int q = 0; q < SKY_PARAMS; ++q) gsky[q] += wdot(gs, A.sun_J[q]);
+                cs0 += gs.x;
+                cs1 += gs.y;
+                cs2 += gs.z;
             }
-            R = ck + xyz3(A.vr[AV_W * vs + o]) * R;
+            R = ck + xyz3(A.vr[o * AV_FIELDS + AV_W]) * R;
         }
     }
     for (int q = 0; q < SKY_PARAMS; ++q) {   // one shared add per warp per sky parameter
-        double v = gsky[q];
+        const float3 J = A.sun_J[q];
+        double v = gsky[q] + cs0 * J.x + cs1 * J.y + cs2 * J.z;
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(sg + 4 * A.nmat + q, v);
     }

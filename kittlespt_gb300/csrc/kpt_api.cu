@@ -1632,7 +1632,6 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         A.vend = c->adj_vend.p;
         A.vsky = c->adj_vsky.p;
         A.vis = c->adj_vis.p;
-        A.vstride = (size_t)(D + 1) * F.cap;
     }
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;

@@ -128,7 +128,7 @@ struct AdjParams {
     int* skyqf_count;
     int skyqf_cap;
     // the wavefront replay: per vertex AV_FIELDS float4 fields, field f of
-    // level l, path slot i at vr[f * vstride + l * cap + i]; per path slot
+    // level l, path slot i at vr[(l * cap + i) * AV_FIELDS + f]; per path slot
     // its end (direction, vertex count; throughput, escaped) at vend[2 i],
     // vend[2 i + 1]; vis[l * cap + i] = 1 when the light sample of vertex l
     // is unoccluded
@@ -136,7 +136,6 @@ struct AdjParams {
     float4* vend;
     float4* vsky;              // [cap] the sky radiance of an escaped path's last ray
     unsigned char* vis;
-    size_t vstride;
 };
 
 // fields of the wavefront replay's vertex record
