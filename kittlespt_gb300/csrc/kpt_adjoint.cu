@@ -608,8 +608,9 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
             A.vend[2 * (size_t)loc] = make_float4(de.x, de.y, de.z, __int_as_float(nv));
             A.vend[2 * (size_t)loc + 1] = make_float4(be.x, be.y, be.z, __int_as_float(escaped ? 1 : 0));
         };
-        if (h.inst < 0) {   // the path leaves the scene: the sweep evaluates the sky
+        if (h.inst < 0) {   // the path leaves the scene: k_adj_sky evaluates the sky
             end_path(true, level, d, beta);
+            A.esc[group_append(A.esc_count)] = loc;
             continue;
         }
         Sampler S;
@@ -838,13 +839,12 @@ static __device__ __noinline__ void sky_jacobian_now(const SkyParams& P, float3 
 
 // The sky radiance at the end of every escaped path of the wave (the
 // forward's march), for k_adj_sweep.
-__global__ void __launch_bounds__(PATH_BLOCK) k_adj_sky(FrameParams F, AdjParams A, long long wave0) {
+__global__ void __launch_bounds__(PATH_BLOCK) k_adj_sky(FrameParams F, AdjParams A, long long) {
     const SkyParams& P = F.sky;
     const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
-    const long long left = (long long)F.counts[0] * F.nsamples - wave0;
-    const int n = (int)(left < 0 ? 0 : (left < F.cap ? left : F.cap));
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (__float_as_int(A.vend[2 * (size_t)i + 1].w) == 0) continue;
+    const int n = *A.esc_count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int i = A.esc[q];
         const float3 s = nishita(P, obs, xyz3(A.vend[2 * (size_t)i]));
         A.vsky[i] = make_float4(s.x, s.y, s.z, 0.0f);
     }

@@ -158,6 +158,7 @@ struct kpt_context {
     DBuf<float4> adj_skyqf;     // deferred single-precision sky Jacobians
     DBuf<int> adj_skyqf_count;
     DBuf<float4> adj_vr, adj_vend, adj_vsky;   // the wavefront replay's vertex and end records, escape skies
+    DBuf<int> adj_esc;                          // the wavefront replay's escaped paths, then their count
     DBuf<unsigned char> adj_vis;     // the wavefront replay's light-sample visibility
     DBuf<float4> pixel_sky, radiance, sky_queue;
     DBuf<PathRec> paths[2], unsorted;
@@ -297,7 +298,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     c->adj_skyq.release(); c->adj_skyq_count.release(); c->adj_skyqf.release(); c->adj_skyqf_count.release();
-    c->adj_vr.release(); c->adj_vend.release(); c->adj_vsky.release(); c->adj_vis.release();
+    c->adj_vr.release(); c->adj_vend.release(); c->adj_vsky.release(); c->adj_vis.release(); c->adj_esc.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
     if (c->ev_sky) cudaEventDestroy(c->ev_sky);
@@ -1606,6 +1607,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         KPT_CUDA(c->adj_vr.ensure((size_t)AV_FIELDS * (D + 1) * F.cap));
         KPT_CUDA(c->adj_vend.ensure(2 * (size_t)F.cap));
         KPT_CUDA(c->adj_vsky.ensure((size_t)F.cap));
+        KPT_CUDA(c->adj_esc.ensure((size_t)F.cap + 1));
         KPT_CUDA(c->adj_vis.ensure((size_t)(D + 1) * F.cap));
         KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
         KPT_CUDA(c->adj_skyq_count.ensure(1));
@@ -1631,6 +1633,8 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         A.vr = c->adj_vr.p;
         A.vend = c->adj_vend.p;
         A.vsky = c->adj_vsky.p;
+        A.esc = c->adj_esc.p;
+        A.esc_count = c->adj_esc.p + F.cap;
         A.vis = c->adj_vis.p;
     }
     cudaStream_t s = c->stream;
@@ -1674,6 +1678,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
         for (long long w0 = 0; w0 < items; w0 += F.cap) {
             KPT_CUDA(cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s));
             KPT_CUDA(cudaMemsetAsync(A.vis, 0, (size_t)(D + 1) * F.cap, s));
+            KPT_CUDA(cudaMemsetAsync(A.esc_count, 0, sizeof(int), s));
             for (int l = 0; l <= D; ++l) {
                 if (l > 0) k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
                 k_adj_shade<<<g_vtx, PATH_BLOCK, 0, s>>>(F, A, l, w0);

@@ -135,6 +135,8 @@ struct AdjParams {
     float4* vr;
     float4* vend;
     float4* vsky;              // [cap] the sky radiance of an escaped path's last ray
+    int* esc;                  // [cap] slots of the wave's escaped paths, esc_count of them
+    int* esc_count;
     unsigned char* vis;
 };
 
