@@ -738,6 +738,32 @@ def run_profile_case(spec):
     r.shutdown()
 
 
+def run_adjoint_case(spec):
+    """Two adjoint evaluations of the differentiation scene at a reduced size
+    ("WxHxSPP") with a random adjoint image: the small case that ncu captures
+    of the adjoint's kernels run on."""
+    import torch
+    from kittlespt_gb300 import _lib as K
+    from kittlespt_gb300 import scenes as S
+    from kittlespt_gb300.renderer import Renderer
+    w, h, spp = (int(v) for v in spec.lower().split("x"))
+    sc = adjoint_scene()
+    sc.width, sc.height = w, h
+    sc.camera = S.Camera.look_at((0.0, 1.0, 5.0), (0.0, 0.0, 0.0), 45.0, w, h)
+    r = Renderer(0)
+    r.initialize()
+    r.load_scene(sc)
+    adj = torch.rand((h, w, 4), device="cuda", generator=torch.Generator("cuda").manual_seed(1))
+    n = C.c_int()
+    K.check(r._L.kpt_adjoint_param_count(r.ctx, C.byref(n)))
+    g = torch.zeros(n.value, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        K.check(r._L.kpt_adjoint_device(r.ctx, 0, spp, adj.data_ptr(), g.data_ptr(), None))
+    r.synchronize()
+    print(f"adjoint case {w}x{h}x{spp}: |grad| {float(g.norm()):.6g}", file=sys.stderr)
+    r.shutdown()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -753,9 +779,15 @@ def main():
                          "upscale: 1080p output rendered at 1/2.5 and upscaled, bilinear and FSR")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
+    ap.add_argument("--adjoint-case", default=None, metavar="WxHxSPP",
+                    help="run two adjoint evaluations of the differentiation scene at this size and exit "
+                         "(small case for ncu)")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args.profile_case)
+        return
+    if args.adjoint_case:
+        run_adjoint_case(args.adjoint_case)
         return
     if args.impl == "reference":
         run_reference(args)
