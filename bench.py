@@ -722,6 +722,66 @@ def run_upscale(args):
     print(json.dumps(out))
 
 
+def run_temporal(args):
+    """Temporal accumulation (kpt_settings.temporal_accumulation): the
+    full-frame scene at 1920x1080, 16 spp per call (each sample one reference
+    frame, blended into the reprojected history), the camera moving a little
+    before every call; the same frames with the running mean beside them.
+    Device time per call over K calls (CUDA events on the library's stream, L2
+    flushed between calls)."""
+    import torch
+    from kittlespt_gb300 import scenes as S
+    from kittlespt_gb300.renderer import Renderer
+    sc = S.scene_full(W, H, SPP, DEPTH)
+    r = Renderer(0)
+    r.initialize()
+    r.load_scene(sc)
+    stream = torch.cuda.ExternalStream(r.stream(), device=0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=0)
+    ip = sc.camera.inv_proj.astype(np.float32)
+    res = {}
+    try:
+        for mode, name in ((0, "running_mean"), (1, "temporal")):
+            r.set_renderer_settings(temporal_accumulation=mode)
+            k = 0
+
+            def frame():
+                nonlocal k
+                iv = sc.camera.inv_view.astype(np.float32).copy()
+                iv[:3, 3] += np.float32(0.02 * (k % 16))   # a slow pan, back every 16 frames
+                r.set_camera_inverse(ip, iv)
+                r.execute_rendering(16.0, SPP)
+                k += 1
+            for _ in range(args.warmup):
+                frame()
+                with torch.cuda.stream(stream):
+                    flush.add_(1.0)   # the first torch launch loads its module: keep it out of the timed region
+            r.synchronize()
+            torch.cuda.synchronize()
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                start.record(stream)
+                for j in range(args.steps):
+                    frame()
+                    if j + 1 < args.steps:
+                        flush.add_(1.0)
+                stop.record(stream)
+            r.synchronize()
+            torch.cuda.synchronize()
+            res[name] = {"ms_per_frame": start.elapsed_time(stop) / args.steps}
+            print(f"[bench] {name}: {res[name]['ms_per_frame']:.2f} ms/frame", file=sys.stderr)
+    finally:
+        r.shutdown()
+    t = res["temporal"]
+    out = {"metric": "frames/s, 1920x1080 temporal accumulation, camera moving every frame (16 spp, depth 8)",
+           "value": 1e3 / t["ms_per_frame"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t["ms_per_frame"], "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded procedural scene)",
+           "config": {"workload": "temporal_1080p_16spp_moving_camera", "width": W, "height": H, "spp": SPP,
+                      "max_depth": DEPTH, "l2": "flushed between frames"}, "modes": res}
+    print(json.dumps(out))
+
+
 def run_profile_case(spec):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
     small case that ncu captures of single kernels run on."""
@@ -772,11 +832,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="frame",
-                    choices=["frame", "batch", "adjoint", "traversal", "blas", "upscale"],
+                    choices=["frame", "batch", "adjoint", "traversal", "blas", "upscale", "temporal"],
                     help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one; "
                          "adjoint: gradient evaluations/s of the path-replay adjoint; "
                          "traversal: rays/s on 2M random triangles; blas: BLAS build on upload, host vs device; "
-                         "upscale: 1080p output rendered at 1/2.5 and upscaled, bilinear and FSR")
+                         "upscale: 1080p output rendered at 1/2.5 and upscaled, bilinear and FSR; "
+                         "temporal: 1080p temporal accumulation with a moving camera")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
     ap.add_argument("--adjoint-case", default=None, metavar="WxHxSPP",
@@ -801,6 +862,8 @@ def main():
         run_blas(args)
     elif args.workload == "upscale":
         run_upscale(args)
+    elif args.workload == "temporal":
+        run_temporal(args)
     else:
         run_gpu(args)
 
