@@ -312,12 +312,12 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * persistent grid (resident blocks x SMs) its wave kernels launch with, so
  * that jobs of one batch share the SMs; wave_cap: paths advanced together per
  * wave (queue capacity), 0 = 2^25; shade_block: threads per block of the
- * shading kernel (64, 128 or 256, 0 = 128); sort_rays: 1 groups each level's
+ * shading kernel (64, 128 or 256, 0 = 256); sort_rays: 1 groups each level's
  * extension rays by direction octant before they are traced, 0 keeps them in
  * pixel order (results are the same either way); fetch_batch: in the ray
  * kernels, the lanes of a warp whose rays are done wait until this many are
  * (or the whole warp is) and then store their results and fetch their next
- * rays together (1 .. 32, 0 = 8; results are the same for every value). */
+ * rays together (1 .. 32, 0 = 6; results are the same for every value). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;

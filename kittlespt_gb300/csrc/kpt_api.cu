@@ -188,8 +188,12 @@ static constexpr long long WAVE_CAP = 1LL << 25;
 // device memory for one wave of the wavefront adjoint's vertex records
 static constexpr size_t ADJ_WAVE_BYTES = (size_t)12 << 30;
 // finished lanes of a warp that store results and fetch rays together
-// (kpt_tuning.fetch_batch): 8 measured best on the 1080p16 frame (4..12 within 1.5%)
-static constexpr int FETCH_BATCH = 8;
+// (kpt_tuning.fetch_batch): 6 measured best on the 1080p16 frame with shading
+// blocks of 256 (22.34 ms; 8: 22.45, 4: 22.55, 12: 22.85)
+static constexpr int FETCH_BATCH = 6;
+// threads per block of the shading kernel unless tuned (256: 22.48 ms on the
+// 1080p16 frame against 22.51 with 128 and 64)
+static constexpr int SHADE_BLOCK = SHADE_MAX_BLOCK;
 
 extern "C" {
 
@@ -957,7 +961,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
     k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
     c->launches += 3;
-    const int shade_block = c->tuning.shade_block > 0 ? c->tuning.shade_block : PATH_BLOCK;
+    const int shade_block = c->tuning.shade_block > 0 ? c->tuning.shade_block : SHADE_BLOCK;
     const bool wide = shade_block > PATH_BLOCK;
     const void* shade_fn = wide ? (const void*)k_shade_wide : (const void*)k_shade;
     const int g_shade = persistent_grid(c, shade_fn, shade_block);
@@ -1552,7 +1556,7 @@ kpt_status kpt_launch_count(kpt_context* c, uint64_t* n) {
 void kpt_tuning_default(kpt_tuning* t) {
     t->grid_scale = 1.0f;
     t->wave_cap = 0;
-    t->shade_block = PATH_BLOCK;
+    t->shade_block = SHADE_BLOCK;
     t->sort_rays = 0;
     t->fetch_batch = FETCH_BATCH;
 }
@@ -1569,7 +1573,7 @@ kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
     if (t->fetch_batch < 0 || t->fetch_batch > 32)
         return fail(KPT_ERR_INVALID, "kpt_set_tuning: fetch_batch must be in [0, 32]");
     c->tuning = *t;
-    if (c->tuning.shade_block == 0) c->tuning.shade_block = PATH_BLOCK;
+    if (c->tuning.shade_block == 0) c->tuning.shade_block = SHADE_BLOCK;
     if (c->tuning.fetch_batch == 0) c->tuning.fetch_batch = FETCH_BATCH;
     c->view.fetch_batch = c->tuning.fetch_batch;
     return KPT_OK;
