@@ -130,7 +130,7 @@ struct EasuKernel {
 
 // FsrEasuCon (upscale.cuh:18-62) with the render size as viewport and
 // input size, on the host (IEEE float divisions and the reference's double
-// expressions, the same on every host this builds for)
+// expressions, the same on x86-64 and aarch64 hosts)
 EasuCon easu_constants(int sw, int sh, int dw, int dh) {
     const float inw = (float)sw, inh = (float)sh, ow = (float)dw, oh = (float)dh;
     EasuCon c;

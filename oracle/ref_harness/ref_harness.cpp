@@ -7,7 +7,8 @@
 // mirrors a reference host routine or kernel body and says which; the C ABI
 // matches the oracle's so that tests/golden/make_golden.py can call both the
 // same way.  The reference has no tests and no golden vectors of its own, so
-// the fixtures under tests/golden/ are generated from this build.
+// the fixtures under tests/golden/ are generated from this harness compiled
+// with the reference's sources.
 //
 // The scene set-up replays Renderer::loadScene (renderer.cu:356-436) followed
 // by Renderer::setMeshTransform (renderer.cu:250-269) for every mesh, with one
