@@ -958,7 +958,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s);
     stage_mark(c, KPT_STAGE_CAMERA);
     k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
-    k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
+    k_primary<<<primary_blocks(c->W, c->H), PATH_BLOCK, 0, s>>>(F);
     k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
     c->launches += 3;
     const int shade_block = c->tuning.shade_block > 0 ? c->tuning.shade_block : SHADE_BLOCK;
@@ -1662,7 +1662,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
     k_adjoint_constants<<<1, 32, 0, c->side>>>(F, A);
     KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
-    k_primary<<<(np + PATH_BLOCK - 1) / PATH_BLOCK, PATH_BLOCK, 0, s>>>(F);
+    k_primary<<<primary_blocks(c->W, c->H), PATH_BLOCK, 0, s>>>(F);
     k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);
     c->launches += 4;
     if (rec) {

@@ -9,6 +9,8 @@ namespace kpt {
 constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
 constexpr int SHADE_MAX_BLOCK = 256;   // largest block k_shade is launched with (kpt_tuning.shade_block)
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
+// blocks of k_primary: one per 16 x 8 tile of the image (PATH_BLOCK = 128)
+inline int primary_blocks(int W, int H) { return ((W + 15) / 16) * ((H + 7) / 8); }
 #ifndef KPT_TRACE_MIN_BLOCKS
 #define KPT_TRACE_MIN_BLOCKS 8
 #endif

@@ -37,20 +37,27 @@ namespace kpt {
 // ---------------------------------------------------------------------------
 // camera rays: one per pixel per frame
 
+// A block covers a 16 x 8 tile of pixels, each warp an 8 x 4 part of it, so
+// that a warp's camera rays are neighbours in both directions (the launch
+// has primary_blocks(W, H) blocks of PATH_BLOCK threads).
 __global__ void __launch_bounds__(PATH_BLOCK) k_primary(FrameParams F) {
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
-    const int npix = F.W * F.H;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tiles_x = (F.W + 15) / 16;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x = (blockIdx.x % tiles_x) * 16 + (w & 1) * 8 + (lane & 7);
+    const int y = (blockIdx.x / tiles_x) * 8 + (w >> 1) * 4 + (lane >> 3);
+    const bool in = x < F.W && y < F.H;
+    const int p = y * F.W + x;
     Hit h;
     h.inst = -1;
     XRay r;
-    if (p < npix) {
-        r = camera_ray(F, p % F.W, p / F.W);
+    if (in) {
+        r = camera_ray(F, x, y);
         h = trace_closest(F.scene, r, 0.0f, __int_as_float(0x7f800000), st, stack);
     }
-    const bool hit = p < npix && h.inst >= 0;
-    const bool miss = p < npix && h.inst < 0;
+    const bool hit = in && h.inst >= 0;
+    const bool miss = in && h.inst < 0;
     int j = warp_append(hit, F.counts);
     int m = warp_append(miss, F.counts + 1);
     if (hit) {
@@ -81,9 +88,9 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary(FrameParams F) {
         if (F.vis) F.vis[p] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7f800000));
     }
     flush_stats(st, F.counters ? F.counters + 4 : nullptr);
-    if (F.counters && threadIdx.x == 0) {   // camera rays of this block
-        const int first_px = blockIdx.x * blockDim.x;
-        const int nb = min((int)blockDim.x, npix - first_px);
+    if (F.counters && threadIdx.x == 0) {   // camera rays of this block: its tile inside the image
+        const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+        const int nb = min(16, F.W - tx * 16) * min(8, F.H - ty * 8);
         if (nb > 0) atomicAdd(F.counters + 14, (unsigned long long)nb);
     }
 }
