@@ -173,8 +173,9 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
     for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
          it += (long long)gridDim.x * blockDim.x) {
         const int item = (int)it;
-        const int ks = item / nhit;
-        const int p = F.hit_list[item - ks * nhit];
+        const int hj = item / F.nsamples;   // items are pixel-major, as in the forward
+        const int ks = item - hj * F.nsamples;
+        const int p = F.hit_list[hj];
         const int x = p % F.W, y = p / F.W;
         Sampler S0;
         S0.init(x, y, F.W, F.sample0 + ks);
@@ -575,10 +576,10 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
         int loc;   // the path's slot in the wave
         PrimaryRec h;
         if (first) {
-            const int nhit = F.counts[0];
-            const long long item = wave0 + i;
-            const int k = (int)(item / nhit);
-            const int p = F.hit_list[item - (long long)k * nhit];
+            const long long item = wave0 + i;   // pixel-major, as in the forward
+            const int hj = (int)(item / F.nsamples);
+            const int k = (int)(item - (long long)hj * F.nsamples);
+            const int p = F.hit_list[hj];
             const int x = p % F.W, y = p / F.W;
             Sampler S0;
             S0.init(x, y, F.W, F.sample0 + k);
@@ -871,8 +872,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjPara
     const float inv_n = 1.0f / (float)F.nsamples;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const long long item = wave0 + i;
-        const int ks = (int)(item / nhit);
-        const int p = F.hit_list[item - (long long)ks * nhit];
+        const int p = F.hit_list[item / F.nsamples];
         const float4 e0 = A.vend[2 * (size_t)i], e1 = A.vend[2 * (size_t)i + 1];
         const int nv = __float_as_int(e0.w);
         const bool escaped = __float_as_int(e1.w) != 0;

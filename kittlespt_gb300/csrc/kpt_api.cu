@@ -1252,6 +1252,7 @@ static void enqueue_temporal(kpt_context* c, const FrameParams& F) {
     for (int k = 0; k < F.nsamples; ++k) {
         const int cam = k == 0 ? 0 : 1;
         T.sample = k;
+        T.nsamples = F.nsamples;
         T.inst = c->tinst.p + (size_t)cam * ni;
         for (int r = 0; r < 4; ++r) T.vp[r] = c->tvp[cam][r];
         T.prev_origin = c->torigin[cam];

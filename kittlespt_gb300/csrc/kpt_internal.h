@@ -72,7 +72,7 @@ struct FrameParams {
     int* miss_list;            // [H*W] pixels whose camera ray misses, compacted
     int* counts;               // [0] hits, [1] misses, [2] queued sky evaluations (zeroed per frame)
     float4* pixel_sky;         // [H*W] sky radiance (times LeSun) of a missing camera ray
-    float4* radiance;          // [nsamples][hits] path radiance before clamping
+    float4* radiance;          // [hits][nsamples] path radiance before clamping (item = hit * nsamples + sample)
     float4* sky_queue;         // [2 per entry] (item bits, direction), (throughput, 0)
     // the wave: up to `cap` paths advanced one level per launch triple
     PathRec* paths[2];         // [cap] paths entering even / odd levels
@@ -197,11 +197,11 @@ struct TemporalInst {
 // One reference frame of the temporal path: the clamped sample `sample` of
 // every pixel blended into hist_in reprojected, written to hist_out.
 struct TemporalParams {
-    int W, H, sample;
+    int W, H, sample, nsamples;
     const int* counts;         // [0]: camera rays that hit (slots of a sample in `radiance`)
     const int* hit_index;      // pixel -> hit slot, -1: the camera ray missed
     const PrimaryRec* primary; // per pixel: first hit (instance)
-    const float4* radiance;    // [nsamples][nhit] path radiance
+    const float4* radiance;    // [nhit][nsamples] path radiance
     const float4* pixel_sky;   // per pixel: the sky of a missing camera ray
     const float4* vis;         // per pixel: visible surface position, distance
     const TemporalInst* inst;

@@ -166,10 +166,12 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
         int item;
         PrimaryRec h;
         if (first) {
-            const int nhit = F.counts[0];
+            // items are pixel-major: the samples of one camera hit are
+            // neighbours (one surface point, one material)
             item = (int)(wave0 + i);
-            const int k = item / nhit;
-            const int p = F.hit_list[item - k * nhit];
+            const int hj = item / F.nsamples;
+            const int k = item - hj * F.nsamples;
+            const int p = F.hit_list[hj];
             const int x = p % F.W, y = p / F.W;
             Sampler S0;
             S0.init(x, y, F.W, F.sample0 + k);

@@ -34,11 +34,10 @@ __global__ void k_accumulate(FrameParams F) {
     const int npix = F.W * F.H;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
-    const int nhit = F.counts[0];
-    const int j = F.hit_index[p];
+    const int j = F.hit_index[p];   // radiance is pixel-major: hit j's samples are contiguous
     float4 acc = F.acc ? F.acc[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int k = 0; k < F.nsamples; ++k) {
-        float4 L = j < 0 ? F.pixel_sky[p] : F.radiance[(size_t)k * nhit + j];
+        float4 L = j < 0 ? F.pixel_sky[p] : F.radiance[(size_t)j * F.nsamples + k];
         if (isnan(L.x) || isnan(L.y) || isnan(L.z) || isinf(L.x) || isinf(L.y) || isinf(L.z))
             L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         else
@@ -91,7 +90,7 @@ __global__ void k_temporal(TemporalParams T) {
     if (p >= npix) return;
     const int x = p % T.W, y = p / T.W;
     const int j = T.hit_index[p];
-    const float4 curr = clamp_sample(j < 0 ? T.pixel_sky[p] : T.radiance[(size_t)T.sample * T.counts[0] + j]);
+    const float4 curr = clamp_sample(j < 0 ? T.pixel_sky[p] : T.radiance[(size_t)j * T.nsamples + T.sample]);
     const float4 vs = T.vis[p];
     if (T.depth_out) T.depth_out[p] = vs.w;
     float4 out = make_float4(curr.x, curr.y, curr.z, 0.0f);
