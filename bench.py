@@ -269,7 +269,7 @@ def run_gpu(args):
     # DRAM bytes per frame of each ray kernel from one ncu capture of the
     # 960x540x8 case (profiles/wave_kernels_960x540x8.md), scaled by samples
     # (x8) to this workload
-    traffic = {"extend": (246.4e6 + 19.9e6) * 8.0, "shadow": (131.6e6 + 1.2e6) * 8.0}
+    traffic = {"extend": (245.6e6 + 20.1e6) * 8.0, "shadow": (128.9e6 + 0.9e6) * 8.0}
     dom = max(kern, key=lambda k: stage_ms[k])
     kname, pre = kern[dom]
     rays_frame = delta("camera_rays") + delta("path_rays") + delta("shadow_rays")
