@@ -317,7 +317,7 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * pixel order (results are the same either way); fetch_batch: in the ray
  * kernels, the lanes of a warp whose rays are done wait until this many are
  * (or the whole warp is) and then store their results and fetch their next
- * rays together (1 .. 32, 0 = 6; results are the same for every value). */
+ * rays together (1 .. 32, 0 = 7; results are the same for every value). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;

@@ -188,9 +188,10 @@ static constexpr long long WAVE_CAP = 1LL << 25;
 // device memory for one wave of the wavefront adjoint's vertex records
 static constexpr size_t ADJ_WAVE_BYTES = (size_t)12 << 30;
 // finished lanes of a warp that store results and fetch rays together
-// (kpt_tuning.fetch_batch): 6 measured best on the 1080p16 frame with shading
-// blocks of 256 (22.34 ms; 8: 22.45, 4: 22.55, 12: 22.85)
-static constexpr int FETCH_BATCH = 6;
+// (kpt_tuning.fetch_batch): 7 measured best on the 1080p16 frame with
+// pixel-major waves and shading blocks of 256 (20.51 ms; 6: 20.55-20.60, 8:
+// 20.53, 5: 20.65, 4: 20.83)
+static constexpr int FETCH_BATCH = 7;
 // threads per block of the shading kernel unless tuned (256: 22.48 ms on the
 // 1080p16 frame against 22.51 with 128 and 64)
 static constexpr int SHADE_BLOCK = SHADE_MAX_BLOCK;
