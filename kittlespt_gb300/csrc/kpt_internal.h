@@ -9,8 +9,13 @@ namespace kpt {
 constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
 constexpr int SHADE_MAX_BLOCK = 256;   // largest block k_shade is launched with (kpt_tuning.shade_block)
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
-// blocks of k_primary: one per 16 x 8 tile of the image (PATH_BLOCK = 128)
-inline int primary_blocks(int W, int H) { return ((W + 15) / 16) * ((H + 7) / 8); }
+// k_primary: a warp traces a TILE_W x (32 / TILE_W) tile of pixels, a
+// block of PATH_BLOCK = 128 threads a 2 x 2 arrangement of them
+#ifndef KPT_TILE_W
+#define KPT_TILE_W 8
+#endif
+constexpr int TILE_W = KPT_TILE_W, TILE_H = 32 / KPT_TILE_W;
+inline int primary_blocks(int W, int H) { return ((W + 2 * TILE_W - 1) / (2 * TILE_W)) * ((H + 2 * TILE_H - 1) / (2 * TILE_H)); }
 #ifndef KPT_TRACE_MIN_BLOCKS
 #define KPT_TRACE_MIN_BLOCKS 8
 #endif

@@ -37,16 +37,17 @@ namespace kpt {
 // ---------------------------------------------------------------------------
 // camera rays: one per pixel per frame
 
-// A block covers a 16 x 8 tile of pixels, each warp an 8 x 4 part of it, so
-// that a warp's camera rays are neighbours in both directions (the launch
-// has primary_blocks(W, H) blocks of PATH_BLOCK threads).
+// A block covers a 2 TILE_W x 2 TILE_H tile of pixels, each warp a TILE_W x
+// TILE_H part of it, so that a warp's camera rays are neighbours in both
+// directions (the launch has primary_blocks(W, H) blocks of PATH_BLOCK
+// threads).
 __global__ void __launch_bounds__(PATH_BLOCK) k_primary(FrameParams F) {
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
-    const int tiles_x = (F.W + 15) / 16;
+    const int tiles_x = (F.W + 2 * TILE_W - 1) / (2 * TILE_W);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x = (blockIdx.x % tiles_x) * 16 + (w & 1) * 8 + (lane & 7);
-    const int y = (blockIdx.x / tiles_x) * 8 + (w >> 1) * 4 + (lane >> 3);
+    const int x = (blockIdx.x % tiles_x) * (2 * TILE_W) + (w & 1) * TILE_W + (lane % TILE_W);
+    const int y = (blockIdx.x / tiles_x) * (2 * TILE_H) + (w >> 1) * TILE_H + (lane / TILE_W);
     const bool in = x < F.W && y < F.H;
     const int p = y * F.W + x;
     Hit h;
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary(FrameParams F) {
     flush_stats(st, F.counters ? F.counters + 4 : nullptr);
     if (F.counters && threadIdx.x == 0) {   // camera rays of this block: its tile inside the image
         const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-        const int nb = min(16, F.W - tx * 16) * min(8, F.H - ty * 8);
+        const int nb = min(2 * TILE_W, F.W - tx * 2 * TILE_W) * min(2 * TILE_H, F.H - ty * 2 * TILE_H);
         if (nb > 0) atomicAdd(F.counters + 14, (unsigned long long)nb);
     }
 }
