@@ -15,9 +15,15 @@ triangle test, 64 B per instance transform, counted in-kernel) over its
 device time (event nodes around each launch in the graph) against the
 measured HBM copy bandwidth.
 
---impl reference times the reference algorithm on the host cores (the CPU
-oracle; the reference's own host build exists only where its source tree
-does), on bounded samples of the same frame.
+The same run times the reference's own CUDA megakernel on the same scene
+(built unmodified for sm_103a with its fast maths from the staged reference
+sources by oracle/build_ref.sh; `megakernel`, `vs_megakernel`) and, as
+`cpu_baseline`, the reference's own code built for the host cores on a
+bounded sample of the frame.
+
+--impl reference times that host build of the reference on all host cores
+(kind "reference"; the oracle port, kind "port", only where the staged
+sources are absent), on bounded samples of the same frame.
 """
 
 from __future__ import annotations
@@ -129,13 +135,25 @@ def full_scene():
     return S.scene_full(W, H, SPP, DEPTH)
 
 
-def cpu_sample_rate(scene, max_seconds=20.0, min_seconds=8.0):
-    """The oracle (FP32 restatement of the reference) on all host cores,
-    rendering bands of rows of the same frame at 1 spp until min_seconds of
-    work; returns Msamples/s, cores, and a description of the sample."""
+def cpu_renderer(scene):
+    """The CPU implementation timed as the baseline: the reference's own
+    path-tracing code built for the host cores (oracle/_ref/libkpt_ref_host.so,
+    kind "reference") where its sources were staged and built, else the
+    oracle, our FP32 restatement of it (kind "port").  Returns (scene handle,
+    kind, note)."""
     from oracle import oracle as O
+    if O.available("ref"):
+        return O.Scene(scene, "ref"), "reference", "reference host build (oracle/_ref/libkpt_ref_host.so)"
+    why = "staged reference sources absent" if not O.ref_staged() else "reference host build missing"
+    return O.Scene(scene), "port", f"oracle port ({why})"
+
+
+def cpu_sample_rate(scene, max_seconds=20.0, min_seconds=8.0):
+    """The CPU baseline on all host cores, rendering bands of rows of the same
+    frame at 1 spp until min_seconds of work; returns Msamples/s, cores, kind
+    and a description of the sample."""
     cores = os.cpu_count() or 1
-    sc = O.Scene(scene)
+    sc, kind, note = cpu_renderer(scene)
     band = 8
     rows_done, t0 = 0, time.perf_counter()
     row = 0
@@ -151,17 +169,49 @@ def cpu_sample_rate(scene, max_seconds=20.0, min_seconds=8.0):
             band = min(band * 2, 256)
     samples = rows_done * W
     rate = samples / el / 1e6
-    return rate, cores, f"{rows_done} rows x {W} px x 1 spp of the {W}x{H} frame ({samples} samples, {el:.1f} s)"
+    return rate, cores, kind, (f"{note}: {rows_done} rows x {W} px x 1 spp of the {W}x{H} frame "
+                               f"({samples} samples, {el:.1f} s)")
+
+
+def megakernel_rate(scene, device, frames=SPP, warmup=2):
+    """The reference's own CUDA megakernel (computePathTraceSamplesMegaKernel,
+    built unmodified for sm_103a with its fast maths by oracle/build_ref.sh
+    gpu) on the same scene: `frames` frames of one sample each (frame index =
+    sample index, as the reference accumulates), each timed with CUDA events
+    around launchPathTraceComputeMegaKernel.  Msamples/s = W*H*frames over
+    the summed kernel time.  Returns a dict, or one with "unavailable"."""
+    from oracle import oracle as O
+    if not O.available("refgpu"):
+        return {"unavailable": "reference GPU build absent (sources not staged)"}
+    t0 = time.perf_counter()
+    try:
+        g = O.RefGpuScene(scene, device)
+    except RuntimeError as e:   # a tree too deep for its 16-entry stacks: nothing was launched
+        return {"unavailable": f"megakernel not run: {e}"}
+    build_s = time.perf_counter() - t0
+    try:
+        depth = g.tree_depth()
+        g.render(0, warmup, clear=True, want_accum=False)
+        with ClockSampler(device) as clk:
+            time.sleep(0.5)
+            _, ms = g.render(0, frames, clear=True, want_accum=False)
+        total = float(np.sum(ms))
+    finally:
+        g.close()
+    return {"value": W * H * frames / (total / 1e3) / 1e6, "unit": "Msamples/s", "frames": frames,
+            "spp_per_frame": 1, "ms_per_frame": total / frames, "kernel": "computePathTraceSamplesMegaKernel",
+            "build": "reference shaders/*.cu unmodified, one translation unit, nvcc -use_fast_math sm_103a",
+            "timing": "CUDA events around each launchPathTraceComputeMegaKernel (8x8 blocks)",
+            "tree_depth": depth, "scene_build_s": build_s, "clocks": clk.summary()}
 
 
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    from oracle import oracle as O
     scene = full_scene()
     cores = os.cpu_count() or 1
-    sc = O.Scene(scene)
+    sc, kind, note = cpu_renderer(scene)
     band = 4
     # size one step to a few seconds
     t0 = time.perf_counter()
@@ -181,12 +231,18 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded procedural scene)",
-           "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH},
-           "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": cores, "kind": "port",
-                            "sample": f"per step {band} rows x {W} px x 1 spp of the {W}x{H} frame"},
+           "data": "synthetic (seeded procedural scene, no reference dataset exists)",
+           "config": config_of(scene, 1),
+           "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": cores, "kind": kind,
+                            "sample": f"{note}: per step {band} rows x {W} px x 1 spp of the {W}x{H} frame"},
            "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def config_of(scene, world):
+    return {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
+            "instances": len(scene.instances), "triangles_expanded": scene.ntris_expanded,
+            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "single"}
 
 
 def run_gpu(args):
@@ -300,16 +356,20 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, cores, desc = cpu_sample_rate(scene)
-        cpu = {"value": rate, "unit": "Msamples/s", "cores": cores, "kind": "port", "sample": desc}
+        rate, cores, kind, desc = cpu_sample_rate(scene)
+        cpu = {"value": rate, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": desc}
+    mega = None
+    if rank == 0 and not args.no_megakernel:
+        mega = megakernel_rate(scene, local)
+        if "value" in mega:
+            print(f"[bench] reference megakernel {mega['ms_per_frame']:.2f} ms per 1-spp frame, "
+                  f"{mega['value']:.1f} Msamples/s", file=sys.stderr)
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (seeded procedural scene, no reference dataset exists)",
-               "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
-                          "instances": len(scene.instances), "triangles_expanded": scene.ntris_expanded,
-                          "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "single"},
+               "config": config_of(scene, world),
                "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
                             "unit": "GB/s", "frac": achieved / peak, "traffic": traffic[dom],
                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per frame, "
@@ -329,6 +389,9 @@ def run_gpu(args):
                                                 "inst_xforms": delta(pre + "_inst_xforms")}
                                             for k, pre in (("extension", "path"), ("shadow", "shadow"))},
                "cpu_baseline": cpu,
+               "megakernel": mega,
+               "megakernel_msamples_s": mega.get("value") if mega else None,
+               "vs_megakernel": value / world / mega["value"] if mega and "value" in mega else None,
                "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 128,
                        "d2h_bytes_per_step": W * H * 16},
                "gpu_launches": int(launches), "traversal_overflows": int(overflow),
@@ -831,6 +894,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-megakernel", action="store_true",
+                    help="skip timing the reference's own CUDA megakernel on the same scene")
     ap.add_argument("--workload", default="frame",
                     choices=["frame", "batch", "adjoint", "traversal", "blas", "upscale", "temporal"],
                     help="frame: the 1080p full-frame metric; batch: 32 mixed jobs, batched vs one by one; "

@@ -256,20 +256,20 @@ kpt_status kpt_trace_bounces_device(kpt_context* ctx, int n, const float* origin
 kpt_status kpt_trace_bounces(kpt_context* ctx, int n, const float* origins, const float* dirs, int nbounces,
                              int32_t* instance, int32_t* triangle, float* t);
 
-/* kpt_trace_bounces for callers that must not allocate device memory: a
- * frame loop that cannot afford the device-wide synchronisation cudaMalloc
- * and cudaFree may cause, an application that reserves all its device memory
- * up front, or code running while another library captures a CUDA graph
- * (allocation is not allowed during capture).  No counterpart in the
- * reference.  Rays and hits are staged through one fixed array of
- * KPT_NOALLOC_STAGING_BYTES inside the library, which every GPU that loads
- * libkpt.so holds until the process exits; n * (24 + 12 * (nbounces + 1))
- * must fit in it, larger requests fail with KPT_ERR_INVALID.  The first call
- * on a device looks the array up on that device, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * (two threads, or two contexts of one device at once) race; a call returns
- * once its hits are in host memory.  Needs a committed scene with no pending
- * transform change (KPT_ERR_STATE otherwise). */
+/* kpt_trace_bounces for callers that must not allocate device memory.  No
+ * counterpart in the reference.  Some callers cannot call cudaMalloc: a frame
+ * loop that must never stall (cudaMalloc and cudaFree can synchronise the
+ * whole device), or an application that reserves a fixed device-memory budget
+ * up front and forbids later growth.  This call allocates nothing: rays and
+ * hits are staged through one fixed array of KPT_NOALLOC_STAGING_BYTES inside
+ * the library, which every GPU that loads libkpt.so holds until the process
+ * exits; n * (24 + 12 * (nbounces + 1)) must fit in it, larger requests fail
+ * with KPT_ERR_INVALID.  The first call on a device looks the array up on
+ * that device, so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (two threads, or two contexts of one
+ * device at once) race; a call returns once its hits are in host memory.
+ * Needs a committed scene with no pending transform change (KPT_ERR_STATE
+ * otherwise).  Returns what kpt_trace_bounces returns. */
 #define KPT_NOALLOC_STAGING_BYTES (8u << 20)
 kpt_status kpt_trace_bounces_noalloc(kpt_context* ctx, int n, const float* origins, const float* dirs, int nbounces,
                                      int32_t* instance, int32_t* triangle, float* t);

@@ -2050,12 +2050,11 @@ kpt_status kpt_autotune_batch(kpt_batch* b, int n, kpt_context* const* jobs, con
 // kpt_trace_bounces stages the caller's host rays and hits in device buffers
 // it allocates with cudaMalloc on every call.  Some callers cannot do that:
 // a frame loop that must never stall (cudaMalloc and cudaFree can
-// synchronise the whole device), an application that reserves its device
-// memory up front and forbids later growth, or code that runs while another
-// library is capturing a CUDA graph on the device (allocation calls are not
-// allowed during capture).  kpt_trace_bounces_noalloc serves them: the
-// staging lives in one fixed array below, part of the library's device image,
-// so every GPU that loads libkpt.so holds these 8 MiB until the process exits.
+// synchronise the whole device), or an application that reserves its device
+// memory up front and forbids later growth.  kpt_trace_bounces_noalloc
+// serves them: the staging lives in one fixed array below, part of the
+// library's device image, so every GPU that loads libkpt.so holds these
+// 8 MiB until the process exits.
 //
 // The array is shared by every call in the process and keeps the last call's
 // contents; nothing in it has to start at zero (the inputs are copied in and
@@ -2100,8 +2099,11 @@ extern "C" kpt_status kpt_trace_bounces_noalloc(kpt_context* c, int n, const flo
     if (!c->committed) return fail(KPT_ERR_STATE, "no committed scene");
     if (c->tlas_dirty)   // rebuilding the TLAS could grow a device buffer
         return fail(KPT_ERR_STATE, "kpt_trace_bounces_noalloc: instance transforms changed; render or trace once first");
-    const size_t per_ray = 24 + size_t(nb + 1) * 12;   // origin + direction in, (instance, triangle, t) per bounce out
-    if ((size_t)n * per_ray > NOALLOC_BYTES)
+    // origin + direction in, (instance, triangle, t) per bounce out; checked
+    // in an order that cannot overflow: nbounces first, then n against the
+    // bytes one ray takes
+    constexpr size_t max_nb = (NOALLOC_BYTES - 24) / 12 - 1;
+    if ((size_t)nb > max_nb || (size_t)n > NOALLOC_BYTES / (24 + 12 * ((size_t)nb + 1)))
         return fail(KPT_ERR_INVALID, "kpt_trace_bounces_noalloc: n * (24 + 12 * (nbounces + 1)) bytes exceed the "
                                      "8 MiB staging array (KPT_NOALLOC_STAGING_BYTES)");
     if (n == 0) return KPT_OK;
@@ -2109,7 +2111,7 @@ extern "C" kpt_status kpt_trace_bounces_noalloc(kpt_context* c, int n, const flo
     unsigned char* base = nullptr;
     kpt_status st = noalloc_staging(c->device, &base);
     if (st != KPT_OK) return st;
-    const size_t nr = (size_t)n, no = nr * (nb + 1);
+    const size_t nr = (size_t)n, no = nr * ((size_t)nb + 1);
     float* d_o = reinterpret_cast<float*>(base);          // 12 n bytes
     float* d_d = d_o + 3 * nr;                              // 12 n bytes
     int32_t* d_inst = reinterpret_cast<int32_t*>(d_d + 3 * nr);
@@ -2117,8 +2119,14 @@ extern "C" kpt_status kpt_trace_bounces_noalloc(kpt_context* c, int n, const flo
     float* d_t = reinterpret_cast<float*>(d_tri + no);
     KPT_CUDA(cudaMemcpyAsync(d_o, o, 12 * nr, cudaMemcpyHostToDevice, c->stream));
     KPT_CUDA(cudaMemcpyAsync(d_d, d, 12 * nr, cudaMemcpyHostToDevice, c->stream));
-    k_trace_bounces<<<trace_grid(c, (const void*)k_trace_bounces, n), TRACE_BLOCK, 0, c->stream>>>(
-        c->view, n, (const float3*)d_o, (const float3*)d_d, nb, d_inst, d_tri, d_t, c->counters.p);
+    // the launch of kpt_trace_bounces_device: the same kernel and settings, so
+    // both calls return the same hits; the context's chain counter (not part
+    // of the staging array) must start at zero
+    KPT_CUDA(cudaMemsetAsync(c->fetch.p, 0, sizeof(int), c->stream));
+    SceneView v = c->view;
+    v.fetch_batch = 1;
+    k_trace_chains<<<trace_grid(c, (const void*)k_trace_chains, n), TRACE_BLOCK, 0, c->stream>>>(
+        v, n, (const float3*)d_o, (const float3*)d_d, nb, d_inst, d_tri, d_t, c->fetch.p, c->counters.p);
     c->launches += 1;
     KPT_CUDA(cudaGetLastError());
     KPT_CUDA(cudaMemcpyAsync(inst, d_inst, 4 * no, cudaMemcpyDeviceToHost, c->stream));

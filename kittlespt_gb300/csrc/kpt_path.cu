@@ -649,6 +649,13 @@ struct BounceQueue {
     __device__ __forceinline__ void any(int, bool) {}
 };
 
+// Closest hit plus `nbounces` diffuse bounces per ray: cosine-weighted about
+// the geometric normal facing the incoming ray (Malley's method: a uniform
+// unit-disk point, rejection-sampled from pairs of PCG draws seeded with
+// 4 * ray index + bounce, lifted to the hemisphere and rotated by the Frisvad
+// basis), origin offset 1e-3 along the normal.  IEEE arithmetic throughout,
+// so every bounce is bit-identical to the oracle's.  Writes (nbounces+1) x n.
+// The chains run on the queue traversal (BounceQueue above).
 __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_trace_chains(SceneView s, int n, const float3* o,
                                                                               const float3* d, int nbounces, int* inst,
                                                                               int* tri, float* t, int* next,
@@ -657,43 +664,6 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_trace_chains(
     TraceStats st = {0, 0, 0, 0};
     BounceQueue q{o, d, n, nbounces, inst, tri, t, &s, 0, make_float3(0.0f, 0.0f, 0.0f), make_float3(0.0f, 0.0f, 0.0f)};
     trace_queue<false, BounceQueue, 2>(s, n, next, q, st, stack);
-    flush_stats(st, counters);
-}
-
-// Closest hit plus `nbounces` diffuse bounces per ray: cosine-weighted about
-// the geometric normal facing the incoming ray (Malley's method: a uniform
-// unit-disk point, rejection-sampled from pairs of PCG draws seeded with
-// 4 * ray index + bounce, lifted to the hemisphere and rotated by the Frisvad
-// basis), origin offset 1e-3 along the normal.  IEEE arithmetic throughout,
-// so every bounce is bit-identical to the oracle's.  Writes (nbounces+1) x n.
-__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_bounces(SceneView s, int n, const float3* o, const float3* d,
-                                                               int nbounces, int* inst, int* tri, float* t,
-                                                               unsigned long long* counters) {
-    int stack[STACK_WORDS];
-    TraceStats st = {0, 0, 0, 0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        XRay r = make_xray(o[i], d[i]);
-        for (int b = 0; b <= nbounces; ++b) {
-            size_t k = (size_t)b * n + i;
-            Hit h = trace_closest(s, r, 0.0f, __int_as_float(0x7f800000), st, stack);
-            inst[k] = h.inst;
-            tri[k] = h.tri;
-            t[k] = h.t;
-            if (h.inst < 0) {
-                for (int bb = b + 1; bb <= nbounces; ++bb) {
-                    size_t kk = (size_t)bb * n + i;
-                    inst[kk] = -1;
-                    tri[kk] = -1;
-                    t[kk] = __int_as_float(0x7f800000);
-                }
-                break;
-            }
-            if (b == nbounces) break;
-            float3 no, nd;
-            diffuse_bounce(s, h, r.o, r.d, i, b, &no, &nd);
-            r = make_xray(no, nd);
-        }
-    }
     flush_stats(st, counters);
 }
 

@@ -431,8 +431,18 @@ def scene_small(width=256, height=256, spp=1, max_depth=4, seed=1):
                  name="sphere_pair_256")
 
 
+# Value-noise seeds of the five icosphere variants of the full-frame scene.
+# Among seeds 1000-1999 these are the first five whose subdivision-6 mesh
+# gets a BLAS (binned SAH, leaves of at most 8 triangles) with no interior
+# node deeper than 14: the reference's traversal keeps 16-entry stacks
+# (shaders/blas.cuh:37, shaders/tlas.cuh:10) and pushes both children of an
+# interior node of depth d onto at most d pending entries, so these trees
+# never overflow them.  Most seeds give depth 15.
+FULL_FRAME_VARIANT_SEEDS = (1019, 1081, 1160, 1232, 1321)
+
+
 def scene_full(width=1920, height=1080, spp=16, max_depth=8, seed=2,
-               n_variants=5, subdiv=6, grid=8, n_lights=16):
+               n_variants=5, subdiv=6, grid=8, n_lights=16, variant_seeds=None):
     """Full-frame plain-method scene: 5 displaced icospheres (subdivision 6,
     81,920 triangles each, value-noise amplitude 0.1), 64 instances on an 8x8
     grid with spacing 3, random yaw U(0, 2pi) and scale U(0.5, 1.5),
@@ -442,9 +452,11 @@ def scene_full(width=1920, height=1080, spp=16, max_depth=8, seed=2,
     on a 4x4 grid at height 3; Nishita sky and sun (default sun angles);
     post chain with 6-level bloom, auto exposure and AgX.  The camera sits at
     (0, 4, 22) looking at (0, 1, 0) with a 45 deg field of view, so that the
-    upper part of the frame shows the sky above the horizon."""
+    upper part of the frame shows the sky above the horizon.  The variants'
+    noise seeds are ``variant_seeds`` (default FULL_FRAME_VARIANT_SEEDS)."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    meshes = [displaced_icosphere(subdiv, 0.1, seed=1000 + k) for k in range(n_variants)]
+    vs = FULL_FRAME_VARIANT_SEEDS if variant_seeds is None else variant_seeds
+    meshes = [displaced_icosphere(subdiv, 0.1, seed=vs[k]) for k in range(n_variants)]
     meshes.append(quad(0.5, 0.5, 0.0, facing_up=False, mat_id=0))
     light_mesh = len(meshes) - 1
     mats = []

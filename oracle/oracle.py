@@ -3,8 +3,10 @@
 Loads ``oracle/libkpt_oracle.so`` (our FP32 restatement of the reference hot
 path, built by ``oracle/build_oracle.sh``) or, with ``prefix="ref"``,
 ``oracle/_ref/libkpt_ref_host.so`` (the reference's own code compiled for the
-host by ``oracle/build_ref.sh``; only where the reference tree exists).  Both
-export the same C ABI, so every helper below drives either one.
+host by ``oracle/build_ref.sh`` from its staged sources).  Both export the
+same C ABI, so every helper below drives either one.  ``RefGpuScene`` drives
+``oracle/_ref/libkpt_ref_gpu.so``: the reference's own CUDA megakernel, built
+for the GPU by ``oracle/build_ref.sh gpu``.
 
 Only tests, the smoke check and the benchmark's CPU-baseline leg use this
 module; the product path (``kittlespt_gb300``) never imports it.
@@ -22,6 +24,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libkpt_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libkpt_ref_host.so")
+REF_GPU_SO = os.path.join(HERE, "_ref", "libkpt_ref_gpu.so")
+REF_SRC = os.path.join(HERE, "_ref", "src", "KittlesPT", "src", "shaders")
 
 _f = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -34,14 +38,21 @@ _v = C.c_void_p
 _libs = {}
 
 
-def build(ref: bool = False) -> None:
-    script = "build_ref.sh" if ref else "build_oracle.sh"
-    subprocess.run(["sh", os.path.join(HERE, script)], check=True,
-                   stdout=subprocess.DEVNULL)
+def build(ref: bool = False, what: str = "all") -> None:
+    """Builds the oracle, or with ref=True the reference's own code
+    (build_ref.sh `what`: stage, host, gpu or all)."""
+    cmd = ["sh", os.path.join(HERE, "build_ref.sh"), what] if ref else ["sh", os.path.join(HERE, "build_oracle.sh")]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+
+
+def ref_staged() -> bool:
+    """True where the reference's sources have been staged for building."""
+    return os.path.isdir(REF_SRC)
 
 
 def available(prefix: str = "orc") -> bool:
-    return os.path.exists(REF_SO if prefix == "ref" else ORACLE_SO)
+    path = {"ref": REF_SO, "refgpu": REF_GPU_SO}.get(prefix, ORACLE_SO)
+    return os.path.exists(path)
 
 
 def lib(prefix: str = "orc"):
@@ -379,3 +390,114 @@ def adjoint_estimate(records: bytes, n: int, albedo, roughness, sky, fixed):
     out = np.zeros(1, np.float64)
     items = L.orc_adjoint_estimate(_ptr(buf), n, _ptr(a), _ptr(r), _ptr(s), _ptr(f), _ptr(out))
     return float(out[0]), int(items)
+
+
+class RefGpuScene:
+    """The reference's own CUDA megakernel on the GPU, over a scene in its
+    layout (oracle/_ref/libkpt_ref_gpu.so, built by ``build_ref.sh gpu``).
+    Construction raises RuntimeError if a tree is deeper than the reference's
+    16-entry traversal stacks allow; no kernel has run then."""
+
+    _L = None
+
+    @classmethod
+    def lib(cls):
+        if cls._L is None:
+            if not os.path.exists(REF_GPU_SO):
+                raise FileNotFoundError(REF_GPU_SO)
+            L = C.CDLL(REF_GPU_SO)
+            L.refgpu_last_error.restype = C.c_char_p
+            L.refgpu_scene_create.restype = _v
+            L.refgpu_scene_create.argtypes = [C.c_int, C.c_int, _f, _f, _f, _i, C.c_int, _i, _i, _f, C.c_int, _v,
+                                              C.c_int, _v, C.c_longlong, _v]
+            L.refgpu_scene_destroy.argtypes = [_v]
+            L.refgpu_tree_depth.argtypes = [_v, _i]
+            L.refgpu_render.restype = C.c_int
+            L.refgpu_render.argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _v, _v]
+            L.refgpu_first_hits.restype = C.c_int
+            L.refgpu_first_hits.argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, _i, _i, _f]
+            cls._L = L
+        return cls._L
+
+    def __init__(self, scene, device: int = 0):
+        L = self.lib()
+        ex = scene.expanded()
+        self._keep = ex
+        self.materials = np.ascontiguousarray(scene.materials)
+        tex = getattr(scene, "textures", None)
+        targs = (0, None, 0, None)
+        if tex:
+            desc, pix = scene.texture_arrays()
+            self._tex = (desc, pix)
+            targs = (len(tex), _ptr(desc), int(pix.size), _ptr(pix))
+        n = int(ex["positions"].shape[0])
+        self.h = L.refgpu_scene_create(device, n, ex["positions"].reshape(-1), ex["normals"].reshape(-1),
+                                       ex["uvs"].reshape(-1), ex["material"], len(ex["mesh_offset"]),
+                                       ex["mesh_offset"], ex["mesh_count"],
+                                       np.ascontiguousarray(np.transpose(ex["models"], (0, 2, 1))).reshape(-1),
+                                       len(self.materials), _ptr(self.materials), *targs)
+        if not self.h:
+            raise RuntimeError(L.refgpu_last_error().decode())
+        self.scene = scene
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib().refgpu_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tree_depth(self):
+        out = np.zeros(2, np.int32)
+        self.lib().refgpu_tree_depth(self.h, out)
+        return dict(blas=int(out[0]), tlas=int(out[1]))
+
+    def _view(self, max_depth):
+        sc = self.scene
+        st = sc.settings.copy()
+        if max_depth is not None:
+            st["max_depth"] = max_depth
+        ip = np.ascontiguousarray(sc.camera.inv_proj.T, np.float32).reshape(-1)
+        iv = np.ascontiguousarray(sc.camera.inv_view.T, np.float32).reshape(-1)
+        env = np.ascontiguousarray(sc.env)
+        self._st = (st, env)
+        return ip, iv, _ptr(env), _ptr(st)
+
+    def render(self, frame0=0, nframes=1, clear=True, max_depth=None, want_accum=True):
+        """Frames frame0 .. frame0+nframes-1 (one sample per pixel each, the
+        reference's frame index = the sample index).  Returns (accumulation
+        [H][W][4] or None, kernel milliseconds per frame)."""
+        sc = self.scene
+        ip, iv, env, st = self._view(max_depth)
+        acc = np.zeros((sc.height, sc.width, 4), np.float32) if want_accum else None
+        ms = np.zeros(max(nframes, 1), np.float32)
+        rc = self.lib().refgpu_render(self.h, ip, iv, env, st, sc.width, sc.height, frame0, nframes, int(clear),
+                                      _ptr(acc) if acc is not None else None, _ptr(ms))
+        if rc != 0:
+            raise RuntimeError(self.lib().refgpu_last_error().decode())
+        return acc, ms[:nframes]
+
+    def render_samples(self, sample0=0, nsamples=1, max_depth=None):
+        """Per-sample clamped radiance [nsamples][H][W][3]: each sample is one
+        frame rendered into a cleared accumulation."""
+        sc = self.scene
+        out = np.zeros((nsamples, sc.height, sc.width, 3), np.float32)
+        for k in range(nsamples):
+            acc, _ = self.render(sample0 + k, 1, clear=True, max_depth=max_depth)
+            out[k] = acc[..., :3]
+        return out
+
+    def first_hits(self):
+        sc = self.scene
+        ip, iv, env, st = self._view(None)
+        prim = np.zeros((sc.height, sc.width), np.int32)
+        inst = np.zeros_like(prim)
+        t = np.zeros((sc.height, sc.width), np.float32)
+        rc = self.lib().refgpu_first_hits(self.h, ip, iv, env, st, sc.width, sc.height, prim, inst, t)
+        if rc != 0:
+            raise RuntimeError(self.lib().refgpu_last_error().decode())
+        return dict(prim=prim, inst=inst, t=t)

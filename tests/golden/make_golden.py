@@ -43,7 +43,7 @@ def small_scene():
 
 
 def full_scene():
-    return S.scene_full(64, 36, 2, 8, n_variants=2, subdiv=3, grid=3, n_lights=4)
+    return S.scene_full(64, 36, 2, 8, n_variants=2, subdiv=3, grid=3, n_lights=4, variant_seeds=(1000, 1001))
 
 
 def traversal_scene():
