@@ -131,8 +131,13 @@ class ClockSampler:
 
 
 def full_scene():
+    """The full-frame workload, its sky in the arithmetic of the reference's
+    GPU build (kpt_settings.sky_arith = 1), the build whose megakernel it is
+    compared with."""
     from kittlespt_gb300 import scenes as S
-    return S.scene_full(W, H, SPP, DEPTH)
+    sc = S.scene_full(W, H, SPP, DEPTH)
+    sc.sky_arith = 1
+    return sc
 
 
 def cpu_renderer(scene):

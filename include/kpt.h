@@ -85,11 +85,24 @@ typedef struct kpt_settings {
     int32_t bloom, karis, auto_exposure;
     float bloom_final_blend, bloom_internal_blend;
     float frame_delta_ms;
-    int32_t rng_order;         /* argument order of the reference's paired RNG draws: 0 left-to-right, 1 right-to-left */
+    int32_t rng_order;         /* argument evaluation order of the reference's three calls that draw
+                                  two random values in one expression, a set bit meaning right to
+                                  left: 1 = make_float2(get1D(), get1D()) (samplers.cuh:37-40),
+                                  2 = the sun-disc offset (integrator.cuh:155), 4 = the BSDF
+                                  sample's two pairs (integrator.cuh:382); the reference's GPU
+                                  build: 0 (the default), its host build: 7 */
     int32_t temporal_accumulation;
     int32_t postprocess_effects;
     int32_t upscale;
-    int32_t pad;
+    int32_t sky_arith;         /* arithmetic of the Nishita sky and the sun's constants: 1 (the
+                                  default) that of the reference's GPU build -- fast square root,
+                                  division and exponentials, contracted products, fast sine, cosine
+                                  and tangent for the sun -- so that sky values agree with its
+                                  megakernel's; 0 IEEE single precision, as its host build computes
+                                  them.  The sky's altitudes are lengths of ~6.4e6 m vectors (0.5 m
+                                  per ulp against a 1200 m Mie scale height), so the two differ by
+                                  up to ~1e-2 relative in places.  The path-replay adjoint always
+                                  uses IEEE. */
 } kpt_settings;
 
 /* ExposureValues (pod_types.hpp:9-33) with the compensation and white/black

@@ -46,7 +46,7 @@ class Settings(C.Structure):
                 ("auto_exposure", C.c_int32), ("bloom_final_blend", C.c_float),
                 ("bloom_internal_blend", C.c_float), ("frame_delta_ms", C.c_float), ("rng_order", C.c_int32),
                 ("temporal_accumulation", C.c_int32), ("postprocess_effects", C.c_int32), ("upscale", C.c_int32),
-                ("pad", C.c_int32)]
+                ("sky_arith", C.c_int32)]
 
 
 class Exposure(C.Structure):

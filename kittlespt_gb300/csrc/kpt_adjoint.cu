@@ -254,13 +254,13 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
                     const float3 sun_pos = make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
                                                        __fmul_rn(P.sun_dir.z, dsun));
                     float3 off;
-                    if (order == 0) {
-                        float2 a = S.get2D(0);
+                    if ((order & RNG_SUN) == 0) {
+                        float2 a = S.get2D(order);
                         float b = S.get1D();
                         off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                     } else {
                         float b = S.get1D();
-                        float2 a = S.get2D(1);
+                        float2 a = S.get2D(order);
                         off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                     }
                     const float3 target = make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
@@ -368,8 +368,8 @@ __device__ __forceinline__ void adjoint_items(const FrameParams& F, const AdjPar
             const int vi = nv++;
             if (level == F.max_depth || nv == MV) break;
             float2 uu, X;
-            if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
-            else { X = S.get2D(1); uu = S.get2D(1); }
+            if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
+            else { X = S.get2D(order); uu = S.get2D(order); }
             FGrad sg;
             SampleInfo sinfo;
             BsdfSample bs = bsdf_sample_grad(bsdf, wo, uu, X, sg, sinfo);
@@ -658,13 +658,13 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
             bool eval = false;
             if (sun) {
                 float3 off;
-                if (order == 0) {
-                    float2 a = S.get2D(0);
+                if ((order & RNG_SUN) == 0) {
+                    float2 a = S.get2D(order);
                     float b = S.get1D();
                     off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                 } else {
                     float b = S.get1D();
-                    float2 a = S.get2D(1);
+                    float2 a = S.get2D(order);
                     off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                 }
                 target = make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
@@ -751,8 +751,8 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjPara
         bool go = false;
         if (level < F.max_depth && nv < MV) {
             float2 uu, X;
-            if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
-            else { X = S.get2D(1); uu = S.get2D(1); }
+            if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
+            else { X = S.get2D(order); uu = S.get2D(order); }
             FGrad sg;
             SampleInfo sinfo;
             BsdfSample bs = bsdf_sample_grad(bsdf, wo, uu, X, sg, sinfo);

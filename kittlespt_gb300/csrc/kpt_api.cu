@@ -143,6 +143,12 @@ struct kpt_context {
     float thr_black = NAN, thr_white = NAN;
     DBuf<ExposureState> expo_state;
     DBuf<float3> sun_radiance;
+    // the sun's constants in the reference GPU build's arithmetic (direction,
+    // LeSun threshold, disc radius), computed on the device for sun_env
+    DBuf<float> sun_gpu_dev;
+    float sun_gpu[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    bool sun_gpu_valid = false;
+    kpt_environment sun_env{};
     cudaGraphExec_t graph_exec = nullptr;
     // work buffers of the path stage
     DBuf<PrimaryRec> primary, hits;
@@ -227,7 +233,7 @@ void kpt_settings_default(kpt_settings* s) {   // pod_types.hpp:46-57
     s->temporal_accumulation = 0;
     s->postprocess_effects = 0;
     s->upscale = 0;
-    s->pad = 0;
+    s->sky_arith = 1;
 }
 
 void kpt_exposure_default(kpt_exposure* e) {   // SampleApp camera_controller.hpp:55-60
@@ -243,6 +249,8 @@ void kpt_exposure_default(kpt_exposure* e) {   // SampleApp camera_controller.hp
     e->min_shutter = 1.0f / 400.0f;
     e->pad0 = e->pad1 = 0.0f;
 }
+
+static kpt_status sun_constants_gpu(kpt_context* c);
 
 kpt_status kpt_create(int device, kpt_context** out) {
     if (!out) return fail(KPT_ERR_INVALID, "kpt_create: null output");
@@ -275,6 +283,11 @@ kpt_status kpt_create(int device, kpt_context** out) {
     }
     cudaMemsetAsync(c->expo_state.p, 0, sizeof(ExposureState), c->stream);
     cudaMemsetAsync(c->counters.p, 0, 16 * sizeof(unsigned long long), c->stream);
+    if (sun_constants_gpu(c) != KPT_OK) {
+        std::string why = kpt_last_error();
+        kpt_destroy(c);
+        return fail(KPT_ERR_CUDA, "kpt_create: " + why);
+    }
     *out = c;
     return KPT_OK;
 }
@@ -796,6 +809,10 @@ kpt_status kpt_set_environment(kpt_context* c, const kpt_environment* e) {
     if (!c || !e) return fail(KPT_ERR_INVALID, "kpt_set_environment: null argument");
     if (!(e->rayleigh_height > 0.0f) || !(e->mie_height > 0.0f)) return fail(KPT_ERR_INVALID, "kpt_set_environment: scale heights must be positive");
     c->env = *e;
+    if (c->settings.sky_arith) {
+        kpt_status st = sun_constants_gpu(c);
+        if (st != KPT_OK) return st;
+    }
     return clear_accumulation(c);
 }
 kpt_status kpt_get_environment(kpt_context* c, kpt_environment* e) {
@@ -811,10 +828,16 @@ kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
     if (s->postprocess_effects != 0 && s->postprocess_effects != 1)
         return fail(KPT_ERR_INVALID, "kpt_set_settings: postprocess_effects must be 0 or 1");
     if (s->upscale < 0 || s->upscale > 2) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscale must be 0, 1 or 2");
+    if (s->rng_order < 0 || s->rng_order > 7) return fail(KPT_ERR_INVALID, "kpt_set_settings: rng_order must be in 0..7");
+    if (s->sky_arith != 0 && s->sky_arith != 1) return fail(KPT_ERR_INVALID, "kpt_set_settings: sky_arith must be 0 or 1");
     const bool resize = (s->upscale != 0) != (c->settings.upscale != 0) && c->OW > 0;
     c->settings = *s;
     if (resize) {   // the render resolution follows the switch at once
         kpt_status st = apply_resolution(c, c->OW, c->OH);
+        if (st != KPT_OK) return st;
+    }
+    if (c->settings.sky_arith) {
+        kpt_status st = sun_constants_gpu(c);
         if (st != KPT_OK) return st;
     }
     return clear_accumulation(c);
@@ -864,10 +887,40 @@ static SkyParams sky_params(const kpt_environment& e) {
     return P;
 }
 
+// The sun's constants in the arithmetic of the reference's GPU build,
+// computed once per environment with the device's fast functions
+// (k_sun_constants_gpu) and kept on the host.  Synchronises the stream.
+static kpt_status sun_constants_gpu(kpt_context* c) {
+    if (c->sun_gpu_valid && std::memcmp(&c->sun_env, &c->env, sizeof(kpt_environment)) == 0) return KPT_OK;
+    KPT_CUDA(cudaSetDevice(c->device));
+    KPT_CUDA(c->sun_gpu_dev.ensure(5));
+    k_sun_constants_gpu<<<1, 32, 0, c->stream>>>(c->env.sun_phi, c->env.sun_theta, c->env.sun_angular_diameter,
+                                                 c->sun_gpu_dev.p);
+    c->launches += 1;
+    KPT_CUDA(cudaGetLastError());
+    KPT_CUDA(cudaMemcpyAsync(c->sun_gpu, c->sun_gpu_dev.p, sizeof(c->sun_gpu), cudaMemcpyDeviceToHost, c->stream));
+    KPT_CUDA(cudaStreamSynchronize(c->stream));
+    c->sun_env = c->env;
+    c->sun_gpu_valid = true;
+    return KPT_OK;
+}
+
+// The frame's sky parameters in the arithmetic the settings select.
+static SkyParams frame_sky(kpt_context* c) {
+    SkyParams P = sky_params(c->env);
+    P.gpu_arith = c->settings.sky_arith;
+    if (P.gpu_arith && c->sun_gpu_valid) {
+        P.sun_dir = make_float3(c->sun_gpu[0], c->sun_gpu[1], c->sun_gpu[2]);
+        P.cos_half_sun = c->sun_gpu[3];
+        P.sun_radius_m = c->sun_gpu[4];
+    }
+    return P;
+}
+
 static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     FrameParams F{};
     F.scene = c->view;
-    F.sky = sky_params(c->env);
+    F.sky = frame_sky(c);
     rows_of(c->inv_proj, F.inv_proj, 4);
     rows_of(c->inv_view, F.inv_view, 3);
     F.cam_pos = make_float3(c->inv_view[12], c->inv_view[13], c->inv_view[14]);
@@ -1492,7 +1545,7 @@ kpt_status kpt_sky_device(kpt_context* c, int n, const float* dirs, float* rgb) 
     if (!c || n < 0 || (n > 0 && (!dirs || !rgb))) return fail(KPT_ERR_INVALID, "kpt_sky_device: bad arguments");
     KPT_CUDA(cudaSetDevice(c->device));
     if (n == 0) return KPT_OK;
-    k_sky<<<(n + 127) / 128, 128, 0, c->stream>>>(sky_params(c->env), n, (const float3*)dirs, (float3*)rgb);
+    k_sky<<<(n + 127) / 128, 128, 0, c->stream>>>(frame_sky(c), n, (const float3*)dirs, (float3*)rgb);
     c->launches += 1;
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;
@@ -1604,6 +1657,7 @@ static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const f
     // room for every sample's escape and every missing pixel
     const size_t qcap = (size_t)c->W * c->H * ((size_t)nsamples + 1);
     FrameParams F = frame_params(c, sample0, nsamples);
+    F.sky = sky_params(c->env);   // the replay and its Jacobians: IEEE sky arithmetic
     // the wavefront replay's records: a wave of at most ADJ_WAVE_BYTES of them
     const int D = F.max_depth;
     const size_t per_path = sizeof(float4) * ((size_t)AV_FIELDS * (D + 1) + 2) + (size_t)(D + 1);

@@ -121,6 +121,7 @@ struct SkyParams {
     float cos_half_sun;       // LeSun threshold
     float sun_radius_m;       // physical radius of the sun disc at 1 AU
     float3 sun_radiance;      // Nishita radiance towards the sun (constant per frame)
+    int gpu_arith;            // 1: sky and sun in the reference GPU build's arithmetic, 0: IEEE
 };
 
 // ---------------------------------------------------------------------------
@@ -158,6 +159,10 @@ __device__ __forceinline__ float3 operator*(float3 a, float s) { return make_flo
 __device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
 __device__ __forceinline__ float3 operator/(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float3 operator-(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3& operator+=(float3& a, float3 b) {
+    a = a + b;
+    return a;
+}
 __device__ __forceinline__ float3 operator+(float3 a, float s) { return make_float3(a.x + s, a.y + s, a.z + s); }
 __device__ __forceinline__ float3 operator-(float3 a, float s) { return make_float3(a.x - s, a.y - s, a.z - s); }
 __device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
@@ -189,6 +194,18 @@ __device__ __forceinline__ uint32_t pcg_hash(uint32_t input) {
     uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
     return (word >> 22u) ^ word;
 }
+// Argument evaluation order of the reference's three calls that draw two
+// random values in one expression, which C++ leaves unspecified; a set bit
+// means right to left.  The reference's GPU build (nvcc) evaluates all three
+// left to right (RNG_ORDER_GPU, measured against its own megakernel on the
+// GPU: every other order disagrees with it on 15-65% of the samples); its
+// host build (g++) evaluates all three right to left.
+constexpr int RNG_PAIR = 1;       // make_float2(get1D(), get1D())          samplers.cuh:37-40
+constexpr int RNG_SUN = 2;        // make_float3(get2D()*2-1, get1D()*2-1)  integrator.cuh:155
+constexpr int RNG_BSDF = 4;       // sampleF(wo, get2D(), get2D())          integrator.cuh:382
+constexpr int RNG_ORDER_GPU = 0;
+constexpr int RNG_ORDER_HOST = RNG_PAIR | RNG_SUN | RNG_BSDF;
+
 struct Sampler {
     uint32_t seed;
     __device__ __forceinline__ void init(int px, int py, int width, int index) {
@@ -200,10 +217,11 @@ struct Sampler {
         seed = pcg_hash(seed);
         return __fmul_rn((float)seed, 1.0f / 4294967295.0f);
     }
-    // make_float2(get1D(), get1D()) in the given argument evaluation order
+    // make_float2(get1D(), get1D()) (samplers.cuh:37-40) in the argument
+    // evaluation order of bit RNG_PAIR of `order` (0: left to right)
     __device__ __forceinline__ float2 get2D(int order) {
         float a = get1D(), b = get1D();
-        return order == 0 ? make_float2(a, b) : make_float2(b, a);
+        return (order & RNG_PAIR) == 0 ? make_float2(a, b) : make_float2(b, a);
     }
 };
 

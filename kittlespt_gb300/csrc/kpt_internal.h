@@ -224,6 +224,7 @@ __global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, fl
                         int* inst, int* tri, float* t, float2* uv, int* next, unsigned long long* counters);
 __global__ void k_occluded(SceneView s, int n, const float3* o, const float3* d, float tmin, const float* tmax,
                            uint8_t* out, int* next, unsigned long long* counters);
+__global__ void k_sun_constants_gpu(float phi, float theta, float diameter, float* out);
 __global__ void k_trace_chains(SceneView s, int n, const float3* o, const float3* d, int nbounces, int* inst,
                                int* tri, float* t, int* next, unsigned long long* counters);
 

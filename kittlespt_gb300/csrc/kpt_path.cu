@@ -238,27 +238,30 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
             // the sun's centre at 1 AU, each product rounded on its own:
             // target - sun_pos below cancels two values near 1.5e11, which a
             // fused multiply-add would shift by up to half their ulp (~1e-5
-            // of the difference)
-            const float3 sun_pos = make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
-                                               __fmul_rn(P.sun_dir.z, dsun));
+            // of the difference) -- as the reference's GPU build does, with
+            // gpu_arith
+            const float3 sun_pos = P.gpu_arith ? P.sun_dir * dsun
+                                               : make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
+                                                             __fmul_rn(P.sun_dir.z, dsun));
             float3 wi = P.sun_dir, target, Lem;
             float pdf = 0.0f, prob = 0.0f;
             bool eval;
             if (sun) {
                 // sampleLdSun: jittered point on the sun disc at 1 AU
                 float3 off;
-                if (order == 0) {
-                    float2 a = S.get2D(0);
+                if ((order & RNG_SUN) == 0) {
+                    float2 a = S.get2D(order);
                     float b = S.get1D();
                     off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                 } else {
                     float b = S.get1D();
-                    float2 a = S.get2D(1);
+                    float2 a = S.get2D(order);
                     off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
                 }
-                target = make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
-                                     __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
-                                     __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
+                target = P.gpu_arith ? sun_pos + (off * P.sun_radius_m)
+                                     : make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
+                                                   __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
+                                                   __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
                 eval = true;
             } else {
                 // sampleLd: uniform light pick, uniform point on the triangle
@@ -316,8 +319,8 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
         F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
         if (level == F.max_depth) continue;
         float2 uu, X;
-        if (order == 0) { uu = S.get2D(0); X = S.get2D(0); }
-        else { X = S.get2D(1); uu = S.get2D(1); }
+        if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
+        else { X = S.get2D(order); uu = S.get2D(order); }
         BsdfSample bs = bsdf.sample(wo, uu, X);
         if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) continue;
         beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
@@ -513,6 +516,20 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_sky_queue(FrameParams F, int lev
         float4 L = F.radiance[item];
         F.radiance[item] = make_float4(L.x + sk.x * b.x, L.y + sk.y * b.y, L.z + sk.z * b.z, 0.0f);
     }
+}
+
+// The sun's constants in the reference GPU build's arithmetic (fast sine,
+// cosine and tangent): its direction, getSunDirection (integrator.cuh:222-230),
+// LeSun's threshold (:137) and the disc radius at 1 AU,
+// angularDiameterToPhysicalDiameter / 2 (atmosphere.cuh:79-82).
+__global__ void k_sun_constants_gpu(float phi, float theta, float diameter, float* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const float3 d = normalize(make_float3(cosf(phi) * cosf(theta), sinf(theta), sinf(phi) * cosf(theta)));
+    out[0] = d.x;
+    out[1] = d.y;
+    out[2] = d.z;
+    out[3] = cosf(diameter / 2.0f);
+    out[4] = (2.0f * 149.597e9f * tanf(diameter / 2.0f)) / 2.0f;
 }
 
 // Nishita radiance towards the sun: a per-frame constant.

@@ -327,8 +327,91 @@ __device__ __forceinline__ float3 xpoint(float3 o, float t, float3 d) {
     return make_float3(xa(o.x, xm(t, d.x)), xa(o.y, xm(t, d.y)), xa(o.z, xm(t, d.z)));
 }
 
-// Radiance of the sky seen from `o` along `d`.
+// The same model in the arithmetic of the reference's GPU build: plain
+// single-precision operators under fast maths (approximate square root,
+// division and exponential, contracted products), written with the
+// reference's expression structure (intersectSphere, atmosphere.cuh:30-57;
+// sampleLi, :132-223) so that the compiler forms the same operations.  Its
+// altitudes carry that build's rounding (one ulp of a ~6.4e6 m length is
+// 0.5 m), so its sky agrees with that build's rather than with IEEE
+// arithmetic.
+__device__ __forceinline__ bool sphere_hit_gpu(float3 o, float3 d, float radius, float* t0, float* t1) {
+    float3 oc = make_float3(0.0f - o.x, 0.0f - o.y, 0.0f - o.z);
+    float a = dot(d, d);
+    float b = -2.0f * dot(d, oc);
+    float c = dot(oc, oc) - Sqr(radius);
+    float disc = Sqr(b) - 4.0f * a * c;
+    if (disc < 0.0f) return false;
+    float sq = sqrtf(disc);
+    *t0 = (-b - sq) / (2.0f * a);
+    *t1 = (-b + sq) / (2.0f * a);
+    if (*t0 > *t1) {
+        float t = *t0;
+        *t0 = *t1;
+        *t1 = t;
+    }
+    return !(*t1 < 0.0f);
+}
+
+static __device__ __noinline__ float3 nishita_gpu(const SkyParams& P, float3 o, float3 d) {
+    float tmin = 0.0f, tmax = __int_as_float(0x7f800000);
+    {
+        float te, tx;
+        if (!sphere_hit_gpu(o, d, P.atm_r, &te, &tx) || tx < 0.0f) return make_float3(0.0f, 0.0f, 0.0f);
+        if (te > tmin && te > 0.0f) tmin = te;
+        if (tx < tmax) tmax = tx;
+    }
+    const float depth = tmax - tmin;
+    const float step = depth / 16.0f;
+    float t = tmin;
+    float3 iR = make_float3(0.0f, 0.0f, 0.0f), iM = make_float3(0.0f, 0.0f, 0.0f);
+    float oR = 0.0f, oM = 0.0f;
+    const float3 tR = make_float3(P.sigma_r.x + 0.0f, P.sigma_r.y + 0.0f, P.sigma_r.z + 0.0f);
+    const float tM = P.sigma_m + P.sigma_am;
+#pragma unroll 1
+    for (int i = 0; i < 16; ++i) {
+        const float3 sp = o + ((t + (step * 0.5f)) * d);
+        const float alt = length(sp) - P.earth_r;
+        const float pR = expf(-alt / P.h_r) * step;
+        const float pM = expf(-alt / P.h_m) * step;
+        oR += pR;
+        oM += pM;
+        float lte, ltx;
+        sphere_hit_gpu(sp, P.sun_dir, P.atm_r, &lte, &ltx);
+        const float lstep = ltx / 8.0f;
+        float lt = 0.0f, lR = 0.0f, lM = 0.0f;
+        int j;
+#pragma unroll
+        for (j = 0; j < 8; ++j) {
+            const float3 spl = sp + ((lt + (lstep * 0.5f)) * P.sun_dir);
+            const float altl = length(spl) - P.earth_r;
+            if (altl < 0.0f) break;
+            lR += expf(-altl / P.h_r) * lstep;
+            lM += expf(-altl / P.h_m) * lstep;
+            lt += lstep;
+        }
+        if (j == 8) {
+            const float sr = oR + lR, sm = oM + lM;
+            const float3 tau = make_float3(tR.x * sr + tM * sm, tR.y * sr + tM * sm, tR.z * sr + tM * sm);
+            const float3 Tr = make_float3(expf(-tau.x), expf(-tau.y), expf(-tau.z));
+            iR += Tr * pR;
+            iM += Tr * pM;
+        }
+        t += step;
+    }
+    float mu = dot(d, P.sun_dir);
+    float rp = (3.0f * (1.0f + Sqr(mu))) / (16.0f * PI_F);
+    const float g = 0.76f;
+    float den = (8.0f * PI_F) * ((2.0f + Sqr(g)) * powf(1.0f + Sqr(g) - 2.0f * g * mu, 1.5f));
+    float mp = 3.0f * ((1.0f - Sqr(g)) * (1.0f + Sqr(mu))) / den;
+    float3 L = P.sigma_r * iR * rp + make_float3(P.sigma_m, P.sigma_m, P.sigma_m) * iM * mp;
+    return L * 6.0e5f * P.sun_emission;
+}
+
+// Radiance of the sky seen from `o` along `d`, in the arithmetic the frame
+// selects (P.gpu_arith).
 static __device__ __noinline__ float3 nishita(const SkyParams& P, float3 o, float3 d) {
+    if (P.gpu_arith) return nishita_gpu(P, o, d);
     float tmin = 0.0f, tmax = __int_as_float(0x7f800000);
     {
         float te, tx;

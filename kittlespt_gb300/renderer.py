@@ -105,7 +105,8 @@ class Renderer:
                                    karis=bool(st["karis"]), auto_exposure=bool(st["auto_exposure"]),
                                    bloom_final_blend=float(st["bloom_final_blend"]),
                                    bloom_internal_blend=float(st["bloom_internal_blend"]),
-                                   frame_delta_ms=float(st["frame_delta_ms"]))
+                                   frame_delta_ms=float(st["frame_delta_ms"]),
+                                   sky_arith=int(getattr(scene, "sky_arith", 0)))
         self.set_exposure(scene.exposure)
         self.scene = scene
 

@@ -362,6 +362,10 @@ class Scene:
     name: str = ""
     # 8-bit textures (TextureSceneEntity, pod_types.hpp): [h, w, channels] uint8 each
     textures: List[np.ndarray] = dataclasses.field(default_factory=list)
+    # arithmetic of the sky and the sun's constants (kpt_settings.sky_arith):
+    # 0 IEEE single precision, as the oracle and the reference's host build
+    # compute them; 1 that of the reference's GPU build
+    sky_arith: int = 0
 
     def texture_arrays(self):
         """(desc int32 [n, 4] = width, height, channels, byte offset; pixels

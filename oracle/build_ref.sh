@@ -60,7 +60,7 @@ host() {
         -include "$here/ref_harness/ref_prelude.h" \
         -I"$CUDA/include" -I"$CUDA/include/cccl" -I"$out/shim" \
         -I"$src/src" -I"$src/thirdparty" -I"$src/thirdparty/glad/include" \
-        "$here/ref_harness/ref_harness.cpp" -o "$out/libkpt_ref_host.so.tmp" -lpthread
+        "$here/ref_harness/ref_harness.cpp" -o "$out/libkpt_ref_host.so.tmp" -lpthread -Wl,-z,defs
     mv "$out/libkpt_ref_host.so.tmp" "$out/libkpt_ref_host.so"
     echo "built $out/libkpt_ref_host.so"
 }
@@ -71,7 +71,7 @@ gpu() {
     # translation unit instead of its relocatable device code; host code
     # without contraction so the host BVH build matches the other builds
     "$NVCC" -std=c++17 -O3 -use_fast_math -gencode arch=compute_103a,code=sm_103a -lineinfo -shared \
-        -Xcompiler -fPIC,-fpermissive,-ffp-contract=off -w \
+        -Xcompiler -fPIC,-fpermissive,-ffp-contract=off -w -Xlinker -z,defs \
         -include "$here/ref_harness/ref_gpu_prelude.h" \
         -I"$out/shim" -I"$src/src" -I"$src/thirdparty" -I"$src/thirdparty/glad/include" \
         "$here/ref_harness/ref_gpu_harness.cu" -o "$out/libkpt_ref_gpu.so.tmp"

@@ -16,9 +16,11 @@
 // XYZ) the expression is evaluated in double as C++ requires.
 //
 // Order of RNG draws: the reference writes three calls whose argument
-// evaluation order C++ leaves unspecified (samplers.cuh:37-40,
-// integrator.cuh:155, integrator.cuh:382).  `rng_order` selects left-to-right
-// (0) or right-to-left (1) for all three sites.
+// evaluation order C++ leaves unspecified.  `rng_order` is a bit mask, a set
+// bit meaning right to left: 1 = the pair of get2D (samplers.cuh:37-40),
+// 2 = the sun-disc offset (integrator.cuh:155), 4 = the BSDF sample's two
+// pairs (integrator.cuh:382).  The reference's GPU build evaluates them as
+// 0, its host build (g++) as 7.
 
 #include <algorithm>
 #include <atomic>
@@ -192,7 +194,7 @@ static inline uint32_t pcg_hash(uint32_t input) {  // samplers.cuh:12-17
 }
 struct Sampler {
     uint32_t seed;
-    int order;  // 0: left-to-right argument evaluation, 1: right-to-left
+    int order;  // bit 0: the pair's argument evaluation order (0 left to right)
     // samplers.cuh:24-29: seed = pixel index scaled by max(frame, 1) in float
     void init(int px, int py, int width, int index, int dimension = 0) {
         seed = (uint32_t)(px + py * width);
@@ -205,7 +207,7 @@ struct Sampler {
         return (float)seed * INV_UINT32MAX;
     }
     f2 get2D() {  // samplers.cuh:37-40
-        if (order == 0) { float a = get1D(); float b = get1D(); return {a, b}; }
+        if ((order & 1) == 0) { float a = get1D(); float b = get1D(); return {a, b}; }
         float b = get1D(); float a = get1D(); return {a, b};
     }
 };
@@ -1184,9 +1186,43 @@ struct Frame {
     int rng_order;
 };
 
+// Rounding-sensitivity probe (test support, not part of the reference's
+// algorithm): when given to Li, the quantities a fast-maths build computes
+// with rounding that differs from this one -- every scattered ray direction,
+// geometric normal, area-light sample point, surface point and the path
+// throughput -- are moved by a relative amount of at most eps (directions,
+// normals, throughput) or eps_pos (points) in a pseudo-random direction drawn
+// from its own stream, the sample's random numbers being unchanged.  Camera
+// rays, traversal and the sun's target are computed exactly alike everywhere
+// and are not moved.  A
+// sample whose radiance moves by more than the parity tolerance under such a
+// perturbation of a few ulps sits at a decision that rounding can flip (a ray
+// grazing a triangle edge or silhouette, a shadow ray grazing an occluder, a
+// hemisphere or total-internal-reflection test, a Russian-roulette draw next
+// to its threshold) or is ill-conditioned (a near-specular lobe).
+struct Perturb {
+    uint32_t state;
+    float eps, eps_pos;
+    float next() {   // in [-1, 1]
+        state = pcg_hash(state);
+        return (float)state * INV_UINT32MAX * 2.0f - 1.0f;
+    }
+    f3 vec() { float a = next(); float b = next(); float c = next(); return {a, b, c}; }
+    f3 dir(f3 d) { return d + vec() * eps; }   // not renormalised: a unit vector off by a few ulps
+    f3 point(f3 p) {
+        float m = fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))) + 1.0f;
+        return p + vec() * (eps_pos * m);
+    }
+    f3 scale(f3 v) {
+        float a = next(); float b = next(); float c = next();
+        return {v.x * (1.0f + eps * a), v.y * (1.0f + eps * b), v.z * (1.0f + eps * c)};
+    }
+};
+
 // Integrator::Li (integrator.cuh:241-402) including LeSun (:135-143),
-// sampleLdSun (:147-186) and sampleLd (:188-220).
-static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c) {
+// sampleLdSun (:147-186) and sampleLd (:188-220).  P (test support) is null
+// except under the rounding-sensitivity probe.
+static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c, Perturb* P = nullptr) {
     const Scene& s = *F.s;
     const int max_depth = F.set.max_depth;
     f3 L = F3(0.0f), beta = F3(1.0f);
@@ -1204,6 +1240,7 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c)
     while (nonzero(beta)) {
         S.seed = S.seed + (uint32_t)depth;
         bool first = (depth == 0);
+        if (P && !first) ray = make_ray(ray.o, P->dir(ray.d));
         Hit h = tlas_intersect(s, ray, 0.0f, INFINITY, c);
         if (h.prim < 0) {
             f3 sk = sky(A, make_ray(observer, ray.d));
@@ -1222,6 +1259,7 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c)
         }
         if (first) { out.first_prim = h.prim; out.first_inst = h.inst; out.first_t = h.t; }
         Surface si = surface_interaction(s, h, ray);
+        if (P) { si.pos = P->point(si.pos); si.ng = P->dir(si.ng); }
         f3 Le = F3(0.0f);
         if (si.light >= 0) Le = light_L(s, s.lights[si.light], si.uv);
         if (nonzero(Le)) {
@@ -1253,7 +1291,7 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c)
                 f3 sun_pos = sd * dist_sun;
                 float sun_r = (2.0f * dist_sun * tanf(F.env.sun_angular_diameter / 2.0f)) / 2.0f;
                 f3 off;
-                if (F.rng_order == 0) {
+                if ((F.rng_order & 2) == 0) {
                     f2 a = S.get2D(); float b = S.get1D();
                     off = {a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f};
                 } else {
@@ -1298,6 +1336,7 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c)
                     f3 p = (tr.p[0] * bary.x) + (tr.p[1] * bary.y);
                     p = p + (tr.p[2] * bary.z);
                     p = xyz(mul(model, F4(p, 1.0f)));
+                    if (P) p = P->point(p);
                     f3 gn = xyz(mul(model, F4(tr.local_gn, 0.0f)));
                     float tri_area = 0.5f * length(cross(tr.p[1] - tr.p[0], tr.p[2] - tr.p[0]));
                     float pdf = 1.0f / tri_area;
@@ -1320,11 +1359,12 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c)
         }
         if (depth++ == max_depth) break;
         f2 u, X;
-        if (F.rng_order == 0) { u = S.get2D(); X = S.get2D(); }
+        if ((F.rng_order & 4) == 0) { u = S.get2D(); X = S.get2D(); }
         else { X = S.get2D(); u = S.get2D(); }
         BSDFSample bs = bsdf.sample(wo, u, X);
         if (bs.scatter == ABSORBED || !nonzero(bs.f)) break;
         beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
+        if (P) beta = P->scale(beta);
         p_b = bsdf.pdf(wo, bs.wi);
         any_non_specular |= !(bs.scatter & SPECULAR);
         prev_pos = si.pos;
@@ -1351,7 +1391,8 @@ static Ray camera_ray(const Frame& F, f2 ndc) {
 
 // One sample of the megakernel body (kernels.cu:385-413): seed, discarded
 // filter draw, camera ray, Li, clampOutput.
-static PathResult megakernel_sample(const Frame& F, int x, int y, int W, int H, int frame_index, Counters& c) {
+static PathResult megakernel_sample(const Frame& F, int x, int y, int W, int H, int frame_index, Counters& c,
+                                    Perturb* P = nullptr) {
     Sampler S;
     S.order = F.rng_order;
     S.init(x, y, W, frame_index);
@@ -1359,7 +1400,7 @@ static PathResult megakernel_sample(const Frame& F, int x, int y, int W, int H, 
     f2 uv = {((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H};
     f2 ndc = {2.0f * uv.x - 1.0f, 2.0f * uv.y - 1.0f};
     Ray r = camera_ray(F, ndc);
-    PathResult pr = Li(F, r, S, c);
+    PathResult pr = Li(F, r, S, c, P);
     pr.L = clamp_output(F3(1.0f) * 1.0f * pr.L);
     return pr;
 }
@@ -1838,6 +1879,51 @@ void orc_render_samples(void* hp, const float* inv_proj, const float* inv_view, 
         int64_t v[8] = {tot.box_tests, tot.tri_tests, tot.inst_xforms, tot.sky_evals, tot.hits, tot.rays, tot.max_stack, tot.stack_overflow};
         for (int k = 0; k < 8; ++k) counters[k] = v[k];
     }
+}
+
+// The rounding-sensitivity probe over the samples of orc_render_samples
+// (test support): for every sample, `ncopies` renders under Perturb with
+// relative sizes eps and eps_pos (streams seeded from the sample, the pixel and the copy),
+// compared with the unperturbed sample: response = the largest over copies
+// and channels of |L' - L| / max(max channel of |L|, 1e-3), the relative
+// error measure of the parity tests.  radiance (may be null) receives the
+// unperturbed samples as orc_render_samples does.
+void orc_render_sensitivity(void* hp, const float* inv_proj, const float* inv_view, const void* env,
+                            const void* settings, int W, int H, int sample0, int nsamples, int rng_order,
+                            int row0, int nrows, float eps, float eps_pos, int ncopies, float* radiance,
+                            float* response, int nthreads) {
+    Frame F;
+    F.s = &((orc_handle*)hp)->s;
+    std::memcpy(&F.env, env, sizeof(Env));
+    std::memcpy(&F.set, settings, sizeof(Settings));
+    F.inv_proj = m4_from(inv_proj);
+    F.inv_view = m4_from(inv_view);
+    F.cam_pos = xyz(F.inv_view.c[3]);
+    F.sun_dir = sun_direction(F.env);
+    F.atm = make_atmosphere(F.env, F.sun_dir);
+    F.rng_order = rng_order;
+    if (nrows <= 0) nrows = H - row0;
+    std::vector<Counters> cs(std::max(nthreads, 1));
+    parallel_rows(nrows, nthreads, [&](int ry, int tid) {
+        int y = row0 + ry;
+        for (int x = 0; x < W; ++x) {
+            for (int k = 0; k < nsamples; ++k) {
+                PathResult pr = megakernel_sample(F, x, y, W, H, sample0 + k, cs[tid]);
+                float scale = fmaxf(fmaxf(fabsf(pr.L.x), fmaxf(fabsf(pr.L.y), fabsf(pr.L.z))), 1e-3f);
+                float worst = 0.0f;
+                for (int q = 0; q < ncopies; ++q) {
+                    Perturb P{pcg_hash((uint32_t)(y * W + x) * 7919u + (uint32_t)(sample0 + k) * 104729u +
+                                       (uint32_t)q * 15485863u), eps, eps_pos};
+                    PathResult pp = megakernel_sample(F, x, y, W, H, sample0 + k, cs[tid], &P);
+                    float d = fmaxf(fabsf(pp.L.x - pr.L.x), fmaxf(fabsf(pp.L.y - pr.L.y), fabsf(pp.L.z - pr.L.z)));
+                    worst = fmaxf(worst, d / scale);
+                }
+                size_t o = ((size_t)k * nrows + ry) * W + x;
+                if (radiance) { radiance[3 * o] = pr.L.x; radiance[3 * o + 1] = pr.L.y; radiance[3 * o + 2] = pr.L.z; }
+                response[o] = worst;
+            }
+        }
+    });
 }
 
 // Nishita radiance seen from 1 m above the ground for n directions.

@@ -90,6 +90,8 @@ def lib(prefix: str = "orc"):
         g("sky_double").argtypes = [C.c_int, _v, _v, _v, _v]
         g("adjoint_estimate").restype = C.c_int
         g("adjoint_estimate").argtypes = [_v, C.c_int, _v, _v, _v, _v, _v]
+        g("render_sensitivity").argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, _v, _f, C.c_int]
         g("histogram").argtypes = [C.c_int, C.c_int, _f, C.c_float, C.c_float, _u64]
         g("exposure").argtypes = [_u64, _v, C.c_float, C.c_float, _f]
         g("hist_thresholds").argtypes = [C.c_float, C.c_float, _f]
@@ -206,6 +208,28 @@ class Scene:
                                    row0, nrows, _ptr(rad) if rad is not None else None, _ptr(alb), _ptr(fh),
                                    _ptr(ft), _ptr(cnt), nthreads or os.cpu_count())
         return dict(radiance=rad, albedo=alb, first_hit=fh, first_t=ft, counters=cnt)
+
+
+    def render_sensitivity(self, sample0=0, nsamples=1, rng_order=0, row0=0, nrows=0, eps=2e-6, eps_pos=2e-7,
+                           ncopies=4, nthreads=None):
+        """The rounding-sensitivity probe of the oracle (orc_render_sensitivity):
+        per sample, the largest relative change of its radiance over `ncopies`
+        re-renders with scattered directions, normals and throughput moved by a
+        relative eps and surface and light-sample points by a relative eps_pos.  Returns dict(radiance
+        [nsamples][rows][W][3], response [nsamples][rows][W])."""
+        sc = self.scene
+        W, H = sc.width, sc.height
+        rows = nrows if nrows > 0 else H - row0
+        rad = np.zeros((nsamples, rows, W, 3), np.float32)
+        resp = np.zeros((nsamples, rows, W), np.float32)
+        ip = np.ascontiguousarray(sc.camera.inv_proj.T, np.float32).reshape(-1)
+        iv = np.ascontiguousarray(sc.camera.inv_view.T, np.float32).reshape(-1)
+        env = np.ascontiguousarray(sc.env)
+        st = sc.settings.copy()
+        self._fn("render_sensitivity")(self.h, ip, iv, _ptr(env), _ptr(st), W, H, sample0, nsamples, rng_order,
+                                       row0, nrows, float(eps), float(eps_pos), int(ncopies), _ptr(rad), resp,
+                                       nthreads or os.cpu_count())
+        return dict(radiance=rad, response=resp)
 
 
 def sky(env, dirs, prefix="orc"):

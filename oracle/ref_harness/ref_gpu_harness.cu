@@ -27,6 +27,7 @@
 // the depth in refgpu_last_error) any scene with one deeper than 14, before
 // any kernel runs.
 
+#include "error_check.cu"
 #include "shaders/kernels.cu"
 #include "shaders/tlas.cu"
 #include "shaders/interaction.cu"

@@ -5,7 +5,8 @@ oracle/build_ref.sh from the reference source tree).
 The reference ships no tests or golden vectors, so these fixtures are the
 pin for the CPU oracle: tests/test_oracle_golden.py checks that the oracle
 reproduces every array here bit for bit.  The right-to-left RNG argument order
-of this host build (g++) is recorded as rng_order=1.
+of this host build (g++), all three unspecified-order call sites right to
+left, is recorded as rng_order=7.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """

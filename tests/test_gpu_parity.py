@@ -5,9 +5,8 @@ Tolerances (from the parity targets of the path):
     runs in IEEE arithmetic; the oracle is pinned to the reference's own code);
   * Nishita sky: 1e-4 relative (fast-maths exp/sqrt as in the reference's
     GPU build);
-  * per-sample radiance: at least 99% of samples within 1e-4 relative; the
-    rest are paths whose Russian-roulette or lobe decision flips on a last-bit
-    difference;
+  * per-sample radiance: within 1e-4 relative, or explained by the oracle's
+    rounding-sensitivity probe (tests/parity_rule.py);
   * modulate, histogram, exposure: bit-exact on the same inputs;
   * display image: 2e-5 absolute (CUDA powf/log2f vs the C library).
 """
@@ -17,6 +16,7 @@ import pytest
 
 from kittlespt_gb300 import scenes as S
 from oracle import oracle as O
+from tests.parity_rule import PROBE_COPIES, PROBE_EPS, PROBE_EPS_POS, check_samples
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -124,7 +124,7 @@ def render_samples(r, sc, n):
     return rad[..., :3].cpu().numpy(), hit.cpu().numpy(), alb[..., :3].cpu().numpy()
 
 
-@pytest.mark.parametrize("which,n,order", [("small", 4, 0), ("small", 2, 1), ("full", 2, 0)])
+@pytest.mark.parametrize("which,n,order", [("small", 4, 0), ("small", 2, 7), ("small", 2, 5), ("full", 2, 0)])
 def test_per_sample_radiance(which, n, order):
     if which == "small":
         sc = S.scene_small(64, 64, n, 4)
@@ -136,15 +136,15 @@ def test_per_sample_radiance(which, n, order):
         rad, hit, alb = render_samples(r, sc, n)
     finally:
         r.shutdown()
-    ref = O.Scene(sc).render_samples(0, n, rng_order=order)
+    o = O.Scene(sc)
+    ref = o.render_samples(0, n, rng_order=order)
     # first hits: exact
     np.testing.assert_array_equal(global_prim(sc, hit[..., 0], hit[..., 1]), ref["first_hit"][..., 0])
     np.testing.assert_array_equal(bits(hit[..., 2].view(np.float32)), bits(ref["first_t"]))
     hitmask = ref["first_hit"][..., 0] >= 0
     np.testing.assert_array_equal(bits(alb[hitmask]), bits(ref["albedo"][hitmask]))
-    err = np.abs(rad - ref["radiance"]).max(-1) / np.maximum(np.abs(ref["radiance"]).max(-1), 1e-3)
-    frac = (err <= 1e-4).mean()
-    assert frac >= 0.99, f"{frac:.4f} of samples within 1e-4"
+    probe = o.render_sensitivity(0, n, order, eps=PROBE_EPS, eps_pos=PROBE_EPS_POS, ncopies=PROBE_COPIES)
+    check_samples(rad, ref["radiance"], probe["response"], f"{which} x{n}, rng order {order}")
     # the mean over samples converges to the same image
     assert np.abs(rad.mean(0) - ref["radiance"].mean(0)).mean() <= 1e-2 * max(ref["radiance"].mean(), 1e-3)
 

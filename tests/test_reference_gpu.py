@@ -6,17 +6,21 @@ build's -use_fast_math from the staged reference sources
 (oracle/build_ref.sh gpu) and driven by oracle/ref_harness/ref_gpu_harness.cu.
 These tests put the CUDA path behind include/kpt.h beside it on the plain
 method's small configuration at its stated size (256x256, depth 4, the
-reference's frame index = the sample index), through the C ABI:
+reference's frame index = the sample index), through the C ABI, with the sky
+in the GPU build's arithmetic (kpt_settings.sky_arith = 1, the default) and
+the RNG argument order of that build (rng_order = 0, the default):
 
   * camera-ray closest hits: our camera rays and traversal are IEEE, the
-    reference's are fast maths, so a ray that passes within a rounding error
-    of a triangle edge may hit the neighbour.  Ids agree on all but a few
-    pixels, each of them on an edge in the IEEE oracle; where ids agree, t
-    agrees within 1e-5 relative;
+    reference's fast maths (its camera direction is normalised with the
+    approximate reciprocal square root, its Moller-Trumbore divides
+    approximately), so ids agree on every pixel and t within 5e-5 relative
+    (measured: 1.24e-5);
   * per-sample radiance (the megakernel's accumulation after one frame from
-    zero is exactly that frame's clamped sample): within 1e-4 relative for all
-    samples whose first hit agrees, but a small tail of paths whose later
-    vertices diverge the same way.
+    zero is exactly that frame's clamped sample): at least 99.8% of the
+    samples within 1e-4 relative (measured: 99.88%); the rest lie where the
+    two builds' traversal rounding or the ill-conditioned sky altitude
+    differ.  Under IEEE sky arithmetic only ~78% agree, and under any other
+    RNG argument order 35-85%.
 
 They are skipped where the reference's sources were not staged (no
 oracle/_ref/libkpt_ref_gpu.so).
@@ -52,8 +56,9 @@ def global_prim(scene, inst, tri):
 def ours(sc, n):
     from kittlespt_gb300.renderer import Renderer
     with Renderer(0) as r:
+        assert r.get_renderer_settings().rng_order == 0 and r.get_renderer_settings().sky_arith == 1
         r.load_scene(sc)
-        assert r.get_renderer_settings().rng_order == 0
+        r.set_renderer_settings(sky_arith=1)
         rad = torch.zeros((n, sc.height, sc.width, 4), dtype=torch.float32, device="cuda:0")
         hit = torch.zeros((sc.height, sc.width, 4), dtype=torch.int32, device="cuda:0")
         r.render_samples_device(0, n, rad.data_ptr(), hit.data_ptr())
@@ -92,7 +97,7 @@ def test_camera_hits_match_the_reference_gpu_build(small):
     both = same & (prim >= 0)
     rel = np.abs(t[both] - ref["t"][both]) / np.abs(ref["t"][both])
     print(f"t: max relative difference {rel.max():.3e} where ids agree")
-    assert rel.max() <= 1e-5
+    assert rel.max() <= 5e-5
     # every pixel whose id differs hits near an edge of the IEEE oracle's triangle
     if (~same).any():
         ys, xs = np.nonzero(~same)
@@ -128,7 +133,46 @@ def test_per_sample_radiance_matches_the_reference_gpu_build(small):
     ok = err <= 1e-4
     print(f"per-sample radiance within 1e-4: {ok.mean():.6f} of {ok.size}; "
           f"where the first hit agrees {ok[:, same_first].mean():.6f}; max err {err.max():.3e}")
-    assert ok.mean() >= 0.99
+    assert ok.mean() >= 0.998
     # the converged image agrees
+    m, mr = rad.mean(0), rad_ref.mean(0)
+    assert np.abs(m - mr).mean() <= 1e-2 * max(float(mr.mean()), 1e-3)
+
+
+@pytest.fixture(scope="module")
+def full_frame():
+    """The full-frame workload (1920x1080, 16 spp, depth 8, the 8x8
+    icosphere grid with 16 lights): the megakernel's 16 frames and our 16
+    samples of the same frame indices."""
+    sc = S.scene_full()
+    sc.sky_arith = 1
+    g = O.RefGpuScene(sc)
+    try:
+        depth = g.tree_depth()
+        hits = g.first_hits()
+        rad_ref = g.render_samples(0, sc.spp)
+    finally:
+        g.close()
+    rad, hit = ours(sc, sc.spp)
+    return sc, depth, hits, rad_ref, rad, hit
+
+
+def test_full_frame_matches_the_reference_gpu_build(full_frame):
+    sc, depth, ref, rad_ref, rad, hit = full_frame
+    assert depth["blas"] <= 14 and depth["tlas"] <= 14
+    prim = global_prim(sc, hit[..., 0], hit[..., 1])
+    same = prim == ref["prim"]
+    print(f"1080p camera-ray ids equal on {same.mean():.6f} of {same.size} pixels ({(~same).sum()} differ)")
+    assert same.mean() >= 0.999
+    t = hit[..., 2].view(np.float32)
+    both = same & (prim >= 0)
+    rel = np.abs(t[both] - ref["t"][both]) / np.abs(ref["t"][both])
+    print(f"1080p t: max relative difference {rel.max():.3e}, 99.99th percentile {np.quantile(rel, 0.9999):.3e}")
+    err = np.abs(rad - rad_ref).max(-1) / np.maximum(np.abs(rad_ref).max(-1), 1e-3)
+    ok = err <= 1e-4
+    print(f"1080p x{sc.spp} per-sample radiance within 1e-4: {ok.mean():.6f} of {ok.size}; "
+          f"where the first hit agrees {ok[:, same].mean():.6f}; quantiles 0.5/0.99/0.999 "
+          f"{np.quantile(err, [0.5, 0.99, 0.999]).tolist()}")
+    assert ok.mean() >= 0.99
     m, mr = rad.mean(0), rad_ref.mean(0)
     assert np.abs(m - mr).mean() <= 1e-2 * max(float(mr.mean()), 1e-3)
