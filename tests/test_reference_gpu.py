@@ -173,6 +173,6 @@ def test_full_frame_matches_the_reference_gpu_build(full_frame):
     print(f"1080p x{sc.spp} per-sample radiance within 1e-4: {ok.mean():.6f} of {ok.size}; "
           f"where the first hit agrees {ok[:, same].mean():.6f}; quantiles 0.5/0.99/0.999 "
           f"{np.quantile(err, [0.5, 0.99, 0.999]).tolist()}")
-    assert ok.mean() >= 0.99
+    assert ok.mean() >= 0.995
     m, mr = rad.mean(0), rad_ref.mean(0)
     assert np.abs(m - mr).mean() <= 1e-2 * max(float(mr.mean()), 1e-3)
