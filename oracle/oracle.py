@@ -438,6 +438,8 @@ class RefGpuScene:
             L.refgpu_tree_depth.argtypes = [_v, _i]
             L.refgpu_render.restype = C.c_int
             L.refgpu_render.argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _v, _v]
+            L.refgpu_effects.restype = C.c_int
+            L.refgpu_effects.argtypes = [C.c_int, C.c_int, _f, _f]
             L.refgpu_first_hits.restype = C.c_int
             L.refgpu_first_hits.argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, _i, _i, _f]
             cls._L = L
@@ -525,3 +527,15 @@ class RefGpuScene:
         if rc != 0:
             raise RuntimeError(self.lib().refgpu_last_error().decode())
         return dict(prim=prim, inst=inst, t=t)
+
+
+def ref_gpu_effects(image):
+    """The reference's own lens-effects kernel (computeEffects) on the GPU for
+    an [H][W][4] float image (the backbuffer); returns the output texture."""
+    L = RefGpuScene.lib()
+    img = np.ascontiguousarray(image, np.float32)
+    H, W = img.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    if L.refgpu_effects(W, H, img.reshape(-1), out.reshape(-1)) != 0:
+        raise RuntimeError(L.refgpu_last_error().decode())
+    return out

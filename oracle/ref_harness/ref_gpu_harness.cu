@@ -362,4 +362,44 @@ int refgpu_first_hits(void* h, const float* inv_proj, const float* inv_view, con
     return 0;
 }
 
+// The reference's lens effects (computeEffects through launchFxComputeKernel,
+// kernels.cu:120-132 and :506-528) on an image: `in` ([H][W] RGBA) is the
+// backbuffer, `out` receives the output texture.
+int refgpu_effects(int W, int H, const float* in, float* out) {
+    if (W <= 0 || H <= 0 || !in || !out) return fail("refgpu_effects: bad arguments");
+    FrameSurface src, dst;
+    cudaChannelFormatDesc cd = cudaCreateChannelDesc<float4>();
+    cudaError_t e = cudaMallocArray(&src.arr, &cd, W, H, cudaArraySurfaceLoadStore);
+    if (e == cudaSuccess) e = cudaMallocArray(&dst.arr, &cd, W, H, cudaArraySurfaceLoadStore);
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    if (e == cudaSuccess) {
+        rd.res.array.array = src.arr;
+        e = cudaCreateSurfaceObject(&src.obj, &rd);
+    }
+    if (e == cudaSuccess) {
+        rd.res.array.array = dst.arr;
+        e = cudaCreateSurfaceObject(&dst.obj, &rd);
+    }
+    const size_t pitch = (size_t)W * sizeof(float4);
+    if (e == cudaSuccess) e = cudaMemcpy2DToArray(src.arr, 0, 0, in, pitch, pitch, H, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        ShaderData sd;
+        sd.output_resolution = make_int2(W, H);
+        sd.render_resolution = make_int2(W, H);
+        sd.backbuffer_texture.dimensions = make_int2(W, H);
+        sd.backbuffer_texture.m_surface_object = src.obj;
+        sd.output_texture.dimensions = make_int2(W, H);
+        sd.output_texture.m_surface_object = dst.obj;
+        KittlesPT::launchFxComputeKernel(sd);
+        e = cudaMemcpy2DFromArray(out, pitch, dst.arr, 0, 0, pitch, H, cudaMemcpyDeviceToHost);
+    }
+    for (FrameSurface* f : {&src, &dst}) {
+        if (f->obj) cudaDestroySurfaceObject(f->obj);
+        if (f->arr) cudaFreeArray(f->arr);
+    }
+    if (e != cudaSuccess) return fail(std::string("refgpu_effects: ") + cudaGetErrorString(e));
+    return 0;
+}
+
 }  // extern "C"

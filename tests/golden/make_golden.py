@@ -51,6 +51,44 @@ def traversal_scene():
     return S.scene_traversal(20000)
 
 
+def textured_scene():
+    """The small scene with every texture slot of the material in use
+    (Material::getBSDF and Texture::evaluate, material.cu:17-70,
+    texture.cuh:34-66; Light::L, light.cu:21-33): an sRGB albedo texture and
+    a normal map on the diffuse sphere, an occlusion-roughness-metallic
+    texture on the conductor, the albedo texture again on the ground, a
+    glass pane with a transmission texture and an emitter with an emission
+    texture above the spheres.  Textures have 3 or 4 channels and odd sizes;
+    the last texel of the last texture sits at the end of the pixel buffer."""
+    sc = S.scene_small(40, 40, 2, 4)
+    rng = np.random.default_rng(77)
+    tex = [rng.integers(0, 256, (9, 13, 3), dtype=np.uint8),    # albedo (sRGB)
+           rng.integers(0, 256, (8, 8, 4), dtype=np.uint8),     # normal map
+           rng.integers(0, 256, (5, 7, 3), dtype=np.uint8),     # occlusion, roughness, metallic
+           rng.integers(0, 256, (6, 6, 3), dtype=np.uint8),     # transmission
+           rng.integers(0, 256, (4, 11, 3), dtype=np.uint8)]    # emission
+    m = [S.material(albedo=(0.9, 0.8, 0.7), roughness=0.4),
+         S.material(albedo=(0.95, 0.64, 0.54), metallic=1.0, roughness=0.6),
+         S.material(albedo=(0.6, 0.6, 0.6), roughness=0.7),
+         S.material(albedo=(0.9, 0.95, 1.0), roughness=0.2, transmission=1.0, ior=1.5),
+         S.material(albedo=(0.8, 0.8, 0.8), emission=(1.0, 0.9, 0.8), emission_scale=15.0)]
+    m[0]["albedo_tex"], m[0]["normal_tex"], m[0]["normal_scale"] = 0, 1, 0.8
+    m[1]["orm_tex"] = 2
+    m[2]["albedo_tex"] = 0
+    m[3]["transmission_tex"] = 3
+    m[4]["emission_tex"] = 4
+    sc.materials = np.stack(m)
+    sc.meshes = [S.uv_sphere(32, 16, 1.0, 0), S.quad(20.0, 20.0, 0.0, True, 2), S.quad(2.0, 2.0, 0.0, True, 3),
+                 S.quad(1.0, 1.0, 0.0, False, 4)]
+    sc.instances = [S.Instance(0, S.translate(-1.5, 0, 0).astype(np.float32), 0),
+                    S.Instance(0, S.translate(1.5, 0, 0).astype(np.float32), 1),
+                    S.Instance(1, S.translate(0, -1.0, 0).astype(np.float32), 2),
+                    S.Instance(2, S.translate(0.5, 1.3, 0.5).astype(np.float32), 3),
+                    S.Instance(3, S.translate(0, 2.5, 0).astype(np.float32), 4)]
+    sc.textures = tex
+    return sc
+
+
 def tricky_scene():
     """Random triangles plus exact duplicates of a third of them, triangles
     with two equal vertices, collinear vertices and slivers, in one mesh
@@ -178,6 +216,11 @@ def main():
     easu_hdr, sharp_hdr = O.fsr(hdr, 121, 67, "ref")
     out.update(up_bilinear=O.upscale(render, 160, 90, "ref"), up_easu=easu, up_fsr=sharp, up_hdr=hdr,
                up_hdr_easu=easu_hdr, up_hdr_fsr=sharp_hdr)
+    # every texture slot (albedo, normal map, ORM, transmission, emission)
+    r = O.Scene(textured_scene(), "ref")
+    rs = r.render_samples(0, 2)
+    out.update(tex_radiance=rs["radiance"], tex_albedo=rs["albedo"], tex_first_hit=rs["first_hit"],
+               tex_first_t=rs["first_t"])
     # closest hits where equal distances are common (duplicated and
     # coincident triangles): which one wins is the reference's traversal order
     r = O.Scene(tricky_scene(), "ref")

@@ -36,6 +36,16 @@ def test_effects_match_oracle(w, h):
     same = (imgs[1] == ref).all(-1)
     assert same.mean() >= 0.995, f"{same.mean():.4f} of pixels equal"
     assert not np.array_equal(imgs[0], imgs[1])   # the effects changed the image
+    if O.available("refgpu"):
+        # the reference's own computeEffects kernel (its GPU build, fast
+        # maths) on the same image: it pins the oracle's restatement and the
+        # CUDA path alike, up to texels whose coordinate its fast tanf / powf
+        # round across an edge
+        rg = O.ref_gpu_effects(imgs[0])
+        so = (rg == ref).all(-1).mean()
+        sg = (rg == imgs[1]).all(-1).mean()
+        print(f"{w}x{h}: reference GPU effects equal the oracle's on {so:.4f}, ours on {sg:.4f} of pixels")
+        assert so >= 0.99 and sg >= 0.99
 
 
 @pytest.mark.parametrize("mode", [1, 2])

@@ -124,10 +124,15 @@ def render_samples(r, sc, n):
     return rad[..., :3].cpu().numpy(), hit.cpu().numpy(), alb[..., :3].cpu().numpy()
 
 
-@pytest.mark.parametrize("which,n,order", [("small", 4, 0), ("small", 2, 7), ("small", 2, 5), ("full", 2, 0)])
+@pytest.mark.parametrize("which,n,order", [("small", 4, 0), ("small", 2, 7), ("small", 2, 5), ("full", 2, 0),
+                                           ("textured", 4, 0)])
 def test_per_sample_radiance(which, n, order):
     if which == "small":
         sc = S.scene_small(64, 64, n, 4)
+    elif which == "textured":   # every texture slot; its oracle is pinned to the reference's own code
+        from tests.golden.make_golden import textured_scene
+        sc = textured_scene()
+        sc.spp = n
     else:
         sc = S.scene_full(96, 54, n, 8, n_variants=2, subdiv=3, grid=3, n_lights=4)
     r = make_renderer(sc)

@@ -12,7 +12,8 @@ import pytest
 from kittlespt_gb300 import scenes as S
 from oracle import oracle as O
 
-from tests.golden.make_golden import bvh_digest, full_scene, small_scene, traversal_scene, tricky_rays, tricky_scene
+from tests.golden.make_golden import (bvh_digest, full_scene, small_scene, textured_scene, traversal_scene,
+                                     tricky_rays, tricky_scene)
 
 
 def bits(a):
@@ -154,3 +155,15 @@ def test_sensitivity_probe_is_inert_at_zero_and_deterministic():
     b = o.render_sensitivity(0, 2, 0, eps=1e-5, eps_pos=1e-6, ncopies=4)
     assert np.array_equal(a["response"], b["response"])
     assert (a["response"] > 5e-5).mean() < 0.5
+
+
+def test_textured_scene_per_sample_radiance(golden):
+    """Every texture slot -- sRGB albedo, normal map, occlusion-roughness-
+    metallic, transmission, emission (through light sampling) -- against the
+    reference's own Material::getBSDF / Texture::evaluate / Light::L
+    (material.cu:17-70, texture.cuh:34-66, light.cu:21-33), bit for bit."""
+    r = O.Scene(textured_scene()).render_samples(0, 2, rng_order=7)
+    np.testing.assert_array_equal(bits(r["radiance"]), bits(golden["tex_radiance"]))
+    np.testing.assert_array_equal(bits(r["albedo"]), bits(golden["tex_albedo"]))
+    np.testing.assert_array_equal(r["first_hit"], golden["tex_first_hit"])
+    np.testing.assert_array_equal(bits(r["first_t"]), bits(golden["tex_first_t"]))
