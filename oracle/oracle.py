@@ -438,6 +438,8 @@ class RefGpuScene:
             L.refgpu_tree_depth.argtypes = [_v, _i]
             L.refgpu_render.restype = C.c_int
             L.refgpu_render.argtypes = [_v, _f, _f, _v, _v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _v, _v]
+            L.refgpu_temporal_frame.restype = C.c_int
+            L.refgpu_temporal_frame.argtypes = [_v, _v, _v, _v, _v, C.c_int, C.c_int, C.c_int, _v, C.c_int, _v, _v]
             L.refgpu_effects.restype = C.c_int
             L.refgpu_effects.argtypes = [C.c_int, C.c_int, _f, _f]
             L.refgpu_first_hits.restype = C.c_int
@@ -516,6 +518,32 @@ class RefGpuScene:
             acc, _ = self.render(sample0 + k, 1, clear=True, max_depth=max_depth)
             out[k] = acc[..., :3]
         return out
+
+    def temporal_frame(self, frame_index, reset=False, camera=None, models=None):
+        """One frame of the reference's temporal accumulation
+        (refgpu_temporal_frame): camera = (inv_proj, inv_view) 4x4 row-major or
+        None to keep it; models = per-mesh 4x4 model matrices in the
+        reference's mesh order or None.  Returns (modulated render,
+        accumulation) [H][W][4] each."""
+        sc = self.scene
+        ip, iv, env, st = self._view(None)
+        if camera is not None:
+            ip = np.ascontiguousarray(np.asarray(camera[0], np.float32).T).reshape(-1)
+            iv = np.ascontiguousarray(np.asarray(camera[1], np.float32).T).reshape(-1)
+        elif not reset:
+            ip = iv = None
+        mp = None
+        if models is not None:
+            mp = np.ascontiguousarray(np.transpose(np.asarray(models, np.float32), (0, 2, 1))).reshape(-1)
+        render = np.zeros((sc.height, sc.width, 4), np.float32)
+        acc = np.zeros_like(render)
+        rc = self.lib().refgpu_temporal_frame(self.h, _ptr(ip) if ip is not None else None,
+                                              _ptr(iv) if iv is not None else None, env, st, sc.width, sc.height,
+                                              frame_index, _ptr(mp) if mp is not None else None, int(reset),
+                                              _ptr(render), _ptr(acc))
+        if rc != 0:
+            raise RuntimeError(self.lib().refgpu_last_error().decode())
+        return render, acc
 
     def first_hits(self):
         sc = self.scene

@@ -41,7 +41,9 @@
 #include "ref_records.h"
 #include "ref_scene.h"
 
+#include <array>
 #include <cstdio>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -104,6 +106,7 @@ struct GpuScene {
     cudaEvent_t ev[2] = {nullptr, nullptr};
     ShaderData sd;
     int blas_depth = 0, tlas_depth = 0;
+    std::vector<std::array<float, 16>> models;   // each mesh's current model matrix (column-major)
 };
 
 // deepest interior node below `root` (root depth 0; -1 for a leaf root)
@@ -237,6 +240,8 @@ void* refgpu_scene_create(int device, int ntris, const float* pos, const float* 
     GpuScene* g = new GpuScene();
     ref_replay_load_scene(&g->host, ntris, pos, nrm, uv, mat, nmeshes, mesh_off, mesh_cnt, models, nmaterials,
                           materials, ntextures, tex_desc, npixels, pixels);
+    g->models.resize(nmeshes);
+    for (int mi = 0; mi < nmeshes; ++mi) std::memcpy(g->models[mi].data(), models + 16 * mi, 64);
     RefScene& r = g->host;
     for (size_t i = 0; i < r.blas.size(); ++i)
         g->blas_depth = std::max(g->blas_depth, blas_interior_depth(r.nodes, r.blas[i].bvhnode_root_index));
@@ -359,6 +364,90 @@ int refgpu_first_hits(void* h, const float* inv_proj, const float* inv_view, con
     cudaFree(di);
     cudaFree(dt);
     if (e != cudaSuccess) return fail(std::string("refgpu_first_hits: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+// One frame of Renderer::executeRendering (renderer.cu:103-195) with
+// temporal accumulation on (integrator_use_temporal_accumulation), for the
+// parts the path stage touches: Renderer::setView (:342-354) when the camera
+// is given, Renderer::setMeshTransform (:250-269) for every mesh whose model
+// matrix differs from its current one (models: column-major, one per mesh,
+// may be null) and the TLAS rebuild of updateTLAS, the megakernel (which
+// computes the velocity and reprojects, kernels.cu:165-338), the copy of the
+// render into the accumulation texture, modulateSamples, the G-buffer copy
+// into the previous G-buffer and the camera's per-frame update.  reset = 1
+// starts a sequence: accumulation and previous G-buffer zeroed and the given
+// camera as both previous and current.  render_out receives the modulated
+// render and accum_out the accumulation texture ([H][W] RGBA each; alpha of
+// the accumulation = the history length), either may be null.
+int refgpu_temporal_frame(void* h, const float* inv_proj, const float* inv_view, const void* env, const void* settings,
+                          int W, int H, int frame_index, const float* models, int reset, float* render_out,
+                          float* accum_out) {
+    GpuScene* g = (GpuScene*)h;
+    if (!g || W <= 0 || H <= 0) return fail("refgpu_temporal_frame: bad arguments");
+    if (ensure_surfaces(*g, W, H)) return -1;
+    const EnvRecord& e = *(const EnvRecord*)env;
+    const SettingsRecord& st = *(const SettingsRecord*)settings;
+    ShaderData& sd = g->sd;
+    sd.procedural_environment_data.sun_angular_diameter_rad = e.sun_angular_diameter;
+    sd.procedural_environment_data.sun_phi_rad = e.sun_phi;
+    sd.procedural_environment_data.sun_theta_rad = e.sun_theta;
+    sd.procedural_environment_data.sun_emission_factor = e.sun_emission_factor;
+    sd.renderer_settings = RendererSettings();
+    sd.renderer_settings.integrator_max_ray_depth = st.max_depth;
+    sd.renderer_settings.integrator_use_temporal_accumulation = true;
+    if (reset) {
+        if (clear_surface(g->surf[2], W, H) || clear_surface(g->surf[4], W, H)) return -1;
+        Camera cam;
+        cam.setView(mat_from(inv_proj), mat_from(inv_view));
+        cam.setView(cam.curr_inv_projection_matrix, cam.curr_inv_view_matrix);
+        sd.scene_camera = cam;
+    } else if (inv_proj && inv_view) {
+        sd.scene_camera.setView(mat_from(inv_proj), mat_from(inv_view));
+    }
+    if (models) {
+        RefScene& r = g->host;
+        bool moved = false;
+        for (size_t mi = 0; mi < g->models.size(); ++mi) {
+            if (std::memcmp(g->models[mi].data(), models + 16 * mi, 64) == 0) continue;
+            std::memcpy(g->models[mi].data(), models + 16 * mi, 64);
+            Mat4 model = mat_from(models + 16 * mi);
+            TriangleMesh tm = r.meshes[mi];
+            tm.setTransform(model.inverse());
+            r.meshes[mi] = tm;
+            BLAS2 b = r.blas[tm.blas_index];
+            b.setTransform(model);
+            r.blas[tm.blas_index] = b;
+            moved = true;
+        }
+        if (moved) {   // updateTLAS (renderer_resource.cuh:24-26)
+            TLASBuilder tb(&r.blas, &r.tlasnodes);   // rebuilt in place, as updateTLAS does
+            r.sd.top_level_acceleration_structure = tb.build();
+            if (tlas_interior_depth(r.tlasnodes, r.sd.top_level_acceleration_structure.tlasnode_root_index) + 2 >
+                REF_STACK)
+                return fail("refgpu_temporal_frame: TLAS deeper than the reference's stack allows");
+            sd.top_level_acceleration_structure = r.sd.top_level_acceleration_structure;
+            if (r.tlasnodes.size() > g->tlasnodes.n) return fail("refgpu_temporal_frame: TLAS grew");
+            RG_CUDA(cudaMemcpy(g->tlasnodes.p, thrust::raw_pointer_cast(r.tlasnodes.data()),
+                               sizeof(TLASNode) * r.tlasnodes.size(), cudaMemcpyDefault));
+            RG_CUDA(cudaMemcpy(g->blas.p, thrust::raw_pointer_cast(r.blas.data()), sizeof(BLAS2) * r.blas.size(),
+                               cudaMemcpyDefault));
+            RG_CUDA(cudaMemcpy(g->meshes.p, thrust::raw_pointer_cast(r.meshes.data()),
+                               sizeof(TriangleMesh) * r.meshes.size(), cudaMemcpyDefault));
+            sd.tlas_nodes_buffer = Buffer<TLASNode>(g->tlasnodes.p, r.tlasnodes.size());
+        }
+    }
+    sd.frame_index = frame_index;
+    KittlesPT::launchPathTraceComputeMegaKernel(sd);
+    const size_t pitch = (size_t)W * sizeof(float4);
+    RG_CUDA(cudaMemcpy2DArrayToArray(g->surf[2].arr, 0, 0, g->surf[1].arr, 0, 0, pitch, H, cudaMemcpyDeviceToDevice));
+    KittlesPT::launchModulateComputeKernel(sd);
+    if (render_out)
+        RG_CUDA(cudaMemcpy2DFromArray(render_out, pitch, g->surf[1].arr, 0, 0, pitch, H, cudaMemcpyDeviceToHost));
+    if (accum_out)
+        RG_CUDA(cudaMemcpy2DFromArray(accum_out, pitch, g->surf[2].arr, 0, 0, pitch, H, cudaMemcpyDeviceToHost));
+    RG_CUDA(cudaMemcpy2DArrayToArray(g->surf[4].arr, 0, 0, g->surf[3].arr, 0, 0, pitch, H, cudaMemcpyDeviceToDevice));
+    sd.scene_camera.setView(sd.scene_camera.curr_inv_projection_matrix, sd.scene_camera.curr_inv_view_matrix);
     return 0;
 }
 
