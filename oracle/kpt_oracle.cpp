@@ -746,9 +746,13 @@ struct GGX {
         float g1l = (2.0f * nl) / (nl + tl);
         return g1v * g1l;
     }
-    f3 sample_wm(f2 u) const {  // bsdf.cuh:59-74
+    // xs (rounding-sensitivity probe only, 1 otherwise) scales the cosine
+    // before the inverse cosine
+    f3 sample_wm(f2 u, float xs = 1.0f) const {  // bsdf.cuh:59-74
         float a2 = Sqr(alpha);
-        float theta = acosf(sqrtf((1.0f - u.x) / ((a2 - 1.0f) * u.x + 1.0f)));
+        float x = sqrtf((1.0f - u.x) / ((a2 - 1.0f) * u.x + 1.0f));
+        if (xs != 1.0f) x = fminf(x * xs, 1.0f);
+        float theta = acosf(x);
         float phi = 2.0f * PI * u.y;
         f3 wm = {sinf(theta) * cosf(phi), sinf(theta) * sinf(phi), cosf(theta)};
         return normalize(wm);
@@ -852,10 +856,10 @@ struct BSDF {  // UnifiedBSDF, bsdf.cuh:166-624
         float pd = pdf_diffuse(wo, wi);
         return 0.5f * (ps + pd);
     }
-    BSDFSample sample_opaque(f3 wo, f2 u, float X) const {
+    BSDFSample sample_opaque(f3 wo, f2 u, float X, float xs = 1.0f) const {
         BSDFSample bs;
         if (X < 0.5f) {
-            f3 wm = ggx.sample_wm(u);
+            f3 wm = ggx.sample_wm(u, xs);
             f3 wi = reflect(-wo, wm);
             f3 f = f_glossy(wo, wi, wm) * 2.0f;
             bs.scatter = GLOSSY | REFLECTED; bs.f = f; bs.wi = wi; bs.pdf = pdf_glossy(wo, wi, wm);
@@ -883,18 +887,18 @@ struct BSDF {  // UnifiedBSDF, bsdf.cuh:166-624
         return M;
     }
     float pdf_conductor(f3 wo, f3 wi) const { return pdf_glossy(wo, wi, normalize(wo + wi)); }
-    BSDFSample sample_conductor(f3 wo, f2 u) const {
-        f3 wm = ggx.sample_wm(u);
+    BSDFSample sample_conductor(f3 wo, f2 u, float xs = 1.0f) const {
+        f3 wm = ggx.sample_wm(u, xs);
         f3 wi = reflect(-wo, wm);
         BSDFSample bs;
         bs.scatter = GLOSSY | REFLECTED; bs.f = f_conductor(wo, wi); bs.wi = wi;
         bs.pdf = pdf_glossy(wo, wi, wm);
         return bs;
     }
-    BSDFSample sample_transparent(f3 wo, f2 u, float X) const {
+    BSDFSample sample_transparent(f3 wo, f2 u, float X, float xs = 1.0f) const {
         bool inside = backface;
         float eta = inside ? (1.0f / ior) : ior;
-        f3 ht = ggx.sample_wm(u);
+        f3 ht = ggx.sample_wm(u, xs);
         f3 wi = {0, 0, 0};
         bool tir = !refract_(wo, ht, eta, &wi);
         BSDFSample bs;
@@ -973,14 +977,14 @@ struct BSDF {  // UnifiedBSDF, bsdf.cuh:166-624
         if (wd > 0.0f) p += wd * pdf_opaque(wo, wi);
         return p;
     }
-    BSDFSample sample(f3 w_wo, f2 u, f2 X) const {
+    BSDFSample sample(f3 w_wo, f2 u, f2 X, float xs = 1.0f) const {
         f3 wo = mul(transpose(basis), w_wo);
         float pm = metallic;
         float pt = (1.0f - pm) * transmission;
         BSDFSample bs;
-        if (X.x < pm) bs = sample_conductor(wo, u);
-        else if (X.x < pt) bs = sample_transparent(wo, u, X.y);
-        else bs = sample_opaque(wo, u, X.y);
+        if (X.x < pm) bs = sample_conductor(wo, u, xs);
+        else if (X.x < pt) bs = sample_transparent(wo, u, X.y, xs);
+        else bs = sample_opaque(wo, u, X.y, xs);
         bs.wi = mul(basis, bs.wi);
         return bs;
     }
@@ -1192,9 +1196,16 @@ struct Frame {
 // geometric normal, area-light sample point, surface point and the path
 // throughput -- are moved by a relative amount of at most eps (directions,
 // normals, throughput) or eps_pos (points) in a pseudo-random direction drawn
-// from its own stream, the sample's random numbers being unchanged.  Camera
-// rays, traversal and the sun's target are computed exactly alike everywhere
-// and are not moved.  A
+// from its own stream.  The inputs of the computations that amplify rounding
+// are moved by eps_pos too: the interpolated texture coordinates (a texel
+// edge) and the random numbers that the BSDF and the light sampler map to a
+// direction or a point, and by a few ulps the cosine of the sampled GGX
+// microfacet normal (near the lobe's axis its inverse cosine turns one ulp of
+// a value next to 1 into ~1e-4 of angle, ~1e-3 at roughness 0.01); the
+// numbers that choose a lobe, a light
+// or the sun, and Russian roulette's, are the same in every build and are
+// not moved.  Camera rays, traversal and the sun's target are computed
+// exactly alike everywhere and are not moved either.  A
 // sample whose radiance moves by more than the parity tolerance under such a
 // perturbation of a few ulps sits at a decision that rounding can flip (a ray
 // grazing a triangle edge or silhouette, a shadow ray grazing an occluder, a
@@ -1216,6 +1227,13 @@ struct Perturb {
     f3 scale(f3 v) {
         float a = next(); float b = next(); float c = next();
         return {v.x * (1.0f + eps * a), v.y * (1.0f + eps * b), v.z * (1.0f + eps * c)};
+    }
+    f2 uv(f2 v) {   // relative eps_pos, kept in [0, 1] where the value was
+        float a = next(); float b = next();
+        f2 r = {v.x * (1.0f + eps_pos * a), v.y * (1.0f + eps_pos * b)};
+        if (v.x <= 1.0f && r.x > 1.0f) r.x = v.x;
+        if (v.y <= 1.0f && r.y > 1.0f) r.y = v.y;
+        return r;
     }
 };
 
@@ -1259,7 +1277,7 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c,
         }
         if (first) { out.first_prim = h.prim; out.first_inst = h.inst; out.first_t = h.t; }
         Surface si = surface_interaction(s, h, ray);
-        if (P) { si.pos = P->point(si.pos); si.ng = P->dir(si.ng); }
+        if (P) { si.pos = P->point(si.pos); si.ng = P->dir(si.ng); si.uv = P->uv(si.uv); }
         f3 Le = F3(0.0f);
         if (si.light >= 0) Le = light_L(s, s.lights[si.light], si.uv);
         if (nonzero(Le)) {
@@ -1321,6 +1339,7 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c,
                     const Light& lt = s.lights[li];
                     float prob = 1.0f / (float)nl;
                     f2 u = S.get2D();
+                    if (P) u = P->uv(u);
                     // Light::sampleLi (light.cu:35-45) + Triangle::sample (triangle.cuh:104-118)
                     const Tri& tr = s.tris[lt.prim];
                     const M4& model = s.mesh_model[tr.mesh];
@@ -1361,7 +1380,12 @@ static PathResult Li(const Frame& F, const Ray& ray_in, Sampler& S, Counters& c,
         f2 u, X;
         if ((F.rng_order & 4) == 0) { u = S.get2D(); X = S.get2D(); }
         else { X = S.get2D(); u = S.get2D(); }
-        BSDFSample bs = bsdf.sample(wo, u, X);
+        float xs = 1.0f;
+        if (P) {
+            u = P->uv(u);
+            if (P->eps > 0.0f) xs = 1.0f + 4.0f * FLT_EPSILON * P->next();   // a few ulps of the microfacet cosine
+        }
+        BSDFSample bs = bsdf.sample(wo, u, X, xs);
         if (bs.scatter == ABSORBED || !nonzero(bs.f)) break;
         beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
         if (P) beta = P->scale(beta);

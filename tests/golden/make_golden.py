@@ -59,7 +59,14 @@ def textured_scene():
     texture on the conductor, the albedo texture again on the ground, a
     glass pane with a transmission texture and an emitter with an emission
     texture above the spheres.  Textures have 3 or 4 channels and odd sizes;
-    the last texel of the last texture sits at the end of the pixel buffer."""
+    the last texel of the last texture sits at the end of the pixel buffer.
+    The roughness channel of the ORM texture stays at or above 64/255 (a
+    roughness of at least 0.15 on the conductor): below ~0.03 (alpha < 1e-3)
+    the reference treats the lobe as smooth -- no light sample, D clamped --
+    yet samples its microfacet normal with the raw alpha, where the normal's
+    cosine is within ~alpha^2 of 1 and a fast-maths build's ulps move the
+    sampled angle by percent: no two builds agree there, and the scene
+    measures texture parity instead."""
     sc = S.scene_small(40, 40, 2, 4)
     rng = np.random.default_rng(77)
     tex = [rng.integers(0, 256, (9, 13, 3), dtype=np.uint8),    # albedo (sRGB)
@@ -85,6 +92,7 @@ def textured_scene():
                     S.Instance(1, S.translate(0, -1.0, 0).astype(np.float32), 2),
                     S.Instance(2, S.translate(0.5, 1.3, 0.5).astype(np.float32), 3),
                     S.Instance(3, S.translate(0, 2.5, 0).astype(np.float32), 4)]
+    tex[2][..., 1] = 64 + (tex[2][..., 1].astype(np.int32) * 191) // 255
     sc.textures = tex
     return sc
 

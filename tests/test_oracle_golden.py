@@ -151,10 +151,10 @@ def test_sensitivity_probe_is_inert_at_zero_and_deterministic():
     z = o.render_sensitivity(0, 2, 0, eps=0.0, eps_pos=0.0, ncopies=2)
     assert np.array_equal(z["radiance"], ref["radiance"])
     assert not z["response"].any()
-    a = o.render_sensitivity(0, 2, 0, eps=1e-5, eps_pos=1e-6, ncopies=4)
-    b = o.render_sensitivity(0, 2, 0, eps=1e-5, eps_pos=1e-6, ncopies=4)
+    a = o.render_sensitivity(0, 2, 0, eps=1e-4, eps_pos=1e-5, ncopies=4)
+    b = o.render_sensitivity(0, 2, 0, eps=1e-4, eps_pos=1e-5, ncopies=4)
     assert np.array_equal(a["response"], b["response"])
-    assert (a["response"] > 5e-5).mean() < 0.5
+    assert np.median(a["response"]) < 1e-4
 
 
 def test_textured_scene_per_sample_radiance(golden):
