@@ -330,18 +330,13 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * pixel order (results are the same either way); fetch_batch: in the ray
  * kernels, the lanes of a warp whose rays are done wait until this many are
  * (or the whole warp is) and then store their results and fetch their next
- * rays together (1 .. 32, 0 = 7; results are the same for every value);
- * tail_paths: once at most this many paths enter a level of the wave, one
- * thread finishes each of them -- shading, shadow ray and continuation --
- * instead of launching the remaining levels (0 = the default, a negative
- * value never; results are the same either way). */
+ * rays together (1 .. 32, 0 = 7; results are the same for every value). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;
     int32_t shade_block;
     int32_t sort_rays;
     int32_t fetch_batch;
-    int32_t tail_paths;
 } kpt_tuning;
 void kpt_tuning_default(kpt_tuning* t);
 kpt_status kpt_set_tuning(kpt_context* ctx, const kpt_tuning* t);

@@ -198,9 +198,6 @@ static constexpr size_t ADJ_WAVE_BYTES = (size_t)12 << 30;
 // pixel-major waves and shading blocks of 256 (20.51 ms; 6: 20.55-20.60, 8:
 // 20.53, 5: 20.65, 4: 20.83)
 static constexpr int FETCH_BATCH = 7;
-// default of kpt_tuning.tail_paths: the wave's tail takes over a level that
-// at most this many paths enter
-static constexpr int TAIL_PATHS = 1 << 16;
 // threads per block of the shading kernel unless tuned (256: 22.48 ms on the
 // 1080p16 frame against 22.51 with 128 and 64)
 static constexpr int SHADE_BLOCK = SHADE_MAX_BLOCK;
@@ -943,9 +940,6 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     F.unsorted = c->tuning.sort_rays ? c->unsorted.p : nullptr;
     F.octants = c->octants.p;
     F.cap = c->wave_cap;
-    // the tail is off where the continuations are sorted (it reads a level's
-    // paths in place)
-    F.tail_paths = (F.unsorted || c->tuning.tail_paths < 0) ? 0 : c->tuning.tail_paths;
     F.primary = c->primary.p;
     F.hit_list = c->hit_list.p;
     F.hit_index = c->hit_index.p;
@@ -1034,8 +1028,6 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     // streams, joined before k_shade(l + 1); serial when stages are timed
     const bool fork = c->tf == nullptr && c->ev_fork.size() >= (size_t)D + 1;
     const int g_sky = persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK);
-    const int g_tail = std::max(1, std::min((F.tail_paths + TAIL_BLOCK - 1) / TAIL_BLOCK,
-                                            persistent_grid(c, (const void*)k_tail, TAIL_BLOCK)));
     for (long long w0 = 0; w0 < items; w0 += F.cap) {
         cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
         // the sky queue's length when the wave starts: where its level 0 begins
@@ -1047,10 +1039,6 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
             if (l > 0) {
                 stage_mark(c, KPT_STAGE_EXTEND);
                 k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
-                if (F.tail_paths > 0) {   // returns at once unless few paths enter level l
-                    k_tail<<<g_tail, TAIL_BLOCK, 0, s>>>(F, l);
-                    c->launches += 1;
-                }
                 if (fork) cudaStreamWaitEvent(s, c->ev_join[l - 1], 0);
             }
             stage_mark(c, KPT_STAGE_SHADE);
@@ -1626,7 +1614,6 @@ void kpt_tuning_default(kpt_tuning* t) {
     t->shade_block = SHADE_BLOCK;
     t->sort_rays = 0;
     t->fetch_batch = FETCH_BATCH;
-    t->tail_paths = TAIL_PATHS;
 }
 
 kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
@@ -1643,7 +1630,6 @@ kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
     c->tuning = *t;
     if (c->tuning.shade_block == 0) c->tuning.shade_block = SHADE_BLOCK;
     if (c->tuning.fetch_batch == 0) c->tuning.fetch_batch = FETCH_BATCH;
-    if (c->tuning.tail_paths == 0) c->tuning.tail_paths = TAIL_PATHS;
     c->view.fetch_batch = c->tuning.fetch_batch;
     return KPT_OK;
 }

@@ -9,7 +9,6 @@ namespace kpt {
 constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
 constexpr int SHADE_MAX_BLOCK = 256;   // largest block k_shade is launched with (kpt_tuning.shade_block)
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
-constexpr int TAIL_BLOCK = 64;     // threads per block of the wave's tail (k_tail)
 // k_primary: a warp traces a TILE_W x (32 / TILE_W) tile of pixels, a
 // block of PATH_BLOCK = 128 threads a 2 x 2 arrangement of them
 #ifndef KPT_TILE_W
@@ -89,17 +88,7 @@ struct FrameParams {
     PathRec* unsorted;         // [cap] k_shade's continuations before the octant sort, null: no sort
     int* octants;              // [16 * (max_depth + 2)] per level: paths per direction octant, cursors
     int cap;
-    int tail_paths;            // k_tail finishes the paths of a level once at most this many enter it (0: never)
 };
-
-// The level from which the wave's tail (k_tail) has finished the wave's
-// paths, 0 if none: word 6 of the counters after the last level, zeroed with
-// them when a wave starts.  The later launches of that level and those of
-// the following levels return at once.
-__device__ __forceinline__ bool tail_taken(const FrameParams& F, int level) {
-    const int t = F.level_counts[LEVEL_WORDS * (F.max_depth + 1) + 6];
-    return t != 0 && t <= level;
-}
 
 // ---------------------------------------------------------------------------
 // path-replay adjoint (kpt_adjoint.cu)
@@ -235,7 +224,6 @@ __global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, fl
                         int* inst, int* tri, float* t, float2* uv, int* next, unsigned long long* counters);
 __global__ void k_occluded(SceneView s, int n, const float3* o, const float3* d, float tmin, const float* tmax,
                            uint8_t* out, int* next, unsigned long long* counters);
-__global__ void k_tail(FrameParams F, int level);
 __global__ void k_sun_constants_gpu(float phi, float theta, float diameter, float* out);
 __global__ void k_trace_chains(SceneView s, int n, const float3* o, const float3* d, int nbounces, int* inst,
                                int* tri, float* t, int* next, unsigned long long* counters);

@@ -116,17 +116,11 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary_sky(FrameParams F) {
 
 // Shadow ray of Integrator::unoccluded (integrator.cuh:124-131): from the
 // offset surface point towards `target`, stopping 0.11 short of it.
-__device__ __forceinline__ void shadow_ray(const Surf& si, float3 target, float3& o, float3& d, float& tmax) {
-    o = si.backface ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
-    d = normalize(target - o);
-    tmax = length(target - o) - 0.11f;
-}
-
 __device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si, float3 target, float3 contrib,
                                             int item, int* counter, bool from_back) {
-    float3 o, d;
-    float tmax;
-    shadow_ray(si, target, o, d, tmax);
+    float3 o = si.backface ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+    float3 d = normalize(target - o);
+    float tmax = length(target - o) - 0.11f;
     int j = group_append(counter);
     if (from_back) j = F.cap - 1 - j;
     ShadowRec r;
@@ -146,188 +140,11 @@ __device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si
 // emission here, its light sample in k_shadow, the next vertex's terms at the
 // next level, the sky last.  Level 0 starts the paths of items
 // wave0 .. wave0+cap-1 from the camera-ray hits of k_primary.
-// One vertex of Integrator::Li for one path (the loop body of shade_level,
-// below): `h` is the path's hit at this level; o, d the ray that found it;
-// beta, p_b, prev and seed the path's throughput, BSDF pdf, previous vertex
-// and random-number state; L its radiance so far.  The vertex's outcomes go
-// to `sink`: the sky direction of a path that left the scene (its last
-// term), the radiance after this vertex's emission, the shadow ray of its
-// light sample with the radiance it adds if unoccluded (sun: true for a sun
-// sample), and the continuation (a PathRec, the next level's input).
-template <class Sink>
-__device__ __forceinline__ void shade_vertex(const FrameParams& F, int level, const PrimaryRec& h, float3 o, float3 d,
-                                             float3 beta, float3 prev, float3 L, float p_b, uint32_t seed, int item,
-                                             Sink& sink) {
+__device__ __forceinline__ void shade_level(const FrameParams& F, int level, long long wave0) {
     const SceneView& s = F.scene;
     const SkyParams& P = F.sky;
     const int order = F.rng_order;
     const int nl = s.nlights;
-    const bool first = level == 0;
-    if (h.inst < 0) {
-        sink.sky(item, d, beta, L);   // the path ends here: the sky is its last term
-        return;
-    }
-    Sampler S;
-    S.seed = seed + (uint32_t)level;
-    Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
-    float3 Le = make_float3(0.0f, 0.0f, 0.0f);
-    if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
-    if (nonzero(Le)) {
-        float w_l = 1.0f;
-        if (si.light >= 0 && !first) {
-            const LightRec& lt = s.lights[si.light];
-            float pmf = 1.0f / (float)nl;
-            float dist = length(si.pos - prev);
-            float cosl = AbsDot(normalize(si.pos - prev), si.ng);
-            float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
-            w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
-        }
-        L = L + Le * w_l * beta;
-    }
-    Bsdf bsdf = bsdf_at(s, si);
-    if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);   // demodulate (bsdf.cuh:286-288)
-    if (!first && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
-    const float3 wo = -d;
-    if (!(bsdf.alpha < 0.001f)) {
-        // The light sample: each branch draws its numbers and sets up its
-        // direction; the BSDF is then evaluated once for all lanes (the
-        // sun / area-light choice is random per lane, so both branches
-        // run in every warp), and each branch finishes its own sample.
-        const bool sun = S.get1D() < 0.5f;
-        const float dsun = 149.597e9f;
-        // the sun's centre at 1 AU, each product rounded on its own:
-        // target - sun_pos below cancels two values near 1.5e11, which a
-        // fused multiply-add would shift by up to half their ulp (~1e-5
-        // of the difference) -- as the reference's GPU build does, with
-        // gpu_arith
-        const float3 sun_pos = P.gpu_arith ? P.sun_dir * dsun
-                                           : make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
-                                                         __fmul_rn(P.sun_dir.z, dsun));
-        float3 wi = P.sun_dir, target, Lem;
-        float pdf = 0.0f, prob = 0.0f;
-        bool eval;
-        if (sun) {
-            // sampleLdSun: jittered point on the sun disc at 1 AU
-            float3 off;
-            if ((order & RNG_SUN) == 0) {
-                float2 a = S.get2D(order);
-                float b = S.get1D();
-                off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
-            } else {
-                float b = S.get1D();
-                float2 a = S.get2D(order);
-                off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
-            }
-            target = P.gpu_arith ? sun_pos + (off * P.sun_radius_m)
-                                 : make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
-                                               __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
-                                               __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
-            eval = true;
-        } else {
-            // sampleLd: uniform light pick, uniform point on the triangle
-            float X = S.get1D();
-            eval = false;
-            if (nl >= 1) {
-                int li = min((int)(X * (float)nl), nl - 1);
-                const LightRec& lt = s.lights[li];
-                prob = 1.0f / (float)nl;
-                float2 uu = S.get2D(order);
-                const InstRec& lir = s.inst[lt.inst];
-                float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
-                float bx, by;
-                if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
-                else { by = uu.y / 2.0f; bx = uu.x - by; }
-                float bz = 1.0f - bx - by;
-                float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
-                                         bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
-                float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
-                p = row3(model, p, 1.0f);
-                float3 gn = row3(model, lt.gn, 0.0f);
-                pdf = 1.0f / lt.tri_area;
-                pdf *= Sqr(length(p - si.pos));
-                pdf /= AbsDot(normalize(p - si.pos), gn);
-                wi = normalize(p - si.pos);
-                Lem = emission_of(s, lt.material, luv);
-                target = p;
-                eval = !(pdf <= 0.0f || !nonzero(Lem));
-            }
-        }
-        float3 fcos = make_float3(0.0f, 0.0f, 0.0f);
-        if (eval) fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
-        if (sun) {
-            const float3 sun_rad = *F.sun_radiance;
-            if (nonzero(fcos) && nonzero(sun_rad)) {
-                float area = PI_F * Sqr(P.sun_radius_m);
-                float3 sn = normalize(target - sun_pos), wt = normalize(target - si.pos);
-                float th = AbsDot(sn, -wt);
-                float spdf = (1.0f / area) / (th / Sqr(dsun));
-                float3 Ld = (fcos * sun_rad * 6.0e5f) / spdf;
-                float3 c = Ld * beta / 0.5f;
-                if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
-                    sink.shadow(si, target, c, item, true);
-            }
-        } else if (eval && nonzero(fcos)) {
-            float p_l = prob * pdf;
-            float pb = bsdf.pdf(wo, wi);
-            float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
-            float3 Ld = (Lem * fcos * w_l) / p_l;
-            float3 c = Ld * beta / (1.0f - 0.5f);
-            if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
-                sink.shadow(si, target, c, item, false);
-        }
-    }
-    sink.radiance(item, L);
-    if (level == F.max_depth) return;
-    float2 uu, X;
-    if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
-    else { X = S.get2D(order); uu = S.get2D(order); }
-    BsdfSample bs = bsdf.sample(wo, uu, X);
-    if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) return;
-    beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
-    p_b = bsdf.pdf(wo, bs.wi);
-    o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
-    float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
-    if (mx < 1.0f && level >= 1) {
-        float q = fmaxf(0.0f, 1.0f - mx);
-        if (S.get1D() < q) return;
-        beta = beta / (1.0f - q);
-    }
-    if (!nonzero(beta)) return;   // while (throughput) (integrator.cuh:266)
-    PathRec pr;
-    pr.o_pb = make_float4(o.x, o.y, o.z, p_b);
-    pr.d_seed = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, __uint_as_float(S.seed));
-    pr.beta_item = make_float4(beta.x, beta.y, beta.z, __int_as_float(item));
-    pr.prev = make_float4(si.pos.x, si.pos.y, si.pos.z, 0.0f);
-    sink.next(pr);
-}
-
-// The wave's sink: sky lookups, shadow rays and continuations appended to the
-// level's compacted queues, the radiance written back to the item.
-struct WaveSink {
-    const FrameParams& F;
-    int* here;        // level_counts of this level
-    int* ahead;       // level_counts of the next level
-    PathRec* out;     // the next level's paths
-    __device__ __forceinline__ void sky(int item, float3 d, float3 beta, float3) {
-        const int q = group_append(F.counts + 2);
-        F.sky_queue[2 * (size_t)q] = make_float4(__int_as_float(item), d.x, d.y, d.z);
-        F.sky_queue[2 * (size_t)q + 1] = make_float4(beta.x, beta.y, beta.z, 0.0f);
-    }
-    __device__ __forceinline__ void radiance(int item, float3 L) {
-        F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
-    }
-    __device__ __forceinline__ void shadow(const Surf& si, float3 target, float3 c, int item, bool sun) {
-        if (sun) emit_shadow(F, si, target, c, item, here + 1, false);
-        else emit_shadow(F, si, target, c, item, here + 2, true);
-    }
-    __device__ __forceinline__ void next(const PathRec& pr) {
-        const int j = group_append(ahead);
-        out[j] = pr;
-    }
-};
-
-__device__ __forceinline__ void shade_level(const FrameParams& F, int level, long long wave0) {
-    if (tail_taken(F, level)) return;
     const bool first = level == 0;
     int n;
     if (first) {
@@ -383,8 +200,146 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
             const float4 l4 = F.radiance[item];
             L = make_float3(l4.x, l4.y, l4.z);
         }
-        WaveSink sink{F, here, next, out};
-        shade_vertex(F, level, h, o, d, beta, prev, L, p_b, seed, item, sink);
+        if (h.inst < 0) {
+            // the sky is evaluated by k_sky_queue; the path ends here
+            const int q = group_append(F.counts + 2);
+            F.sky_queue[2 * (size_t)q] = make_float4(__int_as_float(item), d.x, d.y, d.z);
+            F.sky_queue[2 * (size_t)q + 1] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+            continue;
+        }
+        Sampler S;
+        S.seed = seed + (uint32_t)level;
+        Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
+        float3 Le = make_float3(0.0f, 0.0f, 0.0f);
+        if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
+        if (nonzero(Le)) {
+            float w_l = 1.0f;
+            if (si.light >= 0 && !first) {
+                const LightRec& lt = s.lights[si.light];
+                float pmf = 1.0f / (float)nl;
+                float dist = length(si.pos - prev);
+                float cosl = AbsDot(normalize(si.pos - prev), si.ng);
+                float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
+                w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
+            }
+            L = L + Le * w_l * beta;
+        }
+        Bsdf bsdf = bsdf_at(s, si);
+        if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);   // demodulate (bsdf.cuh:286-288)
+        if (!first && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
+        const float3 wo = -d;
+        if (!(bsdf.alpha < 0.001f)) {
+            // The light sample: each branch draws its numbers and sets up its
+            // direction; the BSDF is then evaluated once for all lanes (the
+            // sun / area-light choice is random per lane, so both branches
+            // run in every warp), and each branch finishes its own sample.
+            const bool sun = S.get1D() < 0.5f;
+            const float dsun = 149.597e9f;
+            // the sun's centre at 1 AU, each product rounded on its own:
+            // target - sun_pos below cancels two values near 1.5e11, which a
+            // fused multiply-add would shift by up to half their ulp (~1e-5
+            // of the difference) -- as the reference's GPU build does, with
+            // gpu_arith
+            const float3 sun_pos = P.gpu_arith ? P.sun_dir * dsun
+                                               : make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
+                                                             __fmul_rn(P.sun_dir.z, dsun));
+            float3 wi = P.sun_dir, target, Lem;
+            float pdf = 0.0f, prob = 0.0f;
+            bool eval;
+            if (sun) {
+                // sampleLdSun: jittered point on the sun disc at 1 AU
+                float3 off;
+                if ((order & RNG_SUN) == 0) {
+                    float2 a = S.get2D(order);
+                    float b = S.get1D();
+                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                } else {
+                    float b = S.get1D();
+                    float2 a = S.get2D(order);
+                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+                }
+                target = P.gpu_arith ? sun_pos + (off * P.sun_radius_m)
+                                     : make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
+                                                   __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
+                                                   __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
+                eval = true;
+            } else {
+                // sampleLd: uniform light pick, uniform point on the triangle
+                float X = S.get1D();
+                eval = false;
+                if (nl >= 1) {
+                    int li = min((int)(X * (float)nl), nl - 1);
+                    const LightRec& lt = s.lights[li];
+                    prob = 1.0f / (float)nl;
+                    float2 uu = S.get2D(order);
+                    const InstRec& lir = s.inst[lt.inst];
+                    float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
+                    float bx, by;
+                    if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
+                    else { by = uu.y / 2.0f; bx = uu.x - by; }
+                    float bz = 1.0f - bx - by;
+                    float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
+                                             bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
+                    float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
+                    p = row3(model, p, 1.0f);
+                    float3 gn = row3(model, lt.gn, 0.0f);
+                    pdf = 1.0f / lt.tri_area;
+                    pdf *= Sqr(length(p - si.pos));
+                    pdf /= AbsDot(normalize(p - si.pos), gn);
+                    wi = normalize(p - si.pos);
+                    Lem = emission_of(s, lt.material, luv);
+                    target = p;
+                    eval = !(pdf <= 0.0f || !nonzero(Lem));
+                }
+            }
+            float3 fcos = make_float3(0.0f, 0.0f, 0.0f);
+            if (eval) fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
+            if (sun) {
+                const float3 sun_rad = *F.sun_radiance;
+                if (nonzero(fcos) && nonzero(sun_rad)) {
+                    float area = PI_F * Sqr(P.sun_radius_m);
+                    float3 sn = normalize(target - sun_pos), wt = normalize(target - si.pos);
+                    float th = AbsDot(sn, -wt);
+                    float spdf = (1.0f / area) / (th / Sqr(dsun));
+                    float3 Ld = (fcos * sun_rad * 6.0e5f) / spdf;
+                    float3 c = Ld * beta / 0.5f;
+                    if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                        emit_shadow(F, si, target, c, item, here + 1, false);
+                }
+            } else if (eval && nonzero(fcos)) {
+                float p_l = prob * pdf;
+                float pb = bsdf.pdf(wo, wi);
+                float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
+                float3 Ld = (Lem * fcos * w_l) / p_l;
+                float3 c = Ld * beta / (1.0f - 0.5f);
+                if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                    emit_shadow(F, si, target, c, item, here + 2, true);
+            }
+        }
+        F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
+        if (level == F.max_depth) continue;
+        float2 uu, X;
+        if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
+        else { X = S.get2D(order); uu = S.get2D(order); }
+        BsdfSample bs = bsdf.sample(wo, uu, X);
+        if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) continue;
+        beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
+        p_b = bsdf.pdf(wo, bs.wi);
+        o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+        float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
+        if (mx < 1.0f && level >= 1) {
+            float q = fmaxf(0.0f, 1.0f - mx);
+            if (S.get1D() < q) continue;
+            beta = beta / (1.0f - q);
+        }
+        if (!nonzero(beta)) continue;   // while (throughput) (integrator.cuh:266)
+        const int j = group_append(next);
+        PathRec pr;
+        pr.o_pb = make_float4(o.x, o.y, o.z, p_b);
+        pr.d_seed = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, __uint_as_float(S.seed));
+        pr.beta_item = make_float4(beta.x, beta.y, beta.z, __int_as_float(item));
+        pr.prev = make_float4(si.pos.x, si.pos.y, si.pos.z, 0.0f);
+        out[j] = pr;
     }
 }
 
@@ -395,95 +350,6 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, 
 }
 __global__ void __launch_bounds__(SHADE_MAX_BLOCK) k_shade_wide(FrameParams F, int level, long long wave0) {
     shade_level(F, level, wave0);
-}
-
-// ---------------------------------------------------------------------------
-// the wave's tail: one thread finishes a path
-
-// The tail's sink: the vertex's outcomes stay with the thread.
-struct TailSink {
-    bool missed = false, has_shadow = false, has_next = false, sun = false;
-    float3 L, so, sd, contrib;
-    float stmax;
-    PathRec next_rec;
-    __device__ __forceinline__ void sky(int, float3, float3, float3) { missed = true; }
-    __device__ __forceinline__ void radiance(int, float3 Lv) { L = Lv; }
-    __device__ __forceinline__ void shadow(const Surf& si, float3 target, float3 c, int, bool is_sun) {
-        shadow_ray(si, target, so, sd, stmax);
-        contrib = c;
-        has_shadow = true;
-        sun = is_sun;
-    }
-    __device__ __forceinline__ void next(const PathRec& pr) {
-        next_rec = pr;
-        has_next = true;
-    }
-};
-
-// When at most F.tail_paths paths enter `level` (kpt_tuning.tail_paths), one
-// thread finishes each of them: it shades every remaining vertex, traces the
-// vertex's shadow ray and its continuation itself (trace_any,
-// trace_closest: the same answers as the wave's queue traversal) and adds
-// the terms to the path's radiance in the wave's order -- the vertex's
-// emission, its light sample if unoccluded, the next vertex's terms, the sky
-// last -- and it marks the wave as finished from `level` on, so that the
-// later levels' launches return at once.  A wave launch lasts as long as its
-// slowest ray however few rays it holds; the tail pays that latency once per
-// path instead of once per level.  It counts its rays into the level
-// counters as the wave would.
-__global__ void __launch_bounds__(TAIL_BLOCK) k_tail(FrameParams F, int level) {
-    int* flag = F.level_counts + LEVEL_WORDS * (F.max_depth + 1) + 6;
-    const int taken = *flag;
-    if (taken != 0 && taken != level) return;
-    const int n = F.level_counts[LEVEL_WORDS * level];
-    if (n == 0 || n > F.tail_paths) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *flag = level;   // read back by the level's later launches only
-    int stack[STACK_WORDS];
-    TraceStats ext = {0, 0, 0, 0}, shd = {0, 0, 0, 0};
-    const SkyParams& P = F.sky;
-    const float3 obs = make_float3(0.0f, P.earth_r + 1.0f, 0.0f);
-    const PathRec* in = F.paths[level & 1];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        PathRec pr = in[i];
-        PrimaryRec h = F.hits[i];
-        const int item = __float_as_int(pr.beta_item.w);
-        const float4 l4 = F.radiance[item];
-        float3 L = make_float3(l4.x, l4.y, l4.z);
-        for (int l = level;; ++l) {
-            const float3 o = make_float3(pr.o_pb.x, pr.o_pb.y, pr.o_pb.z);
-            const float3 d = make_float3(pr.d_seed.x, pr.d_seed.y, pr.d_seed.z);
-            const float3 beta = make_float3(pr.beta_item.x, pr.beta_item.y, pr.beta_item.z);
-            const float3 prev = make_float3(pr.prev.x, pr.prev.y, pr.prev.z);
-            if (h.inst < 0) {   // k_sky_queue's term: the path's last
-                const float3 sk = nishita(P, obs, d);
-                L = make_float3(L.x + sk.x * beta.x, L.y + sk.y * beta.y, L.z + sk.z * beta.z);
-                break;
-            }
-            TailSink t;
-            shade_vertex(F, l, h, o, d, beta, prev, L, pr.o_pb.w, __float_as_uint(pr.d_seed.w), item, t);
-            L = t.L;
-            if (t.has_shadow) {   // k_shadow's term
-                atomicAdd(F.level_counts + LEVEL_WORDS * l + (t.sun ? 1 : 2), 1);
-                if (!trace_any(F.scene, make_xray(t.so, t.sd), 0.0f, t.stmax, shd, stack))
-                    L = make_float3(L.x + t.contrib.x, L.y + t.contrib.y, L.z + t.contrib.z);
-            }
-            if (!t.has_next) break;
-            pr = t.next_rec;
-            atomicAdd(F.level_counts + LEVEL_WORDS * (l + 1), 1);
-            const Hit hh = trace_closest(F.scene,
-                                         make_xray(make_float3(pr.o_pb.x, pr.o_pb.y, pr.o_pb.z),
-                                                   make_float3(pr.d_seed.x, pr.d_seed.y, pr.d_seed.z)),
-                                         0.0f, __int_as_float(0x7f800000), ext, stack);
-            h.t = hh.t;
-            h.u = hh.u;
-            h.v = hh.v;
-            h.inst = hh.inst;
-            h.tri = hh.tri;
-        }
-        F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
-    }
-    flush_stats(ext, F.counters);
-    flush_stats(shd, F.counters + 8);
 }
 
 // Rays the wave traced: extension rays (paths entering levels >= 1) and
@@ -584,7 +450,6 @@ struct ExtendQueue {
 };
 
 __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_extend(FrameParams F, int level) {
-    if (tail_taken(F, level)) return;
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
     int* lc = F.level_counts + LEVEL_WORDS * level;
@@ -620,7 +485,6 @@ struct ShadowQueue {
 };
 
 __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameParams F, int level) {
-    if (tail_taken(F, level)) return;
     int stack[STACK_WORDS];
     TraceStats st = {0, 0, 0, 0};
     int* lc = F.level_counts + LEVEL_WORDS * level;
@@ -639,7 +503,6 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameP
 __global__ void __launch_bounds__(PATH_BLOCK) k_sky_queue(FrameParams F, int level) {
     int i0 = 0, n = F.counts[2];
     if (level >= 0) {
-        if (tail_taken(F, level)) return;   // the tail queues no sky
         const int* mark = F.level_counts + 5;
         i0 = mark[LEVEL_WORDS * (level > 0 ? level - 1 : F.max_depth + 1)];
         n = mark[LEVEL_WORDS * level];
