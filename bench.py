@@ -899,7 +899,9 @@ def run_profile_case(spec):
     w, h, spp = (int(v) for v in spec.lower().split("x"))
     r = Renderer(0)
     r.initialize()
-    r.load_scene(S.scene_full(w, h, spp, DEPTH))
+    sc = S.scene_full(w, h, spp, DEPTH)
+    sc.sky_arith = 1   # as the full-frame workload
+    r.load_scene(sc)
     for _ in range(2):
         r.execute_rendering(16.0, spp)
     r.synchronize()
