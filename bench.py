@@ -564,8 +564,12 @@ def adjoint_rate(steps, warmup, check_sky=True):
     of the parameters that rendered the target (target samples: seed 7, i.e.
     sample indices 7*32 .. 7*32+31).  With check_sky, the adjoint's
     derivatives for the six sky parameters -- which no sampling decision
-    depends on -- are compared with central differences (h = 1e-3 relative)
-    of the forward renderer's loss at the same point (max_rel_err_sky)."""
+    depends on -- are compared with central differences (h = 1e-2 relative)
+    of the forward renderer's loss at the same point (max_rel_err_sky).  The
+    single-precision renderer's differences for the weakest parameter
+    (Rayleigh red) move by ~0.5% between h = 1e-3 and 1e-2 (measured: 8.9e-3
+    and 2.4e-3 from the adjoint), so this check reads a few 1e-3; the
+    adjoint's accuracy is checked against the FP64 oracle."""
     import torch
     from kittlespt_gb300 import build as B
     B.build()
@@ -645,7 +649,7 @@ def adjoint_rate(steps, warmup, check_sky=True):
             return float(((im - target[..., :3].double()) ** 2).sum())
         errs = []
         for i in range(theta0.size - 6, theta0.size):
-            h = 1e-3 * abs(theta0[i])
+            h = 1e-2 * abs(theta0[i])
             tp, tm = theta0.copy(), theta0.copy()
             tp[i] += h
             tm[i] -= h
@@ -654,10 +658,11 @@ def adjoint_rate(steps, warmup, check_sky=True):
         apply(theta0)
         out["max_rel_err_sky"] = float(max(errs))
         out["rel_err_sky"] = [float(x) for x in errs]
-        out["accuracy_check"] = ("sky parameters against central differences (h = 1e-3) of the forward "
-                                 "renderer's loss at this workload; the single-precision sky resolves these "
-                                 "differences to ~3e-3 at the sun.  All parameters are checked against central "
-                                 "differences of the FP64 oracle to 1e-3 in tests/test_adjoint.py")
+        out["accuracy_check"] = ("sky parameters against central differences (h = 1e-2) of the "
+                                 "single-precision forward renderer's loss at this workload, whose "
+                                 "Rayleigh-red difference itself moves by ~0.5% with h; all 18 parameters "
+                                 "are checked against central differences (h = 1e-3) of the FP64 oracle to "
+                                 "1e-3 in tests/test_adjoint.py")
     r.shutdown()
     return out
 
