@@ -378,6 +378,11 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores, kind, desc = cpu_sample_rate(scene)
         cpu = {"value": rate, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": desc}
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = batch_rate(3, 1)
+        print(f"[bench] 32 mixed jobs: batched {batch['batched']['Msamples_per_s']:.0f} Msamples/s, one by one "
+              f"{batch['one_by_one']['Msamples_per_s']:.0f} ({batch['speedup']:.2f}x)", file=sys.stderr)
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_rate(max(3, args.steps // 2), 2)
@@ -424,6 +429,7 @@ def run_gpu(args):
                                             for k, pre in (("extension", "path"), ("shadow", "shadow"))},
                "cpu_baseline": cpu,
                "adjoint": adjoint,
+               "batch": batch,
                "megakernel": mega,
                "megakernel_msamples_s": mega.get("value") if mega else None,
                "vs_megakernel": value / world / mega["value"] if mega and "value" in mega else None,
@@ -465,11 +471,11 @@ def batch_jobs(seed=4):
     return jobs
 
 
-def run_batch(args):
+def batch_rate(steps, warmup):
     """Batched requests against the same jobs launched one by one: total
     Msamples/s and p50/p99 job latency (all jobs arrive at once; a job's
     latency is the wall time from the start of the round to the end of its
-    frame, host submission included)."""
+    frame, host submission included).  Returns a dict."""
     import torch
     from kittlespt_gb300 import build as B
     B.build()
@@ -500,15 +506,15 @@ def run_batch(args):
             job_ms, _ = b.wait()
             return (time.perf_counter() - t0) * 1e3, job_ms + t_sub
 
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             one_by_one()
             batched(0)
         t_tune = time.perf_counter()
         tuning, lanes, tuned_ms = b.autotune(rs, spp, reps=2)
         t_tune = time.perf_counter() - t_tune
         batched(lanes)   # instantiate the tuned graph outside the timed rounds
-        seq = [one_by_one() for _ in range(args.steps)]
-        bat = [batched(lanes) for _ in range(args.steps)]
+        seq = [one_by_one() for _ in range(steps)]
+        bat = [batched(lanes) for _ in range(steps)]
     for r in rs:
         r.shutdown()
     torch.cuda.synchronize()
@@ -516,10 +522,7 @@ def run_batch(args):
     bat_ms = float(np.mean([t for t, _ in bat]))
     seq_lat = np.concatenate([l for _, l in seq])
     bat_lat = np.concatenate([l for _, l in bat])
-    out = {"metric": "total Msamples/s, 32 mixed jobs (batched requests)", "value": samples / bat_ms / 1e3,
-           "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": bat_ms, "higher_is_better": True, "dtype": "f32",
-           "data": "synthetic (seeded mixed jobs of the small and full-frame scene families)",
+    return {"value": samples / bat_ms / 1e3, "unit": "Msamples/s", "ms_per_step": bat_ms,
            "config": {"workload": "batch_32_mixed_jobs", "jobs": BATCH_JOBS, "samples_per_round": samples,
                       "resolutions": [f"{sc.width}x{sc.height}" for sc in jobs], "spp": spp,
                       "depths": [int(sc.settings["max_depth"]) for sc in jobs],
@@ -532,6 +535,16 @@ def run_batch(args):
                           "p99_latency_ms": float(np.percentile(seq_lat, 99))},
            "speedup": seq_ms / bat_ms,
            "autotune": {"tuning": tuning, "lanes": lanes, "device_ms": tuned_ms, "tuning_seconds": t_tune}}
+
+
+def run_batch(args):
+    """The batched-requests workload as its own bench line (--workload batch)."""
+    b = batch_rate(args.steps, args.warmup)
+    out = {"metric": "total Msamples/s, 32 mixed jobs (batched requests)", "value": b["value"],
+           "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": b["ms_per_step"], "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded mixed jobs of the small and full-frame scene families)"}
+    out.update({k: v for k, v in b.items() if k not in ("value", "unit", "ms_per_step")})
     print(json.dumps(out))
 
 
@@ -971,6 +984,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 32 mixed jobs, batched against one by one")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the differentiation workload's gradient evaluations/s")
     ap.add_argument("--no-megakernel", action="store_true",
