@@ -933,9 +933,10 @@ def run_temporal(args):
     print(json.dumps(out))
 
 
-def run_profile_case(spec):
+def run_profile_case(spec, tuning=()):
     """Two frames of the full-frame scene at a reduced size ("WxHxSPP"): the
-    small case that ncu captures of single kernels run on."""
+    small case that ncu captures of single kernels run on.  tuning: kpt_tuning
+    fields as "name=value" strings."""
     from kittlespt_gb300 import scenes as S
     from kittlespt_gb300.renderer import Renderer
     w, h, spp = (int(v) for v in spec.lower().split("x"))
@@ -944,6 +945,8 @@ def run_profile_case(spec):
     sc = S.scene_full(w, h, spp, DEPTH)
     sc.sky_arith = 1   # as the full-frame workload
     r.load_scene(sc)
+    if tuning:
+        r.set_tuning(**{k: (float(v) if k == "grid_scale" else int(v)) for k, v in (t.split("=") for t in tuning)})
     for _ in range(2):
         r.execute_rendering(16.0, spp)
     r.synchronize()
@@ -999,12 +1002,14 @@ def main():
                          "temporal: 1080p temporal accumulation with a moving camera")
     ap.add_argument("--profile-case", default=None, metavar="WxHxSPP",
                     help="render two frames of the full scene at this size and exit (small case for ncu)")
+    ap.add_argument("--tuning", action="append", default=[], metavar="NAME=VALUE",
+                    help="with --profile-case: a kpt_tuning field for its renderer (repeatable)")
     ap.add_argument("--adjoint-case", default=None, metavar="WxHxSPP",
                     help="run two adjoint evaluations of the differentiation scene at this size and exit "
                          "(small case for ncu)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case)
+        run_profile_case(args.profile_case, args.tuning)
         return
     if args.adjoint_case:
         run_adjoint_case(args.adjoint_case)

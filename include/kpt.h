@@ -330,13 +330,18 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * pixel order (results are the same either way); fetch_batch: in the ray
  * kernels, the lanes of a warp whose rays are done wait until this many are
  * (or the whole warp is) and then store their results and fetch their next
- * rays together (1 .. 32, 0 = 7; results are the same for every value). */
+ * rays together (1 .. 32, 0 = 7; results are the same for every value);
+ * group_lobes: the shading kernel regroups each block-sized window of a
+ * level's paths by the lobe family of their hit (opaque, conductor,
+ * transparent, mixed, none) before shading them, levels >= 1 (1 on, -1 off,
+ * 0 = on; results are the same either way). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;
     int32_t shade_block;
     int32_t sort_rays;
     int32_t fetch_batch;
+    int32_t group_lobes;
 } kpt_tuning;
 void kpt_tuning_default(kpt_tuning* t);
 kpt_status kpt_set_tuning(kpt_context* ctx, const kpt_tuning* t);

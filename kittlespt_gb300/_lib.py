@@ -68,7 +68,7 @@ class Stats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("grid_scale", C.c_float), ("wave_cap", C.c_int32), ("shade_block", C.c_int32),
-                ("sort_rays", C.c_int32), ("fetch_batch", C.c_int32)]
+                ("sort_rays", C.c_int32), ("fetch_batch", C.c_int32), ("group_lobes", C.c_int32)]
 
 
 assert C.sizeof(Material) == 72 and C.sizeof(Environment) == 48

@@ -938,6 +938,7 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     F.shadow = c->shadow.p;
     F.level_counts = c->level_counts.p;
     F.unsorted = c->tuning.sort_rays ? c->unsorted.p : nullptr;
+    F.group_lobes = c->tuning.group_lobes > 0 ? 1 : 0;
     F.octants = c->octants.p;
     F.cap = c->wave_cap;
     F.primary = c->primary.p;
@@ -1614,6 +1615,7 @@ void kpt_tuning_default(kpt_tuning* t) {
     t->shade_block = SHADE_BLOCK;
     t->sort_rays = 0;
     t->fetch_batch = FETCH_BATCH;
+    t->group_lobes = 1;
 }
 
 kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
@@ -1627,9 +1629,12 @@ kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
     if (t->sort_rays != 0 && t->sort_rays != 1) return fail(KPT_ERR_INVALID, "kpt_set_tuning: sort_rays must be 0 or 1");
     if (t->fetch_batch < 0 || t->fetch_batch > 32)
         return fail(KPT_ERR_INVALID, "kpt_set_tuning: fetch_batch must be in [0, 32]");
+    if (t->group_lobes < -1 || t->group_lobes > 1)
+        return fail(KPT_ERR_INVALID, "kpt_set_tuning: group_lobes must be -1, 0 or 1");
     c->tuning = *t;
     if (c->tuning.shade_block == 0) c->tuning.shade_block = SHADE_BLOCK;
     if (c->tuning.fetch_batch == 0) c->tuning.fetch_batch = FETCH_BATCH;
+    if (c->tuning.group_lobes == 0) c->tuning.group_lobes = 1;
     c->view.fetch_batch = c->tuning.fetch_batch;
     return KPT_OK;
 }

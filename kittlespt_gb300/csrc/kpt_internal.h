@@ -88,6 +88,7 @@ struct FrameParams {
     PathRec* unsorted;         // [cap] k_shade's continuations before the octant sort, null: no sort
     int* octants;              // [16 * (max_depth + 2)] per level: paths per direction octant, cursors
     int cap;
+    int group_lobes;           // k_shade groups a level's paths by lobe family within each block (levels >= 1)
 };
 
 // ---------------------------------------------------------------------------

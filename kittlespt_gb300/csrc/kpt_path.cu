@@ -116,11 +116,17 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_primary_sky(FrameParams F) {
 
 // Shadow ray of Integrator::unoccluded (integrator.cuh:124-131): from the
 // offset surface point towards `target`, stopping 0.11 short of it.
+__device__ __forceinline__ void shadow_ray(const Surf& si, float3 target, float3& o, float3& d, float& tmax) {
+    o = si.backface ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+    d = normalize(target - o);
+    tmax = length(target - o) - 0.11f;
+}
+
 __device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si, float3 target, float3 contrib,
                                             int item, int* counter, bool from_back) {
-    float3 o = si.backface ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
-    float3 d = normalize(target - o);
-    float tmax = length(target - o) - 0.11f;
+    float3 o, d;
+    float tmax;
+    shadow_ray(si, target, o, d, tmax);
     int j = group_append(counter);
     if (from_back) j = F.cap - 1 - j;
     ShadowRec r;
@@ -140,11 +146,247 @@ __device__ __forceinline__ void emit_shadow(const FrameParams& F, const Surf& si
 // emission here, its light sample in k_shadow, the next vertex's terms at the
 // next level, the sky last.  Level 0 starts the paths of items
 // wave0 .. wave0+cap-1 from the camera-ray hits of k_primary.
-__device__ __forceinline__ void shade_level(const FrameParams& F, int level, long long wave0) {
+// One vertex of Integrator::Li for one path (the loop body of shade_level,
+// below): `h` is the path's hit at this level; o, d the ray that found it;
+// beta, p_b, prev and seed the path's throughput, BSDF pdf, previous vertex
+// and random-number state; L its radiance so far.  The vertex's outcomes go
+// to `sink`: the sky direction of a path that left the scene (its last
+// term), the radiance after this vertex's emission, the shadow ray of its
+// light sample with the radiance it adds if unoccluded (sun: true for a sun
+// sample), and the continuation (a PathRec, the next level's input).
+template <class Sink>
+__device__ __forceinline__ void shade_vertex(const FrameParams& F, int level, const PrimaryRec& h, float3 o, float3 d,
+                                             float3 beta, float3 prev, float3 L, float p_b, uint32_t seed, int item,
+                                             Sink& sink) {
     const SceneView& s = F.scene;
     const SkyParams& P = F.sky;
     const int order = F.rng_order;
     const int nl = s.nlights;
+    const bool first = level == 0;
+    if (h.inst < 0) {
+        sink.sky(item, d, beta, L);   // the path ends here: the sky is its last term
+        return;
+    }
+    Sampler S;
+    S.seed = seed + (uint32_t)level;
+    Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
+    float3 Le = make_float3(0.0f, 0.0f, 0.0f);
+    if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
+    if (nonzero(Le)) {
+        float w_l = 1.0f;
+        if (si.light >= 0 && !first) {
+            const LightRec& lt = s.lights[si.light];
+            float pmf = 1.0f / (float)nl;
+            float dist = length(si.pos - prev);
+            float cosl = AbsDot(normalize(si.pos - prev), si.ng);
+            float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
+            w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
+        }
+        L = L + Le * w_l * beta;
+    }
+    Bsdf bsdf = bsdf_at(s, si);
+    if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);   // demodulate (bsdf.cuh:286-288)
+    if (!first && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
+    const float3 wo = -d;
+    if (!(bsdf.alpha < 0.001f)) {
+        // The light sample: each branch draws its numbers and sets up its
+        // direction; the BSDF is then evaluated once for all lanes (the
+        // sun / area-light choice is random per lane, so both branches
+        // run in every warp), and each branch finishes its own sample.
+        const bool sun = S.get1D() < 0.5f;
+        const float dsun = 149.597e9f;
+        // the sun's centre at 1 AU, each product rounded on its own:
+        // target - sun_pos below cancels two values near 1.5e11, which a
+        // fused multiply-add would shift by up to half their ulp (~1e-5
+        // of the difference) -- as the reference's GPU build does, with
+        // gpu_arith
+        const float3 sun_pos = P.gpu_arith ? P.sun_dir * dsun
+                                           : make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
+                                                         __fmul_rn(P.sun_dir.z, dsun));
+        float3 wi = P.sun_dir, target, Lem;
+        float pdf = 0.0f, prob = 0.0f;
+        bool eval;
+        if (sun) {
+            // sampleLdSun: jittered point on the sun disc at 1 AU
+            float3 off;
+            if ((order & RNG_SUN) == 0) {
+                float2 a = S.get2D(order);
+                float b = S.get1D();
+                off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+            } else {
+                float b = S.get1D();
+                float2 a = S.get2D(order);
+                off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
+            }
+            target = P.gpu_arith ? sun_pos + (off * P.sun_radius_m)
+                                 : make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
+                                               __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
+                                               __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
+            eval = true;
+        } else {
+            // sampleLd: uniform light pick, uniform point on the triangle
+            float X = S.get1D();
+            eval = false;
+            if (nl >= 1) {
+                int li = min((int)(X * (float)nl), nl - 1);
+                const LightRec& lt = s.lights[li];
+                prob = 1.0f / (float)nl;
+                float2 uu = S.get2D(order);
+                const InstRec& lir = s.inst[lt.inst];
+                float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
+                float bx, by;
+                if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
+                else { by = uu.y / 2.0f; bx = uu.x - by; }
+                float bz = 1.0f - bx - by;
+                float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
+                                         bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
+                float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
+                p = row3(model, p, 1.0f);
+                float3 gn = row3(model, lt.gn, 0.0f);
+                pdf = 1.0f / lt.tri_area;
+                pdf *= Sqr(length(p - si.pos));
+                pdf /= AbsDot(normalize(p - si.pos), gn);
+                wi = normalize(p - si.pos);
+                Lem = emission_of(s, lt.material, luv);
+                target = p;
+                eval = !(pdf <= 0.0f || !nonzero(Lem));
+            }
+        }
+        float3 fcos = make_float3(0.0f, 0.0f, 0.0f);
+        if (eval) fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
+        if (sun) {
+            const float3 sun_rad = *F.sun_radiance;
+            if (nonzero(fcos) && nonzero(sun_rad)) {
+                float area = PI_F * Sqr(P.sun_radius_m);
+                float3 sn = normalize(target - sun_pos), wt = normalize(target - si.pos);
+                float th = AbsDot(sn, -wt);
+                float spdf = (1.0f / area) / (th / Sqr(dsun));
+                float3 Ld = (fcos * sun_rad * 6.0e5f) / spdf;
+                float3 c = Ld * beta / 0.5f;
+                if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                    sink.shadow(si, target, c, item, true);
+            }
+        } else if (eval && nonzero(fcos)) {
+            float p_l = prob * pdf;
+            float pb = bsdf.pdf(wo, wi);
+            float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
+            float3 Ld = (Lem * fcos * w_l) / p_l;
+            float3 c = Ld * beta / (1.0f - 0.5f);
+            if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
+                sink.shadow(si, target, c, item, false);
+        }
+    }
+    sink.radiance(item, L);
+    if (level == F.max_depth) return;
+    float2 uu, X;
+    if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
+    else { X = S.get2D(order); uu = S.get2D(order); }
+    BsdfSample bs = bsdf.sample(wo, uu, X);
+    if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) return;
+    beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
+    p_b = bsdf.pdf(wo, bs.wi);
+    o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
+    float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
+    if (mx < 1.0f && level >= 1) {
+        float q = fmaxf(0.0f, 1.0f - mx);
+        if (S.get1D() < q) return;
+        beta = beta / (1.0f - q);
+    }
+    if (!nonzero(beta)) return;   // while (throughput) (integrator.cuh:266)
+    PathRec pr;
+    pr.o_pb = make_float4(o.x, o.y, o.z, p_b);
+    pr.d_seed = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, __uint_as_float(S.seed));
+    pr.beta_item = make_float4(beta.x, beta.y, beta.z, __int_as_float(item));
+    pr.prev = make_float4(si.pos.x, si.pos.y, si.pos.z, 0.0f);
+    sink.next(pr);
+}
+
+// The wave's sink: sky lookups, shadow rays and continuations appended to the
+// level's compacted queues, the radiance written back to the item.
+struct WaveSink {
+    const FrameParams& F;
+    int* here;        // level_counts of this level
+    int* ahead;       // level_counts of the next level
+    PathRec* out;     // the next level's paths
+    __device__ __forceinline__ void sky(int item, float3 d, float3 beta, float3) {
+        const int q = group_append(F.counts + 2);
+        F.sky_queue[2 * (size_t)q] = make_float4(__int_as_float(item), d.x, d.y, d.z);
+        F.sky_queue[2 * (size_t)q + 1] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+    }
+    __device__ __forceinline__ void radiance(int item, float3 L) {
+        F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
+    }
+    __device__ __forceinline__ void shadow(const Surf& si, float3 target, float3 c, int item, bool sun) {
+        if (sun) emit_shadow(F, si, target, c, item, here + 1, false);
+        else emit_shadow(F, si, target, c, item, here + 2, true);
+    }
+    __device__ __forceinline__ void next(const PathRec& pr) {
+        const int j = group_append(ahead);
+        out[j] = pr;
+    }
+};
+
+// The lobe family of a path's hit, for grouping the shading of a level:
+// 0 opaque dielectric, 1 conductor, 2 transparent dielectric, 3 mixed
+// (fractional metallic or transmission, or a texture that makes them so),
+// 4 no hit (the path leaves the scene).
+__device__ __forceinline__ int lobe_family(const SceneView& s, const PrimaryRec& h) {
+    if (h.inst < 0) return 4;
+    const InstRec& ir = s.inst[h.inst];
+    const int m = ir.material >= 0 ? ir.material : s.shade[s.meshes[ir.mesh].shade_base + h.tri].material;
+    const MatRec& mr = s.materials[m];
+    if (mr.orm_tex >= 0 || mr.transmission_tex >= 0) return 3;
+    if (mr.metallic == 0.0f) return mr.transmission == 0.0f ? 0 : (mr.transmission == 1.0f ? 2 : 3);
+    return mr.metallic == 1.0f ? 1 : 3;
+}
+
+__device__ __forceinline__ void shade_path(const FrameParams& F, int level, long long wave0, int i, int* here,
+                                           int* next, PathRec* out) {
+    const bool first = level == 0;
+    float3 o, d, beta, prev, L;
+    float p_b;
+    uint32_t seed;
+    int item;
+    PrimaryRec h;
+    if (first) {
+        // items are pixel-major: the samples of one camera hit are
+        // neighbours (one surface point, one material)
+        item = (int)(wave0 + i);
+        const int hj = item / F.nsamples;
+        const int k = item - hj * F.nsamples;
+        const int p = F.hit_list[hj];
+        const int x = p % F.W, y = p / F.W;
+        Sampler S0;
+        S0.init(x, y, F.W, F.sample0 + k);
+        S0.get1D();   // BoxFilter::sample, result discarded (kernels.cu:397-402)
+        S0.get1D();
+        XRay r = camera_ray(F, x, y);
+        o = r.o;
+        d = r.d;
+        beta = make_float3(1.0f, 1.0f, 1.0f);
+        prev = make_float3(0.0f, 0.0f, 0.0f);
+        L = make_float3(0.0f, 0.0f, 0.0f);
+        p_b = 1.0f;
+        seed = S0.seed;
+        h = F.primary[p];
+    } else {
+        const PathRec pr = F.paths[level & 1][i];
+        o = make_float3(pr.o_pb.x, pr.o_pb.y, pr.o_pb.z);
+        p_b = pr.o_pb.w;
+        d = make_float3(pr.d_seed.x, pr.d_seed.y, pr.d_seed.z);
+        seed = __float_as_uint(pr.d_seed.w);
+        beta = make_float3(pr.beta_item.x, pr.beta_item.y, pr.beta_item.z);
+        item = __float_as_int(pr.beta_item.w);
+        prev = make_float3(pr.prev.x, pr.prev.y, pr.prev.z);
+        h = F.hits[i];
+        const float4 l4 = F.radiance[item];
+        L = make_float3(l4.x, l4.y, l4.z);
+    }
+    WaveSink sink{F, here, next, out};
+    shade_vertex(F, level, h, o, d, beta, prev, L, p_b, seed, item, sink);
+}
+
+__device__ __forceinline__ void shade_level(const FrameParams& F, int level, long long wave0) {
     const bool first = level == 0;
     int n;
     if (first) {
@@ -153,193 +395,37 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
     } else {
         n = F.level_counts[LEVEL_WORDS * level];
     }
-    const PathRec* in = F.paths[level & 1];
     PathRec* out = F.unsorted ? F.unsorted : F.paths[(level + 1) & 1];
     int* here = F.level_counts + LEVEL_WORDS * level;
     int* next = F.level_counts + LEVEL_WORDS * (level + 1);
     // the wave's paths entering level 0 (levels >= 1 count theirs as they
     // are appended); read back by kpt_get_level_counts
     if (first && blockIdx.x == 0 && threadIdx.x == 0) here[0] = n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float3 o, d, beta, prev, L;
-        float p_b;
-        uint32_t seed;
-        int item;
-        PrimaryRec h;
-        if (first) {
-            // items are pixel-major: the samples of one camera hit are
-            // neighbours (one surface point, one material)
-            item = (int)(wave0 + i);
-            const int hj = item / F.nsamples;
-            const int k = item - hj * F.nsamples;
-            const int p = F.hit_list[hj];
-            const int x = p % F.W, y = p / F.W;
-            Sampler S0;
-            S0.init(x, y, F.W, F.sample0 + k);
-            S0.get1D();   // BoxFilter::sample, result discarded (kernels.cu:397-402)
-            S0.get1D();
-            XRay r = camera_ray(F, x, y);
-            o = r.o;
-            d = r.d;
-            beta = make_float3(1.0f, 1.0f, 1.0f);
-            prev = make_float3(0.0f, 0.0f, 0.0f);
-            L = make_float3(0.0f, 0.0f, 0.0f);
-            p_b = 1.0f;
-            seed = S0.seed;
-            h = F.primary[p];
-        } else {
-            const PathRec pr = in[i];
-            o = make_float3(pr.o_pb.x, pr.o_pb.y, pr.o_pb.z);
-            p_b = pr.o_pb.w;
-            d = make_float3(pr.d_seed.x, pr.d_seed.y, pr.d_seed.z);
-            seed = __float_as_uint(pr.d_seed.w);
-            beta = make_float3(pr.beta_item.x, pr.beta_item.y, pr.beta_item.z);
-            item = __float_as_int(pr.beta_item.w);
-            prev = make_float3(pr.prev.x, pr.prev.y, pr.prev.z);
-            h = F.hits[i];
-            const float4 l4 = F.radiance[item];
-            L = make_float3(l4.x, l4.y, l4.z);
+    // Levels >= 1 (with F.group_lobes): the paths of each block-sized window
+    // are regrouped by the lobe family of their hit (a counting sort in
+    // shared memory), so that a warp mostly runs one family's code (a level's
+    // paths hit every kind of material in pixel order).  Every path is still
+    // shaded exactly once and its result does not depend on its slot.
+    const bool group = !first && F.group_lobes;
+    __shared__ int fam_count[8];
+    __shared__ int order[SHADE_MAX_BLOCK];
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        int i = base + threadIdx.x;
+        if (group) {
+            const int fam = i < n ? lobe_family(F.scene, F.hits[i]) : 5;
+            if (threadIdx.x < 8) fam_count[threadIdx.x] = 0;
+            __syncthreads();
+            const int rank = atomicAdd(&fam_count[fam], 1);
+            __syncthreads();
+            int off = 0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) off += k < fam ? fam_count[k] : 0;
+            order[off + rank] = i;
+            __syncthreads();
+            i = order[threadIdx.x];
         }
-        if (h.inst < 0) {
-            // the sky is evaluated by k_sky_queue; the path ends here
-            const int q = group_append(F.counts + 2);
-            F.sky_queue[2 * (size_t)q] = make_float4(__int_as_float(item), d.x, d.y, d.z);
-            F.sky_queue[2 * (size_t)q + 1] = make_float4(beta.x, beta.y, beta.z, 0.0f);
-            continue;
-        }
-        Sampler S;
-        S.seed = seed + (uint32_t)level;
-        Surf si = surface_at(s, h.inst, h.tri, h.t, h.u, h.v, o, d);
-        float3 Le = make_float3(0.0f, 0.0f, 0.0f);
-        if (si.light >= 0) Le = emission_of(s, si.material, si.uv);
-        if (nonzero(Le)) {
-            float w_l = 1.0f;
-            if (si.light >= 0 && !first) {
-                const LightRec& lt = s.lights[si.light];
-                float pmf = 1.0f / (float)nl;
-                float dist = length(si.pos - prev);
-                float cosl = AbsDot(normalize(si.pos - prev), si.ng);
-                float lpdf = pmf * ((1.0f / lt.area) / (cosl / Sqr(dist)));
-                w_l = Sqr(p_b) / (Sqr(p_b) + Sqr(lpdf));
-            }
-            L = L + Le * w_l * beta;
-        }
-        Bsdf bsdf = bsdf_at(s, si);
-        if (first) bsdf.albedo = make_float3(1.0f, 1.0f, 1.0f);   // demodulate (bsdf.cuh:286-288)
-        if (!first && bsdf.alpha < 0.3f) bsdf.alpha = clampf(2.0f * bsdf.alpha, 0.1f, 0.3f);
-        const float3 wo = -d;
-        if (!(bsdf.alpha < 0.001f)) {
-            // The light sample: each branch draws its numbers and sets up its
-            // direction; the BSDF is then evaluated once for all lanes (the
-            // sun / area-light choice is random per lane, so both branches
-            // run in every warp), and each branch finishes its own sample.
-            const bool sun = S.get1D() < 0.5f;
-            const float dsun = 149.597e9f;
-            // the sun's centre at 1 AU, each product rounded on its own:
-            // target - sun_pos below cancels two values near 1.5e11, which a
-            // fused multiply-add would shift by up to half their ulp (~1e-5
-            // of the difference) -- as the reference's GPU build does, with
-            // gpu_arith
-            const float3 sun_pos = P.gpu_arith ? P.sun_dir * dsun
-                                               : make_float3(__fmul_rn(P.sun_dir.x, dsun), __fmul_rn(P.sun_dir.y, dsun),
-                                                             __fmul_rn(P.sun_dir.z, dsun));
-            float3 wi = P.sun_dir, target, Lem;
-            float pdf = 0.0f, prob = 0.0f;
-            bool eval;
-            if (sun) {
-                // sampleLdSun: jittered point on the sun disc at 1 AU
-                float3 off;
-                if ((order & RNG_SUN) == 0) {
-                    float2 a = S.get2D(order);
-                    float b = S.get1D();
-                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
-                } else {
-                    float b = S.get1D();
-                    float2 a = S.get2D(order);
-                    off = make_float3(a.x * 2.0f - 1.0f, a.y * 2.0f - 1.0f, b * 2.0f - 1.0f);
-                }
-                target = P.gpu_arith ? sun_pos + (off * P.sun_radius_m)
-                                     : make_float3(__fadd_rn(sun_pos.x, __fmul_rn(off.x, P.sun_radius_m)),
-                                                   __fadd_rn(sun_pos.y, __fmul_rn(off.y, P.sun_radius_m)),
-                                                   __fadd_rn(sun_pos.z, __fmul_rn(off.z, P.sun_radius_m)));
-                eval = true;
-            } else {
-                // sampleLd: uniform light pick, uniform point on the triangle
-                float X = S.get1D();
-                eval = false;
-                if (nl >= 1) {
-                    int li = min((int)(X * (float)nl), nl - 1);
-                    const LightRec& lt = s.lights[li];
-                    prob = 1.0f / (float)nl;
-                    float2 uu = S.get2D(order);
-                    const InstRec& lir = s.inst[lt.inst];
-                    float4 model[3] = {lir.model[0], lir.model[1], lir.model[2]};
-                    float bx, by;
-                    if (uu.x < uu.y) { bx = uu.x / 2.0f; by = uu.y - bx; }
-                    else { by = uu.y / 2.0f; bx = uu.x - by; }
-                    float bz = 1.0f - bx - by;
-                    float2 luv = make_float2(bx * lt.uv0.x + by * lt.uv1.x + bz * lt.uv2.x,
-                                             bx * lt.uv0.y + by * lt.uv1.y + bz * lt.uv2.y);
-                    float3 p = (lt.p0 * bx) + (lt.p1 * by) + (lt.p2 * bz);
-                    p = row3(model, p, 1.0f);
-                    float3 gn = row3(model, lt.gn, 0.0f);
-                    pdf = 1.0f / lt.tri_area;
-                    pdf *= Sqr(length(p - si.pos));
-                    pdf /= AbsDot(normalize(p - si.pos), gn);
-                    wi = normalize(p - si.pos);
-                    Lem = emission_of(s, lt.material, luv);
-                    target = p;
-                    eval = !(pdf <= 0.0f || !nonzero(Lem));
-                }
-            }
-            float3 fcos = make_float3(0.0f, 0.0f, 0.0f);
-            if (eval) fcos = bsdf.f(wo, wi) * fmaxf(0.0f, dot(wi, (si.backface ? -1.0f : 1.0f) * si.ng));
-            if (sun) {
-                const float3 sun_rad = *F.sun_radiance;
-                if (nonzero(fcos) && nonzero(sun_rad)) {
-                    float area = PI_F * Sqr(P.sun_radius_m);
-                    float3 sn = normalize(target - sun_pos), wt = normalize(target - si.pos);
-                    float th = AbsDot(sn, -wt);
-                    float spdf = (1.0f / area) / (th / Sqr(dsun));
-                    float3 Ld = (fcos * sun_rad * 6.0e5f) / spdf;
-                    float3 c = Ld * beta / 0.5f;
-                    if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
-                        emit_shadow(F, si, target, c, item, here + 1, false);
-                }
-            } else if (eval && nonzero(fcos)) {
-                float p_l = prob * pdf;
-                float pb = bsdf.pdf(wo, wi);
-                float w_l = Sqr(p_l) / (Sqr(p_l) + Sqr(pb));
-                float3 Ld = (Lem * fcos * w_l) / p_l;
-                float3 c = Ld * beta / (1.0f - 0.5f);
-                if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f))
-                    emit_shadow(F, si, target, c, item, here + 2, true);
-            }
-        }
-        F.radiance[item] = make_float4(L.x, L.y, L.z, 0.0f);
-        if (level == F.max_depth) continue;
-        float2 uu, X;
-        if ((order & RNG_BSDF) == 0) { uu = S.get2D(order); X = S.get2D(order); }
-        else { X = S.get2D(order); uu = S.get2D(order); }
-        BsdfSample bs = bsdf.sample(wo, uu, X);
-        if (bs.scatter == SC_ABSORBED || !nonzero(bs.f)) continue;
-        beta = beta * (bs.f * AbsDot(si.ng, bs.wi) / bs.pdf);
-        p_b = bsdf.pdf(wo, bs.wi);
-        o = (bs.scatter & SC_TRANSMITTED) ? (si.pos - (si.ng * HIT_EPS)) : (si.pos + (si.ng * HIT_EPS));
-        float mx = fmaxf(beta.x, fmaxf(beta.y, beta.z));
-        if (mx < 1.0f && level >= 1) {
-            float q = fmaxf(0.0f, 1.0f - mx);
-            if (S.get1D() < q) continue;
-            beta = beta / (1.0f - q);
-        }
-        if (!nonzero(beta)) continue;   // while (throughput) (integrator.cuh:266)
-        const int j = group_append(next);
-        PathRec pr;
-        pr.o_pb = make_float4(o.x, o.y, o.z, p_b);
-        pr.d_seed = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, __uint_as_float(S.seed));
-        pr.beta_item = make_float4(beta.x, beta.y, beta.z, __int_as_float(item));
-        pr.prev = make_float4(si.pos.x, si.pos.y, si.pos.z, 0.0f);
-        out[j] = pr;
+        if (i < n) shade_path(F, level, wave0, i, here, next, out);
+        if (group) __syncthreads();
     }
 }
 

@@ -357,16 +357,16 @@ class Renderer:
 
     # -- launch parameters (no reference counterpart) -------------------------
     def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0, sort_rays: int = 0,
-                   fetch_batch: int = 0):
+                   fetch_batch: int = 0, group_lobes: int = 0):
         t = K.Tuning(grid_scale=grid_scale, wave_cap=wave_cap, shade_block=shade_block, sort_rays=sort_rays,
-                     fetch_batch=fetch_batch)
+                     fetch_batch=fetch_batch, group_lobes=group_lobes)
         K.check(self._L.kpt_set_tuning(self._ctx, C.byref(t)))
 
     def tuning(self) -> dict:
         t = K.Tuning()
         K.check(self._L.kpt_get_tuning(self._ctx, C.byref(t)))
         return {"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block,
-                "sort_rays": t.sort_rays, "fetch_batch": t.fetch_batch}
+                "sort_rays": t.sort_rays, "fetch_batch": t.fetch_batch, "group_lobes": t.group_lobes}
 
 
 class Batch:
@@ -418,7 +418,7 @@ class Batch:
         K.check(self._L.kpt_autotune_batch(self._b, n, jobs, K.iptr(s), reps, C.byref(t), K.iptr(lanes),
                                            K.fptr(ms)))
         return ({"grid_scale": t.grid_scale, "wave_cap": t.wave_cap, "shade_block": t.shade_block,
-                 "sort_rays": t.sort_rays, "fetch_batch": t.fetch_batch}, int(lanes[0]), float(ms[0]))
+                 "sort_rays": t.sort_rays, "fetch_batch": t.fetch_batch, "group_lobes": t.group_lobes}, int(lanes[0]), float(ms[0]))
 
 
 # -- path-replay adjoint (no reference counterpart) ----------------------------

@@ -19,7 +19,7 @@ def test_tuning_defaults_and_errors():
     L = K.load()
     t = K.Tuning()
     L.kpt_tuning_default(C.byref(t))
-    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays, t.fetch_batch) == (1.0, 0, 256, 0, 7)
+    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays, t.fetch_batch, t.group_lobes) == (1.0, 0, 256, 0, 7, 1)
     assert L.kpt_set_tuning(None, C.byref(t)) == -1
     assert L.kpt_get_tuning(None, C.byref(t)) == -1
     assert L.kpt_submit_batch(None, 1, None, None, 0) == -1
