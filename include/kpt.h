@@ -331,10 +331,11 @@ kpt_status kpt_launch_count(kpt_context* ctx, uint64_t* launches);
  * kernels, the lanes of a warp whose rays are done wait until this many are
  * (or the whole warp is) and then store their results and fetch their next
  * rays together (1 .. 32, 0 = 7; results are the same for every value);
- * group_lobes: the shading kernel regroups each block-sized window of a
+ * group_lobes: the shading kernel regroups windows of this many of a
  * level's paths by the lobe family of their hit (opaque, conductor,
- * transparent, mixed, none) before shading them, levels >= 1 (1 on, -1 off,
- * 0 = on; results are the same either way). */
+ * transparent, mixed, none) before shading them, levels >= 1 (a multiple of
+ * 64 in [64, 2048], rounded down to a multiple of the shading block and at
+ * least one block; -1 off; 0 = 2048; results are the same either way). */
 typedef struct kpt_tuning {
     float grid_scale;
     int32_t wave_cap;

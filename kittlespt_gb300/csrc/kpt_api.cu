@@ -938,7 +938,7 @@ static FrameParams frame_params(kpt_context* c, int sample0, int nsamples) {
     F.shadow = c->shadow.p;
     F.level_counts = c->level_counts.p;
     F.unsorted = c->tuning.sort_rays ? c->unsorted.p : nullptr;
-    F.group_lobes = c->tuning.group_lobes > 0 ? 1 : 0;
+    F.group_lobes = c->tuning.group_lobes > 0 ? c->tuning.group_lobes : 0;
     F.octants = c->octants.p;
     F.cap = c->wave_cap;
     F.primary = c->primary.p;
@@ -1020,6 +1020,8 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     const bool wide = shade_block > PATH_BLOCK;
     const void* shade_fn = wide ? (const void*)k_shade_wide : (const void*)k_shade;
     const int g_shade = persistent_grid(c, shade_fn, shade_block);
+    const int g_bounce = persistent_grid(c, wide ? (const void*)k_shade_bounce_wide : (const void*)k_shade_bounce,
+                                         shade_block);
     const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
     const int g_shd = persistent_grid(c, (const void*)k_shadow, TRACE_BLOCK);
     // every pixel may hit: the last waves find no work when fewer do
@@ -1043,8 +1045,13 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 if (fork) cudaStreamWaitEvent(s, c->ev_join[l - 1], 0);
             }
             stage_mark(c, KPT_STAGE_SHADE);
-            if (wide) k_shade_wide<<<g_shade, shade_block, 0, s>>>(F, l, w0);
-            else k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
+            if (l > 0) {
+                if (wide) k_shade_bounce_wide<<<g_bounce, shade_block, 0, s>>>(F, l, w0);
+                else k_shade_bounce<<<g_bounce, shade_block, 0, s>>>(F, l, w0);
+            } else {
+                if (wide) k_shade_wide<<<g_shade, shade_block, 0, s>>>(F, l, w0);
+                else k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
+            }
             stage_mark(c, KPT_STAGE_SHADOW);
             if (fork) {
                 cudaEventRecord(c->ev_fork[l], s);
@@ -1615,7 +1622,7 @@ void kpt_tuning_default(kpt_tuning* t) {
     t->shade_block = SHADE_BLOCK;
     t->sort_rays = 0;
     t->fetch_batch = FETCH_BATCH;
-    t->group_lobes = 1;
+    t->group_lobes = SHADE_WINDOW;
 }
 
 kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
@@ -1629,12 +1636,13 @@ kpt_status kpt_set_tuning(kpt_context* c, const kpt_tuning* t) {
     if (t->sort_rays != 0 && t->sort_rays != 1) return fail(KPT_ERR_INVALID, "kpt_set_tuning: sort_rays must be 0 or 1");
     if (t->fetch_batch < 0 || t->fetch_batch > 32)
         return fail(KPT_ERR_INVALID, "kpt_set_tuning: fetch_batch must be in [0, 32]");
-    if (t->group_lobes < -1 || t->group_lobes > 1)
-        return fail(KPT_ERR_INVALID, "kpt_set_tuning: group_lobes must be -1, 0 or 1");
+    if (!(t->group_lobes == -1 || t->group_lobes == 0 ||
+          (t->group_lobes >= 64 && t->group_lobes <= SHADE_WINDOW && t->group_lobes % 64 == 0)))
+        return fail(KPT_ERR_INVALID, "kpt_set_tuning: group_lobes must be -1, 0 or a multiple of 64 in [64, 2048]");
     c->tuning = *t;
     if (c->tuning.shade_block == 0) c->tuning.shade_block = SHADE_BLOCK;
     if (c->tuning.fetch_batch == 0) c->tuning.fetch_batch = FETCH_BATCH;
-    if (c->tuning.group_lobes == 0) c->tuning.group_lobes = 1;
+    if (c->tuning.group_lobes == 0) c->tuning.group_lobes = SHADE_WINDOW;
     c->view.fetch_batch = c->tuning.fetch_batch;
     return KPT_OK;
 }

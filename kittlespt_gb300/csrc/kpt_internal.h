@@ -8,6 +8,7 @@ namespace kpt {
 
 constexpr int PATH_BLOCK = 128;    // threads per block of the shading kernels
 constexpr int SHADE_MAX_BLOCK = 256;   // largest block k_shade is launched with (kpt_tuning.shade_block)
+constexpr int SHADE_WINDOW = 2048;     // largest window of paths k_shade regroups by lobe family (kpt_tuning.group_lobes)
 constexpr int TRACE_BLOCK = 128;   // threads per block of the ray kernels
 // k_primary: a warp traces a TILE_W x (32 / TILE_W) tile of pixels, a
 // block of PATH_BLOCK = 128 threads a 2 x 2 arrangement of them
@@ -88,7 +89,7 @@ struct FrameParams {
     PathRec* unsorted;         // [cap] k_shade's continuations before the octant sort, null: no sort
     int* octants;              // [16 * (max_depth + 2)] per level: paths per direction octant, cursors
     int cap;
-    int group_lobes;           // k_shade groups a level's paths by lobe family within each block (levels >= 1)
+    int group_lobes;           // k_shade regroups windows of this many paths by lobe family (levels >= 1); 0 = off
 };
 
 // ---------------------------------------------------------------------------
@@ -173,6 +174,9 @@ __global__ void k_primary(FrameParams F);
 __global__ void k_primary_sky(FrameParams F);
 __global__ void k_shade(FrameParams F, int level, long long wave0);        // blocks of <= PATH_BLOCK threads
 __global__ void k_shade_wide(FrameParams F, int level, long long wave0);   // blocks of <= SHADE_MAX_BLOCK threads
+// levels >= 1 (with F.group_lobes > 0 each window of paths regrouped by lobe family)
+__global__ void k_shade_bounce(FrameParams F, int level, long long wave0);
+__global__ void k_shade_bounce_wide(FrameParams F, int level, long long wave0);
 __global__ void k_extend(FrameParams F, int level);
 __global__ void k_count_rays(FrameParams F);   // adds the wave's ray counts to counters[12..13]
 __global__ void k_sort_count(FrameParams F, int level);     // octant histogram of the paths entering level

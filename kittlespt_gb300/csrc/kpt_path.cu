@@ -340,9 +340,8 @@ __device__ __forceinline__ int lobe_family(const SceneView& s, const PrimaryRec&
     return mr.metallic == 1.0f ? 1 : 3;
 }
 
-__device__ __forceinline__ void shade_path(const FrameParams& F, int level, long long wave0, int i, int* here,
-                                           int* next, PathRec* out) {
-    const bool first = level == 0;
+__device__ __forceinline__ void shade_path(const FrameParams& F, bool first, int level, long long wave0, int i,
+                                           int* here, int* next, PathRec* out) {
     float3 o, d, beta, prev, L;
     float p_b;
     uint32_t seed;
@@ -386,8 +385,12 @@ __device__ __forceinline__ void shade_path(const FrameParams& F, int level, long
     shade_vertex(F, level, h, o, d, beta, prev, L, p_b, seed, item, sink);
 }
 
+// BOUNCE: levels >= 1 only (the host launches level 0 with BOUNCE false and
+// every later level with BOUNCE true, whatever F.group_lobes, so that each
+// level's shading is the same compiled code in every configuration)
+template <bool BOUNCE>
 __device__ __forceinline__ void shade_level(const FrameParams& F, int level, long long wave0) {
-    const bool first = level == 0;
+    const bool first = !BOUNCE && level == 0;
     int n;
     if (first) {
         const long long left = (long long)F.counts[0] * F.nsamples - wave0;
@@ -401,41 +404,90 @@ __device__ __forceinline__ void shade_level(const FrameParams& F, int level, lon
     // the wave's paths entering level 0 (levels >= 1 count theirs as they
     // are appended); read back by kpt_get_level_counts
     if (first && blockIdx.x == 0 && threadIdx.x == 0) here[0] = n;
-    // Levels >= 1 (with F.group_lobes): the paths of each block-sized window
-    // are regrouped by the lobe family of their hit (a counting sort in
-    // shared memory), so that a warp mostly runs one family's code (a level's
-    // paths hit every kind of material in pixel order).  Every path is still
-    // shaded exactly once and its result does not depend on its slot.
-    const bool group = !first && F.group_lobes;
+    if (!BOUNCE) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            shade_path(F, first, level, wave0, i, here, next, out);
+        return;
+    }
+    // Levels >= 1: the blocks stride over the level's paths in windows.
+    // With F.group_lobes > 0 a window holds up to F.group_lobes paths, sized
+    // so that every block gets the same number of windows, and is regrouped
+    // by the lobe family of its hits (a counting sort in shared memory) so
+    // that a warp mostly runs one family's code -- a level's paths hit every
+    // kind of material in queue order; the block synchronises once per
+    // window, not once per path of a thread.  Otherwise a window is one
+    // block of paths in queue order.  Every path is shaded exactly once and
+    // its result does not depend on its slot.
+    const bool group = F.group_lobes > 0;
     __shared__ int fam_count[8];
-    __shared__ int order[SHADE_MAX_BLOCK];
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        int i = base + threadIdx.x;
+    __shared__ int order[SHADE_WINDOW];
+    __shared__ unsigned char fam_of[SHADE_WINDOW];
+    const int lane = threadIdx.x & 31;
+    int win = blockDim.x;
+    if (group && n > 0) {
+        const int wmax = max((int)blockDim.x, (min(F.group_lobes, SHADE_WINDOW) / (int)blockDim.x) * (int)blockDim.x);
+        const int per_sweep = gridDim.x * wmax;   // n <= 2^25 and per_sweep <= 2^21: no overflow
+        const int sweeps = (n + per_sweep - 1) / per_sweep;
+        win = (n + gridDim.x * sweeps - 1) / (gridDim.x * sweeps);
+    }
+    // the counting loops run over whole blocks (full warps for the warp votes)
+    const int span = (win + blockDim.x - 1) / blockDim.x * blockDim.x;
+    for (int w0 = blockIdx.x * win; w0 < n; w0 += gridDim.x * win) {
+        const int m = min(win, n - w0);
         if (group) {
-            const int fam = i < n ? lobe_family(F.scene, F.hits[i]) : 5;
             if (threadIdx.x < 8) fam_count[threadIdx.x] = 0;
             __syncthreads();
-            const int rank = atomicAdd(&fam_count[fam], 1);
+            // count each family (one shared atomic per family present in a warp)
+            for (int j = threadIdx.x; j < span; j += blockDim.x) {
+                const int f = j < m ? lobe_family(F.scene, F.hits[w0 + j]) : 5;
+                fam_of[j] = (unsigned char)f;
+                const unsigned peers = __match_any_sync(0xffffffffu, f);
+                if (lane == __ffs(peers) - 1) atomicAdd(&fam_count[f], __popc(peers));
+            }
             __syncthreads();
-            int off = 0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) off += k < fam ? fam_count[k] : 0;
-            order[off + rank] = i;
+            if (threadIdx.x == 0) {
+                int off = 0;
+                for (int k = 0; k < 6; ++k) {
+                    const int c = fam_count[k];
+                    fam_count[k] = off;
+                    off += c;
+                }
+            }
             __syncthreads();
-            i = order[threadIdx.x];
+            // place: the family's offset + the paths of the family placed before
+            for (int j = threadIdx.x; j < span; j += blockDim.x) {
+                const int f = fam_of[j];
+                const unsigned peers = __match_any_sync(0xffffffffu, f);
+                const int leader = __ffs(peers) - 1;
+                int b = 0;
+                if (lane == leader) b = atomicAdd(&fam_count[f], __popc(peers));
+                b = __shfl_sync(0xffffffffu, b, leader);
+                order[b + __popc(peers & ((1u << lane) - 1u))] = w0 + j;
+            }
+            __syncthreads();
         }
-        if (i < n) shade_path(F, level, wave0, i, here, next, out);
+        for (int j = threadIdx.x; j < m; j += blockDim.x)
+            shade_path(F, false, level, wave0, group ? order[j] : w0 + j, here, next, out);
         if (group) __syncthreads();
     }
 }
 
 // one kernel per block-size bound, so that the register allocation of the
-// default launch does not depend on the largest one
+// default launch does not depend on the largest one; k_shade* shade level 0
+// (camera hits), k_shade_bounce* levels >= 1 (held to 64 registers: their
+// window loop would otherwise take the allocation past it and cost a quarter
+// of the resident warps)
 __global__ void __launch_bounds__(PATH_BLOCK) k_shade(FrameParams F, int level, long long wave0) {
-    shade_level(F, level, wave0);
+    shade_level<false>(F, level, wave0);
 }
 __global__ void __launch_bounds__(SHADE_MAX_BLOCK) k_shade_wide(FrameParams F, int level, long long wave0) {
-    shade_level(F, level, wave0);
+    shade_level<false>(F, level, wave0);
+}
+__global__ void __launch_bounds__(PATH_BLOCK, 8) k_shade_bounce(FrameParams F, int level, long long wave0) {
+    shade_level<true>(F, level, wave0);
+}
+__global__ void __launch_bounds__(SHADE_MAX_BLOCK, 4) k_shade_bounce_wide(FrameParams F, int level, long long wave0) {
+    shade_level<true>(F, level, wave0);
 }
 
 // Rays the wave traced: extension rays (paths entering levels >= 1) and

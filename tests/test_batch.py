@@ -19,7 +19,7 @@ def test_tuning_defaults_and_errors():
     L = K.load()
     t = K.Tuning()
     L.kpt_tuning_default(C.byref(t))
-    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays, t.fetch_batch, t.group_lobes) == (1.0, 0, 256, 0, 7, 1)
+    assert (t.grid_scale, t.wave_cap, t.shade_block, t.sort_rays, t.fetch_batch, t.group_lobes) == (1.0, 0, 256, 0, 7, 2048)
     assert L.kpt_set_tuning(None, C.byref(t)) == -1
     assert L.kpt_get_tuning(None, C.byref(t)) == -1
     assert L.kpt_submit_batch(None, 1, None, None, 0) == -1
@@ -85,6 +85,9 @@ def reference_frames():
     (0, dict(sort_rays=1)),
     (2, dict(fetch_batch=1)),
     (0, dict(fetch_batch=32)),
+    (0, dict(group_lobes=-1)),
+    (2, dict(group_lobes=64, shade_block=128)),
+    (0, dict(group_lobes=256, shade_block=64)),
 ])
 def test_batch_matches_one_by_one(reference_frames, lanes, tuning):
     from kittlespt_gb300.renderer import Batch
@@ -135,6 +138,9 @@ def test_batch_errors():
             rs[0].set_tuning(sort_rays=2)
         with pytest.raises(K.KptError):
             rs[0].set_tuning(fetch_batch=33)
+        for g in (1, 96, 4096):
+            with pytest.raises(K.KptError):
+                rs[0].set_tuning(group_lobes=g)
     finally:
         for r in rs:
             r.shutdown()
