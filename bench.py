@@ -381,7 +381,8 @@ def run_gpu(args):
     batch = None
     if rank == 0 and not args.no_batch:
         batch = batch_rate(3, 1)
-        print(f"[bench] 32 mixed jobs: batched {batch['batched']['Msamples_per_s']:.0f} Msamples/s, one by one "
+        print(f"[bench] 32 mixed jobs: batched {batch['batched']['Msamples_per_s']:.0f} Msamples/s (graph branches "
+              f"{batch['batched_branches']['Msamples_per_s']:.0f}), one by one "
               f"{batch['one_by_one']['Msamples_per_s']:.0f} ({batch['speedup']:.2f}x)", file=sys.stderr)
     adjoint = None
     if rank == 0 and not args.no_adjoint:
@@ -515,13 +516,21 @@ def batch_rate(steps, warmup):
         batched(lanes)   # instantiate the tuned graph outside the timed rounds
         seq = [one_by_one() for _ in range(steps)]
         bat = [batched(lanes) for _ in range(steps)]
+        # the same batch with each job's frame a branch of the graph (no
+        # queue spanning the jobs)
+        b.shared = False
+        batched(lanes)
+        br = [batched(lanes) for _ in range(steps)]
+        b.shared = True
     for r in rs:
         r.shutdown()
     torch.cuda.synchronize()
     seq_ms = float(np.mean([t for t, _ in seq]))
     bat_ms = float(np.mean([t for t, _ in bat]))
+    br_ms = float(np.mean([t for t, _ in br]))
     seq_lat = np.concatenate([l for _, l in seq])
     bat_lat = np.concatenate([l for _, l in bat])
+    br_lat = np.concatenate([l for _, l in br])
     return {"value": samples / bat_ms / 1e3, "unit": "Msamples/s", "ms_per_step": bat_ms,
            "config": {"workload": "batch_32_mixed_jobs", "jobs": BATCH_JOBS, "samples_per_round": samples,
                       "resolutions": [f"{sc.width}x{sc.height}" for sc in jobs], "spp": spp,
@@ -529,7 +538,12 @@ def batch_rate(steps, warmup):
                       "instances": [len(sc.instances) for sc in jobs]},
            "batched": {"Msamples_per_s": samples / bat_ms / 1e3, "round_ms": bat_ms,
                        "p50_latency_ms": float(np.percentile(bat_lat, 50)),
-                       "p99_latency_ms": float(np.percentile(bat_lat, 99))},
+                       "p99_latency_ms": float(np.percentile(bat_lat, 99)),
+                       "mode": "shared ray queues spanning the jobs"},
+           "batched_branches": {"Msamples_per_s": samples / br_ms / 1e3, "round_ms": br_ms,
+                                "p50_latency_ms": float(np.percentile(br_lat, 50)),
+                                "p99_latency_ms": float(np.percentile(br_lat, 99)),
+                                "mode": "each job's frame a branch of the graph"},
            "one_by_one": {"Msamples_per_s": samples / seq_ms / 1e3, "round_ms": seq_ms,
                           "p50_latency_ms": float(np.percentile(seq_lat, 50)),
                           "p99_latency_ms": float(np.percentile(seq_lat, 99))},

@@ -350,15 +350,26 @@ kpt_status kpt_get_tuning(kpt_context* ctx, kpt_tuning* t);
 
 /* A batch renders one frame (spp samples, then the post chain) of each of n
  * jobs -- contexts of the batch's device, each with its own scene, camera,
- * resolution and settings, none twice -- as branches of one CUDA graph on the
- * batch's stream: `lanes` chains of jobs run concurrently (jobs are dealt to
- * the lanes longest first by W*H*spp*max_depth; lanes <= 0 or >= n: one lane
- * per job).  kpt_submit_batch returns after the launch; kpt_wait_batch waits
- * and returns each job's device latency from the start of the batch to the
- * end of its frame (job_ms[n], may be null) and the batch's device time. */
+ * resolution and settings, none twice -- as one CUDA graph on the batch's
+ * stream.  Shared queues (the default, kpt_batch_set_shared(b, 1)): when
+ * every job's frame is one wave (W*H*spp <= its wave_cap) without the octant
+ * sort, each level's extension rays and shadow rays of all jobs are traced by
+ * one persistent launch each, from one queue spanning the jobs, in a merged
+ * copy of the jobs' scenes (rebuilt only when a job or its scene changes);
+ * the jobs' camera rays, shading, sky and post chains run concurrently on
+ * their own streams and `lanes` is not used.  Otherwise (or with
+ * kpt_batch_set_shared(b, 0)) each job's frame is a branch of the graph:
+ * `lanes` chains of jobs run concurrently (jobs are dealt to the lanes
+ * longest first by W*H*spp*max_depth; lanes <= 0 or >= n: one lane per
+ * job).  Either way every job's frame is the one it renders alone, bit for
+ * bit.  kpt_submit_batch returns after the launch; kpt_wait_batch waits and
+ * returns each job's device latency from the start of the batch to the end
+ * of its frame (job_ms[n], may be null) and the batch's device time. */
 typedef struct kpt_batch kpt_batch;
 kpt_status kpt_batch_create(int device, kpt_batch** out);
 kpt_status kpt_batch_destroy(kpt_batch* b);
+kpt_status kpt_batch_set_shared(kpt_batch* b, int shared);   /* 1 (default) or 0; not while a batch is pending */
+kpt_status kpt_batch_get_shared(kpt_batch* b, int* shared);
 kpt_status kpt_submit_batch(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp, int lanes);
 kpt_status kpt_wait_batch(kpt_batch* b, float* job_ms, float* total_ms);
 

@@ -138,6 +138,8 @@ SIGNATURES = {
     "kpt_batch_create": (_S, [C.c_int, C.POINTER(_P)]),
     "kpt_batch_destroy": (_S, [_P]),
     "kpt_submit_batch": (_S, [_P, C.c_int, C.POINTER(_P), _I, C.c_int]),
+    "kpt_batch_set_shared": (_S, [_P, C.c_int]),
+    "kpt_batch_get_shared": (_S, [_P, _I]),
     "kpt_wait_batch": (_S, [_P, _F, _F]),
     "kpt_autotune_batch": (_S, [_P, C.c_int, C.POINTER(_P), _I, C.c_int, C.POINTER(Tuning), _I, _F]),
     "kpt_adjoint_param_count": (_S, [_P, C.POINTER(C.c_int)]),

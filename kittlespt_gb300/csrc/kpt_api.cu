@@ -7,6 +7,7 @@
 // bloom chain, tonemap) re-captured and updated in place each frame, with no
 // host synchronisation inside it.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -64,6 +65,8 @@ struct DBuf {
         n = 0;
     }
 };
+
+std::atomic<unsigned long long> g_scene_versions{0};
 
 void rows_of(const float* cm, float4* rows, int nrows) {   // column-major Mat4 -> rows
     for (int r = 0; r < nrows; ++r) rows[r] = make_float4(cm[r], cm[4 + r], cm[8 + r], cm[12 + r]);
@@ -172,6 +175,10 @@ struct kpt_context {
     DBuf<ShadowRec> shadow;
     int wave_cap = 0;
     bool device_blas = false;   // kpt_set_blas_build
+    // the device scene's version (a value no other scene state of any
+    // context has had: a batch's merged scene is rebuilt when one changes)
+    unsigned long long scene_version = 0;
+    int n_nodes = 0, n_tris = 0;   // BLAS nodes and triangles on the device
     kpt_tuning tuning{};   // launch parameters of the path stage (kpt_set_tuning)
 
     // stage timing inside the frame graph: per frame, event-record nodes
@@ -506,6 +513,7 @@ kpt_status kpt_refit_mesh(kpt_context* c, int mesh, const float* positions, cons
     const int tb = c->mesh_tri_base[mesh];
     const int e = refit_blas_device(m, c->d_nodes.p, c->mesh_node_base[mesh], c->d_tris.p, tb, c->d_shade.p, c->stream);
     if (e != 0) return fail(KPT_ERR_CUDA, std::string("kpt_refit_mesh: ") + cudaGetErrorString((cudaError_t)e));
+    c->scene_version = ++g_scene_versions;
     // the lights on the mesh's triangles
     bool lights = false;
     for (LightRec& L : c->h_lights) {
@@ -599,6 +607,7 @@ static kpt_status rebuild_tlas(kpt_context* c) {
     KPT_CUDA(c->d_inst.upload(c->h_inst.data(), c->h_inst.size(), c->stream));
     c->view.inst = c->d_inst.p;
     c->tlas_dirty = false;
+    c->scene_version = ++g_scene_versions;
     return KPT_OK;
 }
 
@@ -707,6 +716,8 @@ kpt_status kpt_commit_scene(kpt_context* c) {
     static_assert(sizeof(MatRec) == sizeof(kpt_material), "material layout");
     std::memcpy(mats.data(), c->materials.data(), sizeof(kpt_material) * mats.size());
     KPT_CUDA(c->d_nodes.upload(nodes.data(), nodes.size(), c->stream));
+    c->n_nodes = (int)nodes.size();
+    c->n_tris = (int)(tris.size() / 3);
     KPT_CUDA(c->d_tris.upload(tris.data(), tris.size(), c->stream));
     KPT_CUDA(c->d_shade.upload(shade.data(), shade.size(), c->stream));
     KPT_CUDA(c->d_meshes.upload(mrec.data(), mrec.size(), c->stream));
@@ -1005,23 +1016,60 @@ static void stage_mark(kpt_context* c, int stage) {
 
 // The path stage: camera rays and their sky, then the wave(s) of paths level
 // by level, the queued sky and the ordered accumulation of every sample.
-static void enqueue_paths(kpt_context* c, const FrameParams& F) {
-    c->levels_depth = F.max_depth;
+// camera rays and their sky
+static void enqueue_camera(kpt_context* c, const FrameParams& F) {
     cudaStream_t s = c->stream;
-    const int np = c->W * c->H;
-    const int D = F.max_depth;
+    c->levels_depth = F.max_depth;
     cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s);
     stage_mark(c, KPT_STAGE_CAMERA);
     k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
     k_primary<<<primary_blocks(c->W, c->H), PATH_BLOCK, 0, s>>>(F);
     k_primary_sky<<<persistent_grid(c, (const void*)k_primary_sky, PATH_BLOCK), PATH_BLOCK, 0, s>>>(F);
     c->launches += 3;
+}
+
+// the start of a wave: its level counters cleared; with `mark`, the sky
+// queue's length recorded as where its level 0 begins
+static void enqueue_wave_start(kpt_context* c, const FrameParams& F, bool mark) {
+    cudaStream_t s = c->stream;
+    const int D = F.max_depth;
+    cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
+    if (mark)
+        cudaMemcpyAsync(c->level_counts.p + LEVEL_WORDS * (D + 1) + 5, c->counts.p + 2, sizeof(int),
+                        cudaMemcpyDeviceToDevice, s);
+    if (F.unsorted) cudaMemsetAsync(c->octants.p, 0, sizeof(int) * 16 * (size_t)(D + 2), s);
+}
+
+// the shading of level l of the wave starting at item w0
+static void enqueue_shade(kpt_context* c, const FrameParams& F, int l, long long w0) {
+    cudaStream_t s = c->stream;
     const int shade_block = c->tuning.shade_block > 0 ? c->tuning.shade_block : SHADE_BLOCK;
     const bool wide = shade_block > PATH_BLOCK;
-    const void* shade_fn = wide ? (const void*)k_shade_wide : (const void*)k_shade;
-    const int g_shade = persistent_grid(c, shade_fn, shade_block);
-    const int g_bounce = persistent_grid(c, wide ? (const void*)k_shade_bounce_wide : (const void*)k_shade_bounce,
-                                         shade_block);
+    if (l > 0) {
+        const int g = persistent_grid(c, wide ? (const void*)k_shade_bounce_wide : (const void*)k_shade_bounce,
+                                      shade_block);
+        if (wide) k_shade_bounce_wide<<<g, shade_block, 0, s>>>(F, l, w0);
+        else k_shade_bounce<<<g, shade_block, 0, s>>>(F, l, w0);
+    } else {
+        const int g = persistent_grid(c, wide ? (const void*)k_shade_wide : (const void*)k_shade, shade_block);
+        if (wide) k_shade_wide<<<g, shade_block, 0, s>>>(F, l, w0);
+        else k_shade<<<g, shade_block, 0, s>>>(F, l, w0);
+    }
+}
+
+// the ordered accumulation of every sample
+static void enqueue_path_end(kpt_context* c, const FrameParams& F) {
+    const int np = c->W * c->H;
+    stage_mark(c, KPT_STAGE_ACCUMULATE);
+    k_accumulate<<<(np + 255) / 256, 256, 0, c->stream>>>(F);
+    c->launches += 1;
+}
+
+static void enqueue_paths(kpt_context* c, const FrameParams& F) {
+    cudaStream_t s = c->stream;
+    const int np = c->W * c->H;
+    const int D = F.max_depth;
+    enqueue_camera(c, F);
     const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
     const int g_shd = persistent_grid(c, (const void*)k_shadow, TRACE_BLOCK);
     // every pixel may hit: the last waves find no work when fewer do
@@ -1032,12 +1080,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
     const bool fork = c->tf == nullptr && c->ev_fork.size() >= (size_t)D + 1;
     const int g_sky = persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK);
     for (long long w0 = 0; w0 < items; w0 += F.cap) {
-        cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s);
-        // the sky queue's length when the wave starts: where its level 0 begins
-        if (fork)
-            cudaMemcpyAsync(c->level_counts.p + LEVEL_WORDS * (D + 1) + 5, c->counts.p + 2, sizeof(int),
-                            cudaMemcpyDeviceToDevice, s);
-        if (F.unsorted) cudaMemsetAsync(c->octants.p, 0, sizeof(int) * 16 * (size_t)(D + 2), s);
+        enqueue_wave_start(c, F, fork);
         for (int l = 0; l <= D; ++l) {
             if (l > 0) {
                 stage_mark(c, KPT_STAGE_EXTEND);
@@ -1045,13 +1088,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
                 if (fork) cudaStreamWaitEvent(s, c->ev_join[l - 1], 0);
             }
             stage_mark(c, KPT_STAGE_SHADE);
-            if (l > 0) {
-                if (wide) k_shade_bounce_wide<<<g_bounce, shade_block, 0, s>>>(F, l, w0);
-                else k_shade_bounce<<<g_bounce, shade_block, 0, s>>>(F, l, w0);
-            } else {
-                if (wide) k_shade_wide<<<g_shade, shade_block, 0, s>>>(F, l, w0);
-                else k_shade<<<g_shade, shade_block, 0, s>>>(F, l, w0);
-            }
+            enqueue_shade(c, F, l, w0);
             stage_mark(c, KPT_STAGE_SHADOW);
             if (fork) {
                 cudaEventRecord(c->ev_fork[l], s);
@@ -1086,9 +1123,7 @@ static void enqueue_paths(kpt_context* c, const FrameParams& F) {
         k_sky_queue<<<g_sky, PATH_BLOCK, 0, s>>>(F, -1);
         c->launches += 1;
     }
-    stage_mark(c, KPT_STAGE_ACCUMULATE);
-    k_accumulate<<<(np + 255) / 256, 256, 0, s>>>(F);
-    c->launches += 1;
+    enqueue_path_end(c, F);
 }
 
 static kpt_status ready(kpt_context* c) {
@@ -1123,10 +1158,11 @@ static void update_thresholds(kpt_context* c) {
 // The frame: enqueued on the context stream (captured into a graph).
 static void enqueue_temporal(kpt_context* c, const FrameParams& F);
 
-static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
+// what follows the path stage: temporal blend or resolve, exposure, upscale,
+// bloom, tonemap, lens effects
+static void enqueue_post(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
     cudaStream_t s = c->stream;
     const int np = c->W * c->H;
-    enqueue_paths(c, F);
     stage_mark(c, KPT_STAGE_POST);
     if (c->settings.temporal_accumulation) {
         enqueue_temporal(c, F);
@@ -1200,6 +1236,11 @@ static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_sample
         c->launches += 1;
     }
     stage_mark(c, KPT_STAGE_COUNT);   // end of the last interval
+}
+
+static void enqueue_frame(kpt_context* c, const FrameParams& F, int total_samples, float delta_ms) {
+    enqueue_paths(c, F);
+    enqueue_post(c, F, total_samples, delta_ms);
 }
 
 // Host-side work of a frame, outside any capture: TLAS rebuild, exposure
@@ -1854,6 +1895,23 @@ struct kpt_batch {
         float ms;
     };
     std::map<std::string, Choice> cache;   // batch signature -> autotuned choice
+    // One queue per ray stage spanning the jobs (kpt_batch_set_shared): the
+    // merged scene, the key it was built for (each job and its scene
+    // version), the jobs' table and the level queues.
+    int shared = 1;
+    cudaStream_t side = nullptr;   // the shadow rays beside the extension rays
+    cudaEvent_t ev_counts = nullptr, ev_shadow = nullptr, ev_level = nullptr;
+    DBuf<BvhNode> m_nodes, m_tlas;
+    DBuf<float4> m_tris;
+    DBuf<MeshRec> m_meshes;
+    DBuf<InstRec> m_inst;
+    SceneView m_view{};
+    std::vector<std::pair<const kpt_context*, unsigned long long>> m_key;
+    std::vector<int> m_tlas_root, m_inst_base;
+    std::vector<BatchJob> h_jobs;
+    DBuf<BatchJob> d_jobs;
+    DBuf<int> d_queues;                    // extension prefix [n + 1], shadow prefix [n + 1], fetch [2]
+    DBuf<unsigned long long> d_counters;   // traversal counters of the batch's ray kernels
 };
 
 namespace {
@@ -1875,6 +1933,75 @@ double job_cost(const kpt_context* c, int spp) {
     return (double)c->W * c->H * spp * (c->settings.max_depth + 1);
 }
 
+// The batch's merged scene: every job's BLAS nodes, triangles, meshes,
+// instances and TLAS nodes one after the other, their indices moved by the
+// job's offsets (enqueued on the batch stream; rebuilt only when the jobs or
+// one of their scenes changed).
+kpt_status merge_scenes(kpt_batch* b, int n, kpt_context* const* jobs) {
+    std::vector<std::pair<const kpt_context*, unsigned long long>> key(n);
+    for (int j = 0; j < n; ++j) key[j] = {jobs[j], jobs[j]->scene_version};
+    if (key == b->m_key) return KPT_OK;
+    long long nn = 0, nt = 0, nm = 0, ni = 0, nl = 0;
+    for (int j = 0; j < n; ++j) {
+        nn += jobs[j]->n_nodes;
+        nt += jobs[j]->n_tris;
+        nm += (long long)jobs[j]->meshes.size();
+        ni += (long long)jobs[j]->instances.size();
+        nl += jobs[j]->view.ntlas;
+    }
+    if (nn > INT32_MAX / 2 || nt > INT32_MAX / 4 || nm > INT32_MAX || ni > INT32_MAX / 2 || nl > INT32_MAX / 2)
+        return fail(KPT_ERR_INVALID, "kpt_submit_batch: the jobs' scenes together are too large to merge");
+    b->m_key.clear();
+    KPT_CUDA(b->m_nodes.ensure(nn));
+    KPT_CUDA(b->m_tris.ensure(3 * nt));
+    KPT_CUDA(b->m_meshes.ensure(nm));
+    KPT_CUDA(b->m_inst.ensure(ni));
+    KPT_CUDA(b->m_tlas.ensure(nl));
+    b->m_tlas_root.assign(n, 0);
+    b->m_inst_base.assign(n, 0);
+    int node_base = 0, tri_base = 0, mesh_base = 0, inst_base = 0, tlas_base = 0;
+    auto blocks = [](int k) { return (k + 255) / 256; };
+    for (int j = 0; j < n; ++j) {
+        const kpt_context* c = jobs[j];
+        const int nodes = c->n_nodes, tris = c->n_tris, meshes = (int)c->meshes.size();
+        const int inst = (int)c->instances.size(), tlas = c->view.ntlas;
+        if (nodes > 0)
+            k_merge_nodes<<<blocks(nodes), 256, 0, b->stream>>>(c->d_nodes.p, nodes, b->m_nodes.p + node_base,
+                                                                 node_base, tri_base);
+        if (tris > 0)
+            KPT_CUDA(cudaMemcpyAsync(b->m_tris.p + 3 * (size_t)tri_base, c->d_tris.p, 3 * sizeof(float4) * (size_t)tris,
+                                     cudaMemcpyDeviceToDevice, b->stream));
+        if (meshes > 0)
+            k_merge_meshes<<<blocks(meshes), 256, 0, b->stream>>>(c->d_meshes.p, meshes, b->m_meshes.p + mesh_base,
+                                                                   node_base, tri_base);
+        if (inst > 0)
+            k_merge_inst<<<blocks(inst), 256, 0, b->stream>>>(c->d_inst.p, inst, b->m_inst.p + inst_base, mesh_base);
+        if (tlas > 0)
+            k_merge_nodes<<<blocks(tlas), 256, 0, b->stream>>>(c->d_tlas.p, tlas, b->m_tlas.p + tlas_base, tlas_base,
+                                                                inst_base);
+        KPT_CUDA(cudaGetLastError());
+        b->m_tlas_root[j] = c->view.tlas_root_leaf ? -inst_base - 1 : tlas_base;
+        b->m_inst_base[j] = inst_base;
+        node_base += nodes;
+        tri_base += tris;
+        mesh_base += meshes;
+        inst_base += inst;
+        tlas_base += tlas;
+    }
+    SceneView v{};
+    v.nodes = b->m_nodes.p;
+    v.tris = b->m_tris.p;
+    v.meshes = b->m_meshes.p;
+    v.inst = b->m_inst.p;
+    v.tlas = b->m_tlas.p;
+    v.ntlas = tlas_base;
+    v.ninst = inst_base;
+    v.fetch_batch = jobs[0]->view.fetch_batch;
+    b->m_view = v;
+    b->m_key = key;
+    return KPT_OK;
+}
+
 std::string batch_signature(int n, kpt_context* const* jobs, const int32_t* spp) {
     std::string sig;
     for (int j = 0; j < n; ++j) {
@@ -1887,7 +2014,135 @@ std::string batch_signature(int n, kpt_context* const* jobs, const int32_t* spp)
 
 }  // namespace
 
+// The batch as one graph whose ray stages span the jobs: each job's camera
+// rays, shading, sky, accumulation and post chain on its own streams; per
+// level, once every job has shaded it, one k_batch_level, one k_shadow_batch
+// (the level's shadow rays of every job) beside one k_extend_batch (the next
+// level's extension rays of every job), in the merged scene.  Each job's
+// sky of a level follows the batch's shadow rays of that level, its next
+// shading both ray kernels, so every job's buffers see the same sequence of
+// writes as when it renders alone.
+static kpt_status submit_shared(kpt_batch* b, int n, kpt_context* const* jobs, const int32_t* spp,
+                                const std::vector<FrameParams>& F) {
+    kpt_status st = merge_scenes(b, n, jobs);
+    if (st != KPT_OK) return st;
+    int D = 0;
+    b->h_jobs.assign(n, BatchJob{});
+    for (int j = 0; j < n; ++j) {
+        const kpt_context* c = jobs[j];
+        BatchJob& J = b->h_jobs[j];
+        J.tlas_lo = c->view.tlas_lo;
+        J.tlas_hi = c->view.tlas_hi;
+        J.paths[0] = F[j].paths[0];
+        J.paths[1] = F[j].paths[1];
+        J.hits = F[j].hits;
+        J.shadow = F[j].shadow;
+        J.radiance = F[j].radiance;
+        J.level_counts = F[j].level_counts;
+        J.counts = F[j].counts;
+        J.tlas_root = b->m_tlas_root[j];
+        J.ninst = c->view.ninst;
+        J.inst_base = b->m_inst_base[j];
+        J.cap = F[j].cap;
+        J.max_depth = F[j].max_depth;
+        D = std::max(D, F[j].max_depth);
+    }
+    KPT_CUDA(b->d_jobs.upload(b->h_jobs.data(), n, b->stream));
+    KPT_CUDA(b->d_queues.ensure(2 * (size_t)(n + 1) + 2));
+    KPT_CUDA(b->d_counters.ensure(16));
+    KPT_CUDA(cudaMemsetAsync(b->d_counters.p, 0, 16 * sizeof(unsigned long long), b->stream));
+    BatchQueues Q;
+    Q.ext_prefix = b->d_queues.p;
+    Q.shd_prefix = b->d_queues.p + (n + 1);
+    Q.fetch = b->d_queues.p + 2 * (n + 1);
+    Q.jobs = b->d_jobs.p;
+    Q.njobs = n;
+    const int sms = jobs[0]->sm_count;
+    int per_ext = 0, per_shd = 0;
+    KPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ext, k_extend_batch, TRACE_BLOCK, 0));
+    KPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_shd, k_shadow_batch, TRACE_BLOCK, 0));
+    const int g_ext = std::max(1, per_ext) * sms, g_shd = std::max(1, per_shd) * sms;
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        cudaEventRecordWithFlags(b->ev_start, b->stream, cudaEventRecordExternal);
+        cudaEventRecord(b->ev_fork, b->stream);
+        for (int j = 0; j < n; ++j) {
+            kpt_context* c = jobs[j];
+            cudaStreamWaitEvent(c->stream, b->ev_fork, 0);
+            enqueue_camera(c, F[j]);
+            enqueue_wave_start(c, F[j], true);
+        }
+        for (int l = 0; l <= D; ++l) {
+            for (int j = 0; j < n; ++j) {
+                kpt_context* c = jobs[j];
+                if (F[j].max_depth < l) continue;
+                if (l > 0) cudaStreamWaitEvent(c->stream, b->ev_level, 0);
+                enqueue_shade(c, F[j], l, 0);
+                cudaEventRecord(c->ev_fork[l], c->stream);
+                cudaStreamWaitEvent(b->stream, c->ev_fork[l], 0);
+            }
+            k_batch_level<<<1, 32, 0, b->stream>>>(Q, l);
+            cudaEventRecord(b->ev_counts, b->stream);
+            cudaStreamWaitEvent(b->side, b->ev_counts, 0);
+            k_shadow_batch<<<g_shd, TRACE_BLOCK, 0, b->side>>>(b->m_view, Q, l, b->d_counters.p);
+            cudaEventRecord(b->ev_shadow, b->side);
+            for (int j = 0; j < n; ++j) {
+                kpt_context* c = jobs[j];
+                if (F[j].max_depth < l) continue;
+                // the level's sky entries are final (their paths ended)
+                cudaStreamWaitEvent(c->sky, b->ev_shadow, 0);
+                k_sky_queue<<<persistent_grid(c, (const void*)k_sky_queue, PATH_BLOCK), PATH_BLOCK, 0, c->sky>>>(F[j], l);
+                c->launches += 2;   // its shading and sky of the level
+            }
+            if (l < D) k_extend_batch<<<g_ext, TRACE_BLOCK, 0, b->stream>>>(b->m_view, Q, l + 1, b->d_counters.p);
+            cudaStreamWaitEvent(b->stream, b->ev_shadow, 0);
+            cudaEventRecord(b->ev_level, b->stream);
+            // the jobs whose last level this was: their sky, ray counts,
+            // accumulation and post chain
+            for (int j = 0; j < n; ++j) {
+                kpt_context* c = jobs[j];
+                if (F[j].max_depth != l) continue;
+                cudaStreamWaitEvent(c->stream, b->ev_shadow, 0);
+                cudaEventRecord(c->ev_sky, c->sky);
+                cudaStreamWaitEvent(c->stream, c->ev_sky, 0);
+                k_count_rays<<<1, 32, 0, c->stream>>>(F[j]);
+                c->launches += 1;
+                enqueue_path_end(c, F[j]);
+                enqueue_post(c, F[j], c->frame_index + spp[j], c->settings.frame_delta_ms);
+                cudaEventRecordWithFlags(b->ev_end[j], c->stream, cudaEventRecordExternal);
+                cudaEventRecord(b->ev_dep[j], c->stream);
+            }
+        }
+        for (int j = 0; j < n; ++j) cudaStreamWaitEvent(b->stream, b->ev_dep[j], 0);
+        ce = cudaStreamEndCapture(b->stream, &g);
+    }
+    KPT_CUDA(ce);
+    st = instantiate(g, &b->exec);
+    if (st != KPT_OK) return st;
+    KPT_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    KPT_CUDA(cudaEventRecord(b->ev_done, b->stream));
+    for (int j = 0; j < n; ++j) {
+        KPT_CUDA(cudaStreamWaitEvent(jobs[j]->stream, b->ev_done, 0));
+        finish_frame(jobs[j], spp[j]);
+    }
+    return KPT_OK;
+}
+
 extern "C" {
+
+kpt_status kpt_batch_set_shared(kpt_batch* b, int shared) {
+    if (!b || (shared != 0 && shared != 1)) return fail(KPT_ERR_INVALID, "kpt_batch_set_shared: bad arguments");
+    if (b->pending) return fail(KPT_ERR_STATE, "kpt_batch_set_shared: a batch is pending");
+    b->shared = shared;
+    return KPT_OK;
+}
+
+kpt_status kpt_batch_get_shared(kpt_batch* b, int* shared) {
+    if (!b || !shared) return fail(KPT_ERR_INVALID, "kpt_batch_get_shared: bad arguments");
+    *shared = b->shared;
+    return KPT_OK;
+}
 
 kpt_status kpt_batch_create(int device, kpt_batch** out) {
     if (!out) return fail(KPT_ERR_INVALID, "kpt_batch_create: null output");
@@ -1898,6 +2153,10 @@ kpt_status kpt_batch_create(int device, kpt_batch** out) {
     kpt_batch* b = new kpt_batch();
     b->device = device;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_counts, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_shadow, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_level, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&b->ev_start) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming) != cudaSuccess) {
@@ -1917,6 +2176,11 @@ kpt_status kpt_batch_destroy(kpt_batch* b) {
         if (e) cudaEventDestroy(e);
     for (auto* v : {&b->ev_end, &b->ev_dep, &b->ev_pre})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
+    for (cudaEvent_t e : {b->ev_counts, b->ev_shadow, b->ev_level})
+        if (e) cudaEventDestroy(e);
+    b->m_nodes.release(); b->m_tlas.release(); b->m_tris.release(); b->m_meshes.release(); b->m_inst.release();
+    b->d_jobs.release(); b->d_queues.release(); b->d_counters.release();
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return KPT_OK;
@@ -1942,6 +2206,25 @@ kpt_status kpt_submit_batch(kpt_batch* b, int n, kpt_context* const* jobs, const
         if (st != KPT_OK) return st;
         KPT_CUDA(cudaEventRecord(b->ev_pre[j], jobs[j]->stream));
         KPT_CUDA(cudaStreamWaitEvent(b->stream, b->ev_pre[j], 0));
+    }
+    // one queue per ray stage spanning the jobs where every job's frame is
+    // one wave without the octant sort; otherwise each job's frame is a
+    // branch of the graph
+    bool shared = b->shared != 0;
+    long long caps = 0;
+    for (int j = 0; j < n && shared; ++j) {
+        const kpt_context* c = jobs[j];
+        const long long items = (long long)c->W * c->H * spp[j];
+        shared = items <= F[j].cap && F[j].unsorted == nullptr && c->tf == nullptr &&
+                 c->ev_fork.size() >= (size_t)F[j].max_depth + 1;
+        caps += F[j].cap;
+    }
+    if (shared && caps <= INT32_MAX) {
+        st = submit_shared(b, n, jobs, spp, F);
+        if (st != KPT_OK) return st;
+        b->n = n;
+        b->pending = true;
+        return KPT_OK;
     }
     // jobs dealt longest first to the least-loaded lane
     const int L = (lanes <= 0 || lanes >= n) ? n : lanes;

@@ -169,6 +169,32 @@ __device__ __forceinline__ float3 onb_apply_exact(float3 n, float3 l) {
                        xa(xa(xm(c0.z, l.x), xm(c1.z, l.y)), xm(n.z, l.z)));
 }
 
+// One job of a batch whose extension and shadow rays are traced from one
+// queue spanning the jobs (kpt_submit_batch): where the job's wave buffers
+// are and where its scene sits in the batch's merged scene.
+struct __align__(16) BatchJob {
+    float4 tlas_lo, tlas_hi;        // root bounds of the job's TLAS
+    const PathRec* paths[2];
+    PrimaryRec* hits;
+    const ShadowRec* shadow;
+    float4* radiance;
+    int* level_counts;
+    const int* counts;              // counts[2]: the job's sky queue length
+    int tlas_root;                  // merged TLAS: root node, or -(instance) - 1
+    int ninst, inst_base, cap, max_depth, pad[3];
+};
+
+// The ray queues of one level of a batch: the prefix sums of the jobs'
+// extension rays (paths entering the level) and shadow rays, and their
+// fetch counters (written by k_batch_level).
+struct BatchQueues {
+    int* ext_prefix;    // [njobs + 1]
+    int* shd_prefix;    // [njobs + 1]
+    int* fetch;         // [2]: extension, shadow
+    const BatchJob* jobs;
+    int njobs;
+};
+
 // kernels (kpt_path.cu, fast maths)
 __global__ void k_primary(FrameParams F);
 __global__ void k_primary_sky(FrameParams F);
@@ -184,6 +210,16 @@ __global__ void k_sort_scatter(FrameParams F, int level);   // paths entering le
 __global__ void k_shadow(FrameParams F, int level);
 __global__ void k_sky_queue(FrameParams F, int level);
 __global__ void k_sky_constants(FrameParams F, float3* sun_radiance);
+// a batch's queues: after every job's k_shade(level), the extension rays of
+// level + 1 and the shadow rays of level (one block)
+__global__ void k_batch_level(BatchQueues Q, int level);
+__global__ void k_extend_batch(SceneView s, BatchQueues Q, int level, unsigned long long* counters);
+__global__ void k_shadow_batch(SceneView s, BatchQueues Q, int level, unsigned long long* counters);
+// the merged scene of a batch: one job's BLAS / TLAS nodes, meshes and
+// instances with their indices moved by the job's offsets
+__global__ void k_merge_nodes(const BvhNode* src, int n, BvhNode* dst, int node_add, int leaf_add);
+__global__ void k_merge_meshes(const MeshRec* src, int n, MeshRec* dst, int node_add, int tri_add);
+__global__ void k_merge_inst(const InstRec* src, int n, InstRec* dst, int mesh_add);
 // kpt_adjoint.cu (fast maths)
 __global__ void k_adjoint_constants(FrameParams F, AdjParams A);
 __global__ void k_sky_grad(SkyParams P, int n, const float3* dirs, float3* out);

@@ -634,6 +634,167 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameP
     flush_stats(st, F.counters + 8);
 }
 
+// ---------------------------------------------------------------------------
+// A batch's ray stages: the extension rays of level + 1 and the shadow rays
+// of level of every job, each traced by one persistent launch from one queue
+// spanning the jobs, in the batch's merged scene (every job's BLAS and TLAS
+// nodes, triangles, meshes and instances, indices moved by the job's
+// offsets).  An entry's job is found by its place in the prefix sums; its
+// TLAS root is the job's; its result goes to the job's own buffers, in the
+// job's own numbering, so each job's frame is the one it renders alone.
+
+__global__ void k_batch_level(BatchQueues Q, int level) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int e = 0, sh = 0;
+    Q.ext_prefix[0] = Q.shd_prefix[0] = 0;
+    for (int j = 0; j < Q.njobs; ++j) {
+        const BatchJob& J = Q.jobs[j];
+        if (level <= J.max_depth) {
+            int* lc = J.level_counts + LEVEL_WORDS * level;
+            sh += lc[1] + lc[2];
+            // the job's sky queue cannot grow before its k_shade(level + 1):
+            // its length ends level's range (as k_shadow records it)
+            lc[5] = J.counts[2];
+            if (level + 1 <= J.max_depth) e += J.level_counts[LEVEL_WORDS * (level + 1)];
+        }
+        Q.ext_prefix[j + 1] = e;
+        Q.shd_prefix[j + 1] = sh;
+    }
+    Q.fetch[0] = Q.fetch[1] = 0;
+}
+
+// the job whose range of a prefix array holds entry i: the last j with prefix[j] <= i
+__device__ __forceinline__ int batch_job_of(const int* prefix, int njobs, int i) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+struct BatchExtendQueue {
+    BatchQueues Q;
+    int level;   // the level the paths enter
+    int cur;     // job of the entry being set up (ray() then root())
+    __device__ __forceinline__ void ray(int i, float3& o, float3& d, float& tmin, float& tmax) {
+        cur = batch_job_of(Q.ext_prefix, Q.njobs, i);
+        const PathRec& p = Q.jobs[cur].paths[level & 1][i - __ldg(Q.ext_prefix + cur)];
+        const float4 a = p.o_pb, b = p.d_seed;
+        o = make_float3(a.x, a.y, a.z);
+        d = make_float3(b.x, b.y, b.z);
+        tmin = 0.0f;
+        tmax = __int_as_float(0x7f800000);
+    }
+    __device__ __forceinline__ void root(int, float4& lo, float4& hi, int& root, int& ninst) const {
+        const BatchJob& J = Q.jobs[cur];
+        lo = J.tlas_lo;
+        hi = J.tlas_hi;
+        root = J.tlas_root;
+        ninst = J.ninst;
+    }
+    __device__ __forceinline__ bool closest(int i, const Hit& h, float3&, float3&) const {
+        const int j = batch_job_of(Q.ext_prefix, Q.njobs, i);
+        const BatchJob& J = Q.jobs[j];
+        PrimaryRec r;
+        r.t = h.t;
+        r.u = h.u;
+        r.v = h.v;
+        r.inst = h.inst >= 0 ? h.inst - J.inst_base : -1;
+        r.tri = h.tri;
+        r.pad0 = r.pad1 = r.pad2 = 0;
+        J.hits[i - __ldg(Q.ext_prefix + j)] = r;
+        return false;
+    }
+    __device__ __forceinline__ void any(int, bool) const {}
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_extend_batch(SceneView s, BatchQueues Q, int level,
+                                                                               unsigned long long* counters) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    BatchExtendQueue q{Q, level, 0};
+    trace_queue<false, BatchExtendQueue, 1, true>(s, __ldg(Q.ext_prefix + Q.njobs), Q.fetch, q, st, stack);
+    flush_stats(st, counters);
+}
+
+struct BatchShadowQueue {
+    BatchQueues Q;
+    int level;
+    int cur;
+    // the entry's record: sun rays from the front of the job's buffer, light rays from the back
+    __device__ __forceinline__ const ShadowRec& rec(int j, int i) const {
+        const BatchJob& J = Q.jobs[j];
+        const int k = i - __ldg(Q.shd_prefix + j);
+        const int nsun = J.level_counts[LEVEL_WORDS * level + 1];
+        return J.shadow[k < nsun ? k : J.cap - 1 - (k - nsun)];
+    }
+    __device__ __forceinline__ void ray(int i, float3& o, float3& d, float& tmin, float& tmax) {
+        cur = batch_job_of(Q.shd_prefix, Q.njobs, i);
+        const ShadowRec& r = rec(cur, i);
+        const float4 a = r.o_tmax, b = r.d_item;
+        o = make_float3(a.x, a.y, a.z);
+        d = make_float3(b.x, b.y, b.z);
+        tmin = 0.0f;
+        tmax = a.w;
+    }
+    __device__ __forceinline__ void root(int, float4& lo, float4& hi, int& root, int& ninst) const {
+        const BatchJob& J = Q.jobs[cur];
+        lo = J.tlas_lo;
+        hi = J.tlas_hi;
+        root = J.tlas_root;
+        ninst = J.ninst;
+    }
+    __device__ __forceinline__ bool closest(int, const Hit&, float3&, float3&) const { return false; }
+    __device__ __forceinline__ void any(int i, bool occluded) const {
+        if (occluded) return;
+        const int j = batch_job_of(Q.shd_prefix, Q.njobs, i);
+        const ShadowRec& r = rec(j, i);
+        const int item = __float_as_int(r.d_item.w);
+        const float4 c = r.contrib;
+        float4* rad = Q.jobs[j].radiance;
+        const float4 L = rad[item];
+        rad[item] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+    }
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow_batch(SceneView s, BatchQueues Q, int level,
+                                                                               unsigned long long* counters) {
+    int stack[STACK_WORDS];
+    TraceStats st = {0, 0, 0, 0};
+    BatchShadowQueue q{Q, level, 0};
+    trace_queue<true, BatchShadowQueue, 1, true>(s, __ldg(Q.shd_prefix + Q.njobs), Q.fetch + 1, q, st, stack);
+    flush_stats(st, counters ? counters + 8 : nullptr);
+}
+
+__global__ void k_merge_nodes(const BvhNode* src, int n, BvhNode* dst, int node_add, int leaf_add) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BvhNode b = src[i];
+    b.d.x += b.d.y == 0 ? node_add : leaf_add;
+    b.d.z += b.d.w == 0 ? node_add : leaf_add;
+    dst[i] = b;
+}
+
+__global__ void k_merge_meshes(const MeshRec* src, int n, MeshRec* dst, int node_add, int tri_add) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    MeshRec m = src[i];
+    if (m.node_root >= 0) m.node_root += node_add;
+    m.leaf_first += tri_add;
+    m.tri_base += tri_add;
+    dst[i] = m;
+}
+
+__global__ void k_merge_inst(const InstRec* src, int n, InstRec* dst, int mesh_add) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    InstRec r = src[i];
+    r.mesh += mesh_add;
+    dst[i] = r;
+}
+
 // sky * throughput of every path that left the scene, added to its sample:
 // the whole queue (level < 0), or the entries k_shade(level) appended, from
 // the end of level - 1's range (the wave's starting length for level 0) to

@@ -336,8 +336,12 @@ __device__ __forceinline__ bool trace_any(const SceneView& s, const XRay& r, flo
 // closest() may return true with the next ray of entry i (a bounce chain):
 // the lane traces it at once, with the same tmin and tmax.  TRI triangles of
 // a leaf are tested per loop iteration (in order; 1 is fastest on the
-// instanced full frame, 2 on one BLAS of 2M random triangles).
-template <bool ANY, class Src, int TRI = 1>
+// instanced full frame, 2 on one BLAS of 2M random triangles).  ROOTS: the
+// queue spans several scenes merged into `s` (a batch), each entry's TLAS
+// root supplied by
+//                          void root(int i, float4& lo, float4& hi, int& root, int& ninst);
+// (root: a node index of s.tlas, or -(instance) - 1 for a single-instance scene).
+template <bool ANY, class Src, int TRI = 1, bool ROOTS = false>
 __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next, Src& src, TraceStats& st,
                                             int* stack) {
     const float INF = __int_as_float(0x7f800000);
@@ -369,9 +373,16 @@ __device__ __forceinline__ void trace_queue(const SceneView& s, int n, int* next
         count = 0;
         float te;
         st.box_tests++;
-        if (s.ninst > 0 &&
-            slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
-            top = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
+        if constexpr (ROOTS) {
+            float4 lo, hi;
+            int root, ninst;
+            src.root(ray, lo, hi, root, ninst);
+            if (ninst > 0 && slab(lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, w, tmin, tmax0, &te)) top = root;
+        } else {
+            if (s.ninst > 0 &&
+                slab(s.tlas_lo.x, s.tlas_lo.y, s.tlas_lo.z, s.tlas_hi.x, s.tlas_hi.y, s.tlas_hi.z, w, tmin, tmax0, &te))
+                top = s.tlas_root_leaf ? -1 : 0;   // TLAS entries: node index, or -(instance) - 1
+        }
     };
     bool occluded = false;   // ANY: a triangle blocked the ray
     for (;;) {

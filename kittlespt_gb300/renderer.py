@@ -371,8 +371,10 @@ class Renderer:
 
 class Batch:
     """Batched requests (no reference counterpart): one frame of each of many
-    renderers -- each its own scene, camera, resolution and settings -- as
-    concurrent branches of one CUDA graph (kpt_submit_batch), and the
+    renderers -- each its own scene, camera, resolution and settings -- in
+    one CUDA graph (kpt_submit_batch): by default each level's extension and
+    shadow rays of every job traced by one launch from one queue spanning the
+    jobs (shared = True), else each job's frame a concurrent branch; and the
     autotuner that picks their launch parameters (kpt_autotune_batch)."""
 
     def __init__(self, device: int = 0):
@@ -397,6 +399,16 @@ class Batch:
         jobs = (C.c_void_p * n)(*[r._ctx.value for r in renderers])
         s = np.ascontiguousarray(np.broadcast_to(np.asarray(spp, np.int32), (n,)))
         return n, jobs, s
+
+    @property
+    def shared(self) -> bool:
+        v = np.zeros(1, np.int32)
+        K.check(self._L.kpt_batch_get_shared(self._b, K.iptr(v)))
+        return bool(v[0])
+
+    @shared.setter
+    def shared(self, on: bool):
+        K.check(self._L.kpt_batch_set_shared(self._b, int(on)))
 
     def submit(self, renderers, spp, lanes: int = 0):
         n, jobs, s = self._args(renderers, spp)

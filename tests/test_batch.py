@@ -1,11 +1,14 @@
 """Batched requests (kpt_submit_batch / kpt_wait_batch / kpt_autotune_batch).
 
-A batch renders one frame of each job as a branch of one CUDA graph; every
-job's samples are computed exactly as by kpt_render_frame, so images and
-accumulations must be bit-identical to rendering the jobs one by one, under
-any lane count and any launch tuning (grid share, wave capacity -- a small one
-forces many waves --, shading block size, octant sort of the extension
-rays)."""
+A batch renders one frame of each job in one CUDA graph: with shared queues
+(the default) each level's extension and shadow rays of all jobs are traced
+by one launch in the jobs' merged scene, otherwise each job's frame is a
+branch of the graph.  Every job's samples are computed exactly as by
+kpt_render_frame, so images and accumulations must be bit-identical to
+rendering the jobs one by one, in either mode, under any lane count and any
+launch tuning (grid share, wave capacity -- a small one forces many waves and
+the branch mode --, shading block size, octant sort of the extension rays,
+lobe grouping)."""
 
 import ctypes as C
 
@@ -89,7 +92,8 @@ def reference_frames():
     (2, dict(group_lobes=64, shade_block=128)),
     (0, dict(group_lobes=256, shade_block=64)),
 ])
-def test_batch_matches_one_by_one(reference_frames, lanes, tuning):
+@pytest.mark.parametrize("shared", [True, False])
+def test_batch_matches_one_by_one(reference_frames, lanes, tuning, shared):
     from kittlespt_gb300.renderer import Batch
     jobs, ref = reference_frames
     rs = _renderers(jobs)
@@ -99,6 +103,8 @@ def test_batch_matches_one_by_one(reference_frames, lanes, tuning):
             for r in rs:
                 r.set_tuning(**tuning)
         with Batch(0) as b:
+            assert b.shared
+            b.shared = shared
             for _ in range(2):
                 b.submit(rs, spp, lanes=lanes)
                 job_ms, total = b.wait()
@@ -127,6 +133,13 @@ def test_batch_errors():
             b.submit(rs, [1])
             with pytest.raises(K.KptError):
                 b.submit(rs, [1])               # previous batch not waited for
+            b.wait()
+        with Batch(0) as b:
+            with pytest.raises(K.KptError):
+                b.shared = 2                    # not a mode
+            b.submit(rs, [1])
+            with pytest.raises(K.KptError):
+                b.shared = False                # a batch is pending
             b.wait()
         with pytest.raises(K.KptError):
             rs[0].set_tuning(grid_scale=0.0)
