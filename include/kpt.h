@@ -103,6 +103,13 @@ typedef struct kpt_settings {
                                   per ulp against a 1200 m Mie scale height), so the two differ by
                                   up to ~1e-2 relative in places.  The path-replay adjoint always
                                   uses IEEE. */
+    int32_t temporal_arith;    /* arithmetic of the temporal reprojection (temporal_accumulation =
+                                  1): 1 (the default) that of the reference's GPU build, which
+                                  inverts the camera and previous model matrices for every pixel
+                                  with contracted products and an approximate reciprocal (a still
+                                  camera then has a velocity of a few ulps, and the truncated
+                                  previous pixel and the bilinear weights follow them); 0 IEEE
+                                  single precision with the matrices inverted once on the host. */
 } kpt_settings;
 
 /* ExposureValues (pod_types.hpp:9-33) with the compensation and white/black
@@ -234,6 +241,10 @@ kpt_status kpt_read_image(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_render(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_accumulation(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_albedo(kpt_context* ctx, float* rgba);
+/* With temporal accumulation: the blended history the reference keeps in its
+ * accumulation texture (rgb, and the history length in alpha), [H][W]; no
+ * frame rendered with temporal accumulation: KPT_ERR_STATE. */
+kpt_status kpt_read_history(kpt_context* ctx, float* rgba);
 kpt_status kpt_read_histogram(kpt_context* ctx, uint64_t* bins256);
 kpt_status kpt_get_stats(kpt_context* ctx, kpt_stats* st);
 /* Diagnostics, no reference counterpart: for each level 0 .. min(max_levels,

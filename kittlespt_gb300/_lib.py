@@ -46,7 +46,7 @@ class Settings(C.Structure):
                 ("auto_exposure", C.c_int32), ("bloom_final_blend", C.c_float),
                 ("bloom_internal_blend", C.c_float), ("frame_delta_ms", C.c_float), ("rng_order", C.c_int32),
                 ("temporal_accumulation", C.c_int32), ("postprocess_effects", C.c_int32), ("upscale", C.c_int32),
-                ("sky_arith", C.c_int32)]
+                ("sky_arith", C.c_int32), ("temporal_arith", C.c_int32)]
 
 
 class Exposure(C.Structure):
@@ -72,7 +72,7 @@ class Tuning(C.Structure):
 
 
 assert C.sizeof(Material) == 72 and C.sizeof(Environment) == 48
-assert C.sizeof(Settings) == 48 and C.sizeof(Exposure) == 48
+assert C.sizeof(Settings) == 52 and C.sizeof(Exposure) == 48
 
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)
@@ -117,6 +117,7 @@ SIGNATURES = {
     "kpt_read_render": (_S, [_P, _F]),
     "kpt_read_accumulation": (_S, [_P, _F]),
     "kpt_read_albedo": (_S, [_P, _F]),
+    "kpt_read_history": (_S, [_P, _F]),
     "kpt_read_histogram": (_S, [_P, C.POINTER(C.c_uint64)]),
     "kpt_get_stats": (_S, [_P, C.POINTER(Stats)]),
     "kpt_get_level_counts": (_S, [_P, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

@@ -136,6 +136,8 @@ struct kpt_context {
     int tdepth_prev = 0;
     DBuf<TemporalInst> tinst;
     std::vector<TemporalInst> h_tinst;
+    DBuf<TemporalGpuInst> tginst;   // the inverse model matrices for k_temporal_gpu
+    std::vector<TemporalGpuInst> h_tginst;
     float4 tvp[2][4];           // current view-projection rows (the same for both)
     float3 torigin[2];          // previous camera position: first sample, later samples
     DBuf<int4> first_hit;
@@ -241,6 +243,7 @@ void kpt_settings_default(kpt_settings* s) {   // pod_types.hpp:46-57
     s->postprocess_effects = 0;
     s->upscale = 0;
     s->sky_arith = 1;
+    s->temporal_arith = 1;
 }
 
 void kpt_exposure_default(kpt_exposure* e) {   // SampleApp camera_controller.hpp:55-60
@@ -311,7 +314,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
-    c->vis.release(); c->tinst.release(); c->backbuf.release(); c->output.release(); c->easu.release();
+    c->vis.release(); c->tinst.release(); c->tginst.release(); c->backbuf.release(); c->output.release(); c->easu.release();
     for (int k = 0; k < 2; ++k) { c->thist[k].release(); c->tdepth[k].release(); }
     for (auto& m : c->mips) m.release();
     c->hist.release(); c->counters.release(); c->thresholds.release(); c->expo_state.release();
@@ -841,6 +844,8 @@ kpt_status kpt_set_settings(kpt_context* c, const kpt_settings* s) {
     if (s->upscale < 0 || s->upscale > 2) return fail(KPT_ERR_INVALID, "kpt_set_settings: upscale must be 0, 1 or 2");
     if (s->rng_order < 0 || s->rng_order > 7) return fail(KPT_ERR_INVALID, "kpt_set_settings: rng_order must be in 0..7");
     if (s->sky_arith != 0 && s->sky_arith != 1) return fail(KPT_ERR_INVALID, "kpt_set_settings: sky_arith must be 0 or 1");
+    if (s->temporal_arith != 0 && s->temporal_arith != 1)
+        return fail(KPT_ERR_INVALID, "kpt_set_settings: temporal_arith must be 0 or 1");
     const bool resize = (s->upscale != 0) != (c->settings.upscale != 0) && c->OW > 0;
     c->settings = *s;
     if (resize) {   // the render resolution follows the switch at once
@@ -1289,6 +1294,11 @@ static void temporal_matrices(kpt_context* c, bool prev_cam, float4* vp, float3*
     }
 }
 
+// The matrices k_temporal_gpu inverts itself: columns of a column-major Mat4.
+static void columns_of(const float* cm, float4* cols) {
+    for (int k = 0; k < 4; ++k) cols[k] = make_float4(cm[4 * k], cm[4 * k + 1], cm[4 * k + 2], cm[4 * k + 3]);
+}
+
 static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
     kpt_status st = ready(c);
     if (st != KPT_OK) return st;
@@ -1316,6 +1326,15 @@ static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
         std::copy(c->h_tinst.begin(), c->h_tinst.end(), both.begin() + ni);
         c->h_tinst.swap(both);
         KPT_CUDA(c->tinst.upload(c->h_tinst.data(), c->h_tinst.size(), c->stream));
+        c->h_tginst.resize(ni);
+        for (size_t i = 0; i < ni; ++i) {
+            float inv[16], pinv[16];
+            inverse4(c->instances[i].model, inv);         // curr_inv_model_matrix
+            inverse4(c->instances[i].prev_model, pinv);   // prev_inv_model_matrix
+            columns_of(inv, c->h_tginst[i].inv_model);
+            columns_of(pinv, c->h_tginst[i].prev_inv_model);
+        }
+        KPT_CUDA(c->tginst.upload(c->h_tginst.data(), ni, c->stream));
     }
     return KPT_OK;
 }
@@ -1332,7 +1351,8 @@ static void finish_frame(kpt_context* c, int spp) {
 }
 
 static void k_temporal_launch(kpt_context* c, const TemporalParams& T, int np, cudaStream_t s) {
-    k_temporal<<<(np + 255) / 256, 256, 0, s>>>(T);
+    if (c->settings.temporal_arith) k_temporal_gpu<<<(np + 255) / 256, 256, 0, s>>>(T);
+    else k_temporal<<<(np + 255) / 256, 256, 0, s>>>(T);
     c->launches += 1;
 }
 
@@ -1363,6 +1383,13 @@ static void enqueue_temporal(kpt_context* c, const FrameParams& F) {
         T.depth_out = k == 0 ? c->tdepth[c->tdepth_prev ^ 1].p : nullptr;
         T.hist_in = c->thist[k & 1].p;
         T.hist_out = c->thist[(k & 1) ^ 1].p;
+        // the reference's frame k of the call: the previous camera for the
+        // first, the current one after it (executeRendering ends with setView)
+        T.ginst = c->tginst.p;
+        columns_of(c->inv_proj, T.inv_proj);
+        columns_of(c->inv_view, T.inv_view);
+        columns_of(k == 0 ? c->prev_inv_proj : c->inv_proj, T.prev_inv_proj);
+        columns_of(k == 0 ? c->prev_inv_view : c->inv_view, T.prev_inv_view);
         k_temporal_launch(c, T, np, s);
     }
     if (F.nsamples & 1)
@@ -1434,6 +1461,10 @@ kpt_status kpt_read_image(kpt_context* c, float* rgba) { return read_buf(c, c ? 
 kpt_status kpt_read_render(kpt_context* c, float* rgba) { return read_buf(c, c ? c->render.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
 kpt_status kpt_read_accumulation(kpt_context* c, float* rgba) { return read_buf(c, c ? c->acc.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
 kpt_status kpt_read_albedo(kpt_context* c, float* rgba) { return read_buf(c, c ? c->albedo.p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0); }
+kpt_status kpt_read_history(kpt_context* c, float* rgba) {
+    if (c && !c->thist[0].p) return fail(KPT_ERR_STATE, "kpt_read_history: no temporal history");
+    return read_buf(c, c ? c->thist[0].p : nullptr, rgba, c ? 16 * (size_t)c->W * c->H : 0);
+}
 kpt_status kpt_read_histogram(kpt_context* c, uint64_t* bins) { return read_buf(c, c ? c->hist.p : nullptr, bins, 256 * sizeof(uint64_t)); }
 
 kpt_status kpt_get_level_counts(kpt_context* c, int max_levels, int32_t* counts, int32_t* levels) {

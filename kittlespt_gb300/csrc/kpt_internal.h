@@ -240,6 +240,12 @@ struct TemporalInst {
     float4 prev_model[3];      // prev_inv_model_matrix.inverse(), rows 0..2
     float4 pm[4];              // prev view-projection * prev model, rows 0..3
 };
+// The same matrices for k_temporal_gpu, which inverts them itself: per
+// instance the inverse model matrices the host holds (columns).
+struct TemporalGpuInst {
+    float4 inv_model[4];       // curr_inv_model_matrix
+    float4 prev_inv_model[4];  // prev_inv_model_matrix
+};
 // One reference frame of the temporal path: the clamped sample `sample` of
 // every pixel blended into hist_in reprojected, written to hist_out.
 struct TemporalParams {
@@ -257,8 +263,13 @@ struct TemporalParams {
     float* depth_out;          // per pixel: this frame's distance for the next frame, may be null
     const float4* hist_in;
     float4* hist_out;
+    // k_temporal_gpu: the camera's inverse projection and view matrices of
+    // this frame and of the previous one (columns), the instances' inverses
+    const TemporalGpuInst* ginst;
+    float4 inv_proj[4], inv_view[4], prev_inv_proj[4], prev_inv_view[4];
 };
-__global__ void k_temporal(TemporalParams T);
+__global__ void k_temporal(TemporalParams T);       // kpt_post.cu, IEEE
+__global__ void k_temporal_gpu(TemporalParams T);   // kpt_path.cu, the reference GPU build's arithmetic
 __global__ void k_accumulate(FrameParams F);
 __global__ void k_sky(SkyParams P, int n, const float3* dirs, float3* out);
 __global__ void k_trace(SceneView s, int n, const float3* o, const float3* d, float tmin, float tmax,

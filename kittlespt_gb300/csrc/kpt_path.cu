@@ -635,6 +635,152 @@ __global__ void __launch_bounds__(TRACE_BLOCK, TRACE_MIN_BLOCKS) k_shadow(FrameP
 }
 
 // ---------------------------------------------------------------------------
+// Temporal accumulation in the reference GPU build's arithmetic
+// (kpt_settings.temporal_arith = 1): computeVelocity, testReprojection and
+// reprojectAccumulate (kernels.cu:164-223, 299-327) with the matrix
+// inverses, products and divisions computed per pixel as that build computes
+// them -- this translation unit's fast maths: contracted products,
+// approximate reciprocal and square root.  The reference inverts four
+// camera matrices and the previous model matrix for every pixel, and the
+// velocity of a still camera is then a few ulps, not zero: the previous
+// pixel coordinate, truncated, and the bilinear weights follow those ulps.
+// The order of operations is the reference's (Mat4 products row by row left
+// to right, Mat4::inverse's closed form, lerp as a + t (b - a)).
+
+struct M4 {
+    float4 c[4];   // columns
+};
+
+__device__ __forceinline__ M4 m4_load(const float4* cols) {
+    M4 m;
+    for (int k = 0; k < 4; ++k) m.c[k] = cols[k];
+    return m;
+}
+
+// Mat4 * float4 (matrix_maths.cuh:258-267)
+__device__ __forceinline__ float4 m4_apply(const M4& m, float4 v) {
+    return make_float4(m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z + m.c[3].x * v.w,
+                       m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z + m.c[3].y * v.w,
+                       m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z + m.c[3].z * v.w,
+                       m.c[0].w * v.x + m.c[1].w * v.y + m.c[2].w * v.z + m.c[3].w * v.w);
+}
+
+// Mat4 * Mat4 (matrix_maths.cuh:269-283): column j is a * b.c[j]
+__device__ __forceinline__ M4 m4_mul(const M4& a, const M4& b) {
+    M4 r;
+    for (int j = 0; j < 4; ++j) r.c[j] = m4_apply(a, b.c[j]);
+    return r;
+}
+
+// Mat4::inverse (matrix_maths.cuh:304-354): cofactors of the column-major
+// entries, the identity when |det| < 1e-6
+__device__ __forceinline__ M4 m4_inverse(const M4& m) {
+    const float4 c0 = m.c[0], c1 = m.c[1], c2 = m.c[2], c3 = m.c[3];
+    const float s00 = c2.z * c3.w - c3.z * c2.w;
+    const float s01 = c2.y * c3.w - c3.y * c2.w;
+    const float s02 = c2.y * c3.z - c3.y * c2.z;
+    const float s03 = c2.x * c3.w - c3.x * c2.w;
+    const float s04 = c2.x * c3.z - c3.x * c2.z;
+    const float s05 = c2.x * c3.y - c3.x * c2.y;
+    const float det = c0.x * (c1.y * s00 - c1.z * s01 + c1.w * s02) - c0.y * (c1.x * s00 - c1.z * s03 + c1.w * s04) +
+                      c0.z * (c1.x * s01 - c1.y * s03 + c1.w * s05) - c0.w * (c1.x * s02 - c1.y * s04 + c1.z * s05);
+    M4 r;
+    if (fabsf(det) < 1e-6f) {
+        r.c[0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+        r.c[1] = make_float4(0.0f, 1.0f, 0.0f, 0.0f);
+        r.c[2] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+        r.c[3] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        return r;
+    }
+    const float id = 1.0f / det;
+    r.c[0].x = (c1.y * s00 - c1.z * s01 + c1.w * s02) * id;
+    r.c[0].y = -(c0.y * s00 - c0.z * s01 + c0.w * s02) * id;
+    r.c[0].z = (c0.y * (c1.z * c3.w - c1.w * c3.z) - c0.z * (c1.y * c3.w - c1.w * c3.y) + c0.w * (c1.y * c3.z - c1.z * c3.y)) * id;
+    r.c[0].w = -(c0.y * (c1.z * c2.w - c1.w * c2.z) - c0.z * (c1.y * c2.w - c1.w * c2.y) + c0.w * (c1.y * c2.z - c1.z * c2.y)) * id;
+    r.c[1].x = -(c1.x * s00 - c1.z * s03 + c1.w * s04) * id;
+    r.c[1].y = (c0.x * s00 - c0.z * s03 + c0.w * s04) * id;
+    r.c[1].z = -(c0.x * (c1.z * c3.w - c1.w * c3.z) - c0.z * (c1.x * c3.w - c1.w * c3.x) + c0.w * (c1.x * c3.z - c1.z * c3.x)) * id;
+    r.c[1].w = (c0.x * (c1.z * c2.w - c1.w * c2.z) - c0.z * (c1.x * c2.w - c1.w * c2.x) + c0.w * (c1.x * c2.z - c1.z * c2.x)) * id;
+    r.c[2].x = (c1.x * s01 - c1.y * s03 + c1.w * s05) * id;
+    r.c[2].y = -(c0.x * s01 - c0.y * s03 + c0.w * s05) * id;
+    r.c[2].z = (c0.x * (c1.y * c3.w - c1.w * c3.y) - c0.y * (c1.x * c3.w - c1.w * c3.x) + c0.w * (c1.x * c3.y - c1.y * c3.x)) * id;
+    r.c[2].w = -(c0.x * (c1.y * c2.w - c1.w * c2.y) - c0.y * (c1.x * c2.w - c1.w * c2.x) + c0.w * (c1.x * c2.y - c1.y * c2.x)) * id;
+    r.c[3].x = -(c1.x * s02 - c1.y * s04 + c1.z * s05) * id;
+    r.c[3].y = (c0.x * s02 - c0.y * s04 + c0.z * s05) * id;
+    r.c[3].z = -(c0.x * (c1.y * c3.z - c1.z * c3.y) - c0.y * (c1.x * c3.z - c1.z * c3.x) + c0.z * (c1.x * c3.y - c1.y * c3.x)) * id;
+    r.c[3].w = (c0.x * (c1.y * c2.z - c1.z * c2.y) - c0.y * (c1.x * c2.z - c1.z * c2.x) + c0.z * (c1.x * c2.y - c1.y * c2.x)) * id;
+    return r;
+}
+
+__device__ __forceinline__ float4 tex_clamp(const float4* t, int W, int H, int x, int y) {   // cudaBoundaryModeClamp
+    x = min(max(x, 0), W - 1);
+    y = min(max(y, 0), H - 1);
+    return t[(size_t)y * W + x];
+}
+
+__device__ __forceinline__ float4 lerp_fm(float4 a, float4 b, float t) {
+    return make_float4(a.x + t * (b.x - a.x), a.y + t * (b.y - a.y), a.z + t * (b.z - a.z), a.w + t * (b.w - a.w));
+}
+
+__global__ void k_temporal_gpu(TemporalParams T) {
+    const int npix = T.W * T.H;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const int x = p % T.W, y = p / T.W;
+    const int j = T.hit_index[p];
+    float4 L = j < 0 ? T.pixel_sky[p] : T.radiance[(size_t)j * T.nsamples + T.sample];
+    // RGBSpectrum::clampOutput (color.cuh:295-302)
+    if (isnan(L.x) || isnan(L.y) || isnan(L.z) || isinf(L.x) || isinf(L.y) || isinf(L.z))
+        L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float3 curr = make_float3(fmaxf(0.0f, fminf(L.x, 1.0e8f)), fmaxf(0.0f, fminf(L.y, 1.0e8f)),
+                                    fmaxf(0.0f, fminf(L.z, 1.0e8f)));
+    const float4 vs = T.vis[p];
+    if (T.depth_out) T.depth_out[p] = vs.w;
+    float4 out = make_float4(curr.x, curr.y, curr.z, 0.0f);
+    if (j >= 0) {
+        const TemporalGpuInst& I = T.ginst[T.primary[p].inst];
+        // computeVelocity (kernels.cu:164-192)
+        const M4 cvp = m4_mul(m4_inverse(m4_load(T.inv_proj)), m4_inverse(m4_load(T.inv_view)));
+        const M4 pvp = m4_mul(m4_inverse(m4_load(T.prev_inv_proj)), m4_inverse(m4_load(T.prev_inv_view)));
+        const M4 pmodel = m4_inverse(m4_load(I.prev_inv_model));
+        const float4 pos = make_float4(vs.x, vs.y, vs.z, 1.0f);
+        const float4 l4 = m4_apply(m4_load(I.inv_model), pos);
+        const float4 local = make_float4(l4.x, l4.y, l4.z, 1.0f);
+        const float4 cc = m4_apply(cvp, pos);
+        const float4 pc = m4_apply(m4_mul(pvp, pmodel), local);
+        const float cx = cc.x / cc.w, cy = cc.y / cc.w;
+        const float px = pc.x / pc.w, py = pc.y / pc.w;
+        const float vx = (cx + 1.0f) / 2.0f - (px + 1.0f) / 2.0f;
+        const float vy = (cy + 1.0f) / 2.0f - (py + 1.0f) / 2.0f;
+        // reprojectAccumulate (kernels.cu:299-327)
+        const float qx = (float)x - vx * (float)T.W;
+        const float qy = (float)y - vy * (float)T.H;
+        if (!(qx < 0.0f || qx >= (float)T.W || qy < 0.0f || qy >= (float)T.H)) {
+            // testReprojection (kernels.cu:206-223)
+            const int ix = (int)qx, iy = (int)qy;
+            const float d2 = T.prev_depth[(size_t)min(max(iy, 0), T.H - 1) * T.W + min(max(ix, 0), T.W - 1)];
+            const float4 w4 = m4_apply(pmodel, local);
+            const float dx = T.prev_inv_view[3].x - w4.x, dy = T.prev_inv_view[3].y - w4.y,
+                        dz = T.prev_inv_view[3].z - w4.z;
+            const float d1 = sqrtf(dx * dx + dy * dy + dz * dz);
+            if (fabsf(d1 - d2) < d2 * 0.045f) {
+                // DeviceTextureBuffer::textureReadBilinear (device_texture_buffer.cuh:42-80), alpha point-sampled
+                const float ws = qx - (float)ix, wt = qy - (float)iy;
+                const float4 c0 = tex_clamp(T.hist_in, T.W, T.H, ix, iy), c1 = tex_clamp(T.hist_in, T.W, T.H, ix + 1, iy);
+                const float4 c2 = tex_clamp(T.hist_in, T.W, T.H, ix, iy + 1),
+                             c3 = tex_clamp(T.hist_in, T.W, T.H, ix + 1, iy + 1);
+                float4 prev = lerp_fm(lerp_fm(c0, c1, ws), lerp_fm(c2, c3, ws), wt);
+                prev.w = c0.w;
+                const float alpha = 1.0f / fminf(prev.w + 1.0f, 16.0f);
+                out = make_float4(prev.x + alpha * (curr.x - prev.x), prev.y + alpha * (curr.y - prev.y),
+                                  prev.z + alpha * (curr.z - prev.z), prev.w + 1.0f);
+            }
+        }
+    }
+    T.hist_out[p] = out;
+}
+
+// ---------------------------------------------------------------------------
 // A batch's ray stages: the extension rays of level + 1 and the shadow rays
 // of level of every job, each traced by one persistent launch from one queue
 // spanning the jobs, in the batch's merged scene (every job's BLAS and TLAS

@@ -106,7 +106,8 @@ class Renderer:
                                    bloom_final_blend=float(st["bloom_final_blend"]),
                                    bloom_internal_blend=float(st["bloom_internal_blend"]),
                                    frame_delta_ms=float(st["frame_delta_ms"]),
-                                   sky_arith=int(getattr(scene, "sky_arith", 0)))
+                                   sky_arith=int(getattr(scene, "sky_arith", 0)),
+                                   temporal_arith=int(getattr(scene, "temporal_arith", 0)))
         self.set_exposure(scene.exposure)
         self.scene = scene
 
@@ -282,6 +283,10 @@ class Renderer:
 
     def read_albedo(self) -> np.ndarray:
         return self._read_render_res(self._L.kpt_read_albedo)
+
+    def read_history(self) -> np.ndarray:
+        """Temporal accumulation's blended history: rgb, history length in alpha."""
+        return self._read_render_res(self._L.kpt_read_history)
 
     def read_histogram(self) -> np.ndarray:
         out = np.zeros(256, np.uint64)

@@ -366,6 +366,9 @@ class Scene:
     # 0 IEEE single precision, as the oracle and the reference's host build
     # compute them; 1 that of the reference's GPU build
     sky_arith: int = 0
+    # arithmetic of the temporal reprojection (kpt_settings.temporal_arith):
+    # 0 IEEE, as the oracle restates it; 1 that of the reference's GPU build
+    temporal_arith: int = 0
 
     def texture_arrays(self):
         """(desc int32 [n, 4] = width, height, channels, byte offset; pixels
