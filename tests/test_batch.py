@@ -216,3 +216,43 @@ def test_batch_matches_oracle():
         print(f"{sc.width}x{sc.height}x{n}: {(err <= 1e-4).mean():.5f} of pixels within 1e-4")
         assert (err <= 1e-4).mean() >= 0.99
         assert np.abs(acc - s).mean() <= 1e-3 * max(float(np.abs(s).mean()), 1e-3)
+
+
+@pytest.mark.gpu
+def test_batch_follows_scene_changes():
+    """The shared queues trace in a merged copy of the jobs' scenes, rebuilt
+    when a job's scene changes: after an instance moves in one job and a
+    mesh is refit in another, the next batch still matches the same jobs
+    rendered one by one, bit for bit."""
+    from kittlespt_gb300.renderer import Batch
+    jobs = _jobs()
+    spp = [s for _, s in jobs]
+    batched, single = _renderers(jobs), _renderers(jobs)
+
+    def change(rs):
+        sc0 = jobs[0][0]
+        m = np.array(sc0.instances[-1].model, np.float32)
+        m[0, 3] += 0.2
+        assert rs[0].set_mesh_transform(len(sc0.instances) - 1, m)
+        pos = jobs[2][0].meshes[0].positions * np.float32(1.05)
+        rs[2].refit_mesh(0, pos)
+
+    try:
+        with Batch(0) as b:
+            assert b.shared
+            b.submit(batched, spp)
+            b.wait()
+            for r, s in zip(single, spp):
+                r.execute_rendering(16.0, s)
+            _same(_outputs(batched), _outputs(single))
+            change(batched)
+            change(single)
+            for _ in range(2):
+                b.submit(batched, spp)
+                b.wait()
+                for r, s in zip(single, spp):
+                    r.execute_rendering(16.0, s)
+            _same(_outputs(batched), _outputs(single))
+    finally:
+        for r in batched + single:
+            r.shutdown()
