@@ -511,7 +511,7 @@ __device__ __forceinline__ void sky_jacobians(const FrameParams& F, const float4
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = q[2 * (size_t)i], b = q[2 * (size_t)i + 1];
         float3 J[SKY_PARAMS];
-        if (DBL) nishita_jacobian_m(P, obs, make_float3(a.x, a.y, a.z), J);
+        if (DBL) nishita_jacobian_s(P, obs, make_float3(a.x, a.y, a.z), J);
         else nishita_grad(P, obs, make_float3(a.x, a.y, a.z), J);
         const float3 w = make_float3(b.x, b.y, b.z);
         for (int k = 0; k < SKY_PARAMS; ++k) gsky[k] += wdot(w, J[k]);

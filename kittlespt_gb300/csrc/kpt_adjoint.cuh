@@ -454,6 +454,98 @@ static __device__ __noinline__ void nishita_jacobian_m(const SkyParams& P, float
     for (int i = 0; i < SKY_PARAMS; ++i) J[i] = make_float3((float)j[i][0], (float)j[i][1], (float)j[i][2]);
 }
 
+// nishita_jacobian_d in single precision, with the geometry rewritten so
+// that nothing cancels: the altitude of o + s d is h / (sqrt(R^2 + h) + R)
+// with h = |o + s d|^2 - R^2 = (|o|^2 - R^2) + s (2 o.d + s d.d) formed from
+// small terms (|o|^2 - R^2 = o.x^2 + o.z^2 + (o.y - R)(o.y + R)), likewise
+// along the sun ray from each view sample, and the far root of each sphere
+// intersection in its stable form; sample positions are tmin + (i + 1/2)
+// step, not a running sum.  The altitudes are then good to ~1e-2 m (one
+// float ulp of a 6.4e6 m vector is 0.5 m), and the Rayleigh derivatives'
+// near-cancellation at the sun (terms ~30x the result) keeps ~1e-5 of the
+// result; the float and FP64 pipes differ ~60x in rate on this part.
+__device__ __forceinline__ float sphere_exit_s(float b, float a, float c) {   // far root of a t^2 + 2 b t + c
+    const float disc = b * b - a * c;
+    if (disc < 0.0f) return -1.0f;
+    const float sq = sqrtf(disc);
+    return b >= 0.0f ? -c / (b + sq) : (sq - b) / a;
+}
+static __device__ __noinline__ void nishita_jacobian_s(const SkyParams& P, float3 o, float3 d, float3* J) {
+    for (int i = 0; i < SKY_PARAMS; ++i) J[i] = make_float3(0.0f, 0.0f, 0.0f);
+    const float3 sun = P.sun_dir;
+    const float R = P.earth_r, A = P.atm_r;
+    const float dA = (A - R) * (A + R);                                   // A^2 - R^2
+    const float h0 = o.x * o.x + o.z * o.z + (o.y - R) * (o.y + R);       // |o|^2 - R^2
+    const float dd = dot(d, d), od = dot(o, d), ss = dot(sun, sun), osun = dot(o, sun), dsun = dot(d, sun);
+    const float tmax = sphere_exit_s(od, dd, h0 - dA);
+    if (!(tmax >= 0.0f)) return;
+    const float disc0 = od * od - dd * (h0 - dA);
+    const float te = (-od - sqrtf(fmaxf(disc0, 0.0f))) / dd;
+    const float tmin = te > 0.0f ? te : 0.0f;
+    const float sR[3] = {P.sigma_r.x, P.sigma_r.y, P.sigma_r.z}, sM = P.sigma_m, tM = P.sigma_m + P.sigma_am;
+    const float hr = P.h_r, hm = P.h_m, ihr2 = 1.0f / (hr * hr), ihm2 = 1.0f / (hm * hm);
+    const float step = (tmax - tmin) / 16.0f;
+    const float R2 = R * R;
+    float oR = 0.0f, oM = 0.0f, doR = 0.0f, doM = 0.0f;
+    float iR[3] = {0, 0, 0}, iM[3] = {0, 0, 0}, diR[4][3] = {}, diM[4][3] = {};
+    for (int i = 0; i < 16; ++i) {
+        const float s = tmin + ((float)i + 0.5f) * step;
+        const float h = h0 + s * (2.0f * od + s * dd);
+        const float alt = h / (sqrtf(R2 + h) + R);
+        const float pR = expf(-alt / hr) * step, pM = expf(-alt / hm) * step;
+        const float dpR = pR * alt * ihr2, dpM = pM * alt * ihm2;
+        oR += pR;
+        oM += pM;
+        doR += dpR;
+        doM += dpM;
+        const float b = osun + s * dsun;                                  // (o + s d) . sun
+        const float ltx = sphere_exit_s(b, ss, h - dA);
+        const float lstep = ltx / 8.0f;
+        float lR = 0.0f, lM = 0.0f, dlR = 0.0f, dlM = 0.0f;
+        int j;
+        for (j = 0; j < 8; ++j) {
+            const float ls = ((float)j + 0.5f) * lstep;
+            const float hl = h + ls * (2.0f * b + ls * ss);
+            const float altl = hl / (sqrtf(R2 + hl) + R);
+            if (altl < 0.0f) break;
+            const float eR = expf(-altl / hr) * lstep, eM = expf(-altl / hm) * lstep;
+            lR += eR;
+            lM += eM;
+            dlR += eR * altl * ihr2;
+            dlM += eM * altl * ihm2;
+        }
+        if (j == 8) {
+            const float sr = oR + lR, sm = oM + lM, dsr = doR + dlR, dsm = doM + dlM;
+            for (int c = 0; c < 3; ++c) {
+                const float Tr = expf(-(sR[c] * sr + tM * sm));
+                iR[c] += Tr * pR;
+                iM[c] += Tr * pM;
+                const float dtau[4] = {sr, sm, sR[c] * dsr, tM * dsm};
+                for (int k = 0; k < 4; ++k) {
+                    const float dTr = Tr == 0.0f ? 0.0f : -Tr * dtau[k];
+                    diR[k][c] += dTr * pR;
+                    diM[k][c] += dTr * pM;
+                }
+                diR[2][c] += Tr * dpR;
+                diM[3][c] += Tr * dpM;
+            }
+        }
+    }
+    const float mu = dot(d, sun);
+    const float rp = 3.0f * (1.0f + mu * mu) / (16.0f * 3.14159265f);
+    const float g = 0.76f;
+    const float den = (8.0f * 3.14159265f) * ((2.0f + g * g) * powf(1.0f + g * g - 2.0f * g * mu, 1.5f));
+    const float mp = 3.0f * ((1.0f - g * g) * (1.0f + mu * mu)) / den;
+    const float K = 6.0e5f * P.sun_emission;
+    for (int c = 0; c < 3; ++c) {
+        float* jr = &J[SKY_RAYLEIGH_R + c].x;
+        jr[c] = ((iR[c] + sR[c] * diR[0][c]) * rp + sM * diM[0][c] * mp) * K;
+        (&J[SKY_MIE].x)[c] = (sR[c] * diR[1][c] * rp + (iM[c] + sM * diM[1][c]) * mp) * K;
+        (&J[SKY_RAYLEIGH_H].x)[c] = (sR[c] * diR[2][c] * rp + sM * diM[2][c] * mp) * K;
+        (&J[SKY_MIE_H].x)[c] = (sR[c] * diR[3][c] * rp + sM * diM[3][c] * mp) * K;
+    }
+}
+
 // nishita() with its derivatives: J[i] = dL/d(parameter i), i < SKY_PARAMS.
 static __device__ __noinline__ float3 nishita_grad(const SkyParams& P, float3 o, float3 d, float3* J) {
     for (int i = 0; i < SKY_PARAMS; ++i) J[i] = make_float3(0.0f, 0.0f, 0.0f);
