@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_rec(FrameParams F, AdjPa
 
 __device__ __forceinline__ float3 xyz3(float4 v) { return make_float3(v.x, v.y, v.z); }
 
-__global__ void __launch_bounds__(PATH_BLOCK) k_adj_shade(FrameParams F, AdjParams A, int level, long long wave0) {
+__global__ void __launch_bounds__(PATH_BLOCK, 6) k_adj_shade(FrameParams F, AdjParams A, int level, long long wave0) {
     constexpr int MV = ADJ_MAX_VERTICES;
     const SceneView& s = F.scene;
     const SkyParams& P = F.sky;
@@ -853,7 +853,9 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sky(FrameParams F, AdjParams
 
 // Every sample of the wave: its radiance from the vertex records (the
 // forward's sum), clamp, image, and the reverse sweep into the gradients.
-__global__ void __launch_bounds__(PATH_BLOCK) k_adj_sweep(FrameParams F, AdjParams A, long long wave0) {
+// the sweep and the vertex replay are held to 128 and 85 registers: left to
+// 193 and 110 they keep 8 and 16 warps per SM on latency-bound loads
+__global__ void __launch_bounds__(PATH_BLOCK, 4) k_adj_sweep(FrameParams F, AdjParams A, long long wave0) {
     extern __shared__ double sg[];
     const int ng = 4 * A.nmat + ADJ_SKY_PARAMS;
     grad_begin(sg, ng);
