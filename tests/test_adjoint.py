@@ -39,14 +39,14 @@ def test_adjoint_api_errors_without_context():
     assert L.kpt_adjoint_record_size() == 192
 
 
-def _scene(seed=3):
+def _scene(seed=3, width=W, height=H, spp=SPP):
     """The sphere-pair scene with random materials and a 400 x 400 ground, so
     that no path leaves the scene below the horizon: there the reference's
     single-precision sky march (the earth's interior on the view ray) is off
     from its exact value by up to ~1%, and the FP64 comparison would measure
     that instead of the adjoint."""
     from kittlespt_gb300 import scenes as S
-    sc = S.scene_small(W, H, SPP, DEPTH)
+    sc = S.scene_small(width, height, spp, DEPTH)
     sc.meshes[1] = S.quad(400.0, 400.0, 0.0, True, 2)
     rng = np.random.Generator(np.random.PCG64(seed))
     mats = sc.materials.copy()
@@ -181,6 +181,32 @@ def test_adjoint_matches_fp64_oracle_fd():
         r.shutdown()
 
 
+@pytest.mark.gpu
+def test_adjoint_matches_fp64_oracle_fd_at_workload_spp():
+    """The same check with the differentiation workload's 32 samples per
+    pixel and depth 6 (on 128x96 pixels instead of 512x512): 393,216 paths
+    replayed, their frozen records re-evaluated in double by the oracle, all
+    18 parameters within 1e-3 of its central differences."""
+    from kittlespt_gb300.renderer import adjoint_param_names
+    w, h, spp = 128, 96, 32
+    sc = _scene(5, w, h, spp)
+    r = _renderer(sc)
+    try:
+        theta = _theta(sc)
+        nmat = len(sc.materials)
+        rng = np.random.Generator(np.random.PCG64(13))
+        adj = np.zeros((h, w, 4), np.float32)
+        adj[..., :3] = rng.uniform(-1.0, 1.0, (h, w, 3))
+        adj *= _hit_mask(r, w, h)[..., None]
+        grad, records, n = _records(r, adj, 0, spp, max_rec=1 << 22)
+        assert np.isfinite(grad).all() and np.abs(grad).max() > 0
+        print(f"{w}x{h}x{spp}: {n} vertex records")
+        fd, _ = _oracle_fd(records, n, theta, nmat, _fixed(sc))
+        _compare(grad, fd, theta, adjoint_param_names(nmat))
+    finally:
+        r.shutdown()
+
+
 def _above_horizon(sc, min_elevation=0.05):
     """1 for pixels whose camera ray rises more than min_elevation (y
     component) above the horizon: near the horizon the reference's
@@ -198,11 +224,11 @@ def _above_horizon(sc, min_elevation=0.05):
     return (w[..., 1] > min_elevation).astype(np.float32)
 
 
-def _hit_mask(r):
+def _hit_mask(r, width=W, height=H):
     """1 where the pixel's camera ray hits the scene."""
     import torch
-    buf = torch.zeros((1, H, W, 4), dtype=torch.float32, device="cuda")
-    fh = torch.zeros((H, W, 4), dtype=torch.int32, device="cuda")
+    buf = torch.zeros((1, height, width, 4), dtype=torch.float32, device="cuda")
+    fh = torch.zeros((height, width, 4), dtype=torch.int32, device="cuda")
     r.render_samples_device(0, 1, buf.data_ptr(), fh.data_ptr())
     r.synchronize()
     return (fh[..., 0] >= 0).cpu().numpy().astype(np.float32)
