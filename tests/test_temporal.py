@@ -198,3 +198,31 @@ def test_temporal_sequence_matches_reference_gpu(arith):
     finally:
         r.shutdown()
         g.close()
+
+
+def test_temporal_settings_and_history_errors():
+    """temporal_arith takes 0 or 1; the history readback needs a frame
+    rendered with temporal accumulation; the history's alpha counts the
+    blended frames (a still camera: one per sample up to 16)."""
+    from kittlespt_gb300 import _lib as K
+    from kittlespt_gb300.renderer import Renderer
+    sc = S.scene_small(32, 24, 1, 2)
+    r = Renderer(0)
+    r.initialize()
+    try:
+        r.load_scene(sc)
+        assert r.get_renderer_settings().temporal_arith == 0   # the scene's (oracle) arithmetic
+        with pytest.raises(K.KptError):
+            r.set_renderer_settings(temporal_arith=2)
+        with pytest.raises(K.KptError):
+            r.read_history()                       # no temporal frame yet
+        r.set_renderer_settings(temporal_accumulation=1, temporal_arith=1)
+        r.execute_rendering(16.0, 3)
+        r.synchronize()
+        hist = r.read_history()
+        assert hist.shape == (24, 32, 4)
+        # camera hits carry 2 blended frames after 3 samples; sky pixels none
+        assert set(np.unique(hist[..., 3]).tolist()) <= {0.0, 2.0}
+        assert (hist[..., 3] == 2.0).any()
+    finally:
+        r.shutdown()
