@@ -585,9 +585,10 @@ def adjoint_scene(seed=7):
 
 def adjoint_rate(steps, warmup, check_sky=True):
     """Gradient evaluations per second of the L2 image loss on the
-    differentiation workload: forward image (mean of 32 samples per pixel),
-    the loss's adjoint image and the path-replay adjoint, all on the device
-    (CUDA events on the library's stream), from an initial guess within +-20%
+    differentiation workload: the split path-replay adjoint's forward half
+    (one replay of 32 samples per pixel that keeps its records and gives the
+    image), the loss's adjoint image, the backward half (the sweep of the
+    records), all on the device (CUDA events on the library's stream), from an initial guess within +-20%
     of the parameters that rendered the target (target samples: seed 7, i.e.
     sample indices 7*32 .. 7*32+31).  With check_sky, the adjoint's
     derivatives for the six sky parameters -- which no sampling decision
@@ -638,34 +639,48 @@ def adjoint_rate(steps, warmup, check_sky=True):
         target = buf.mean(dim=0).clone()
         apply(theta0)
         adj = torch.zeros((ADJ_H, ADJ_W, 4), dtype=torch.float32, device="cuda")
+        img = torch.zeros((ADJ_H, ADJ_W, 4), dtype=torch.float32, device="cuda")
 
         def gradient():
-            r.render_samples_device(0, ADJ_SPP, buf.data_ptr())
-            img = buf.mean(dim=0)
+            # the split adjoint: one replay that keeps its records and gives
+            # the image, the loss's adjoint image, the sweep of the records
+            r.adjoint_forward_device(0, ADJ_SPP, img.data_ptr())
             adj[..., :3] = 2.0 * (img[..., :3] - target[..., :3])
-            K.check(r._L.kpt_adjoint_device(r.ctx, 0, ADJ_SPP, adj.data_ptr(), grad.data_ptr(), None))
-            return img
+            r.adjoint_backward_device(adj.data_ptr(), grad.data_ptr())
 
         for _ in range(warmup):
             gradient()
         torch.cuda.synchronize()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
         ev[0].record(stream)
         for _ in range(steps):
-            img = gradient()
+            gradient()
         ev[1].record(stream)
-        K.check(r._L.kpt_adjoint_device(r.ctx, 0, ADJ_SPP, adj.data_ptr(), grad.data_ptr(), None))
+        r.adjoint_forward_device(0, ADJ_SPP, img.data_ptr())
         ev[2].record(stream)
+        adj[..., :3] = 2.0 * (img[..., :3] - target[..., :3])
+        ev[3].record(stream)
+        r.adjoint_backward_device(adj.data_ptr(), grad.data_ptr())
+        ev[4].record(stream)
+        # the one-call adjoint (a second replay of the forward renderer's samples) for comparison
+        g_one = torch.zeros_like(grad)
+        K.check(r._L.kpt_adjoint_device(r.ctx, 0, ADJ_SPP, adj.data_ptr(), g_one.data_ptr(), None))
+        ev[5].record(stream)
         torch.cuda.synchronize()
     ms = ev[0].elapsed_time(ev[1]) / steps
-    adj_ms = ev[1].elapsed_time(ev[2])
+    fwd_ms, loss_ms, bwd_ms, one_ms = (ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3]),
+                                       ev[3].elapsed_time(ev[4]), ev[4].elapsed_time(ev[5]))
     loss = float(((img[..., :3].double() - target[..., :3].double()) ** 2).sum())
     g = grad.cpu().numpy()
-    out = {"value": 1e3 / ms, "unit": "gradient evaluations/s", "ms_per_gradient": ms, "adjoint_ms": adj_ms,
-           "forward_and_loss_ms": ms - adj_ms, "parameters": int(n.value),
+    gone = g_one.cpu().numpy()
+    out = {"value": 1e3 / ms, "unit": "gradient evaluations/s", "ms_per_gradient": ms,
+           "forward_replay_ms": fwd_ms, "loss_ms": loss_ms, "backward_ms": bwd_ms,
+           "one_call_adjoint_ms": one_ms,
+           "split_vs_one_call_max_rel_diff": float(np.max(np.abs(g - gone) / np.maximum(np.abs(gone), 1e-300))),
+           "parameters": int(n.value),
            "config": {"workload": "adjoint_sphere_pair_512_32spp_depth6", "width": ADJ_W, "height": ADJ_H,
                       "spp": ADJ_SPP, "max_depth": ADJ_DEPTH, "samples_per_gradient": ADJ_W * ADJ_H * ADJ_SPP},
-           "Msamples_per_s_replayed": ADJ_W * ADJ_H * ADJ_SPP / adj_ms / 1e3,
+           "Msamples_per_s_replayed": ADJ_W * ADJ_H * ADJ_SPP / fwd_ms / 1e3,
            "loss": loss, "grad_norm": float(np.linalg.norm(g * np.abs(theta0)))}
     if check_sky:
         def loss_at(theta):
@@ -702,7 +717,9 @@ def run_adjoint(args):
            "ms_per_step": a["ms_per_gradient"], "higher_is_better": True, "dtype": "f32",
            "data": "synthetic (seeded sphere-pair scene with random materials)",
            "config": dict(a["config"], parameters=a["parameters"]),
-           "adjoint_ms": a["adjoint_ms"], "forward_and_loss_ms": a["forward_and_loss_ms"],
+           "forward_replay_ms": a["forward_replay_ms"], "loss_ms": a["loss_ms"], "backward_ms": a["backward_ms"],
+           "one_call_adjoint_ms": a["one_call_adjoint_ms"],
+           "split_vs_one_call_max_rel_diff": a["split_vs_one_call_max_rel_diff"],
            "Msamples_per_s_replayed": a["Msamples_per_s_replayed"], "loss": a["loss"], "grad_norm": a["grad_norm"],
            "max_rel_err_sky": a.get("max_rel_err_sky"), "accuracy_check": a.get("accuracy_check")}
     print(json.dumps(out))

@@ -417,6 +417,21 @@ kpt_status kpt_adjoint_param_count(kpt_context* ctx, int* n);
 kpt_status kpt_adjoint_device(kpt_context* ctx, int sample0, int nsamples, const float* adjoint, double* grad,
                               float* image);
 kpt_status kpt_adjoint(kpt_context* ctx, int sample0, int nsamples, const float* adjoint, double* grad, float* image);
+/* The same adjoint in two calls, for a caller whose loss needs the image
+ * first (an optimisation step): kpt_adjoint_forward_device replays the
+ * samples once, keeps every path's records and writes the image the
+ * gradient belongs to (image, device, [H][W] RGBA float); after the caller
+ * has formed dLoss/dimage, kpt_adjoint_backward_device sweeps the kept
+ * records -- no ray is traced twice -- and writes the gradient (device
+ * doubles).  Both enqueue on the context's stream and do not synchronise.
+ * The records of all W*H*nsamples samples must fit one replay wave (12 GiB,
+ * and at most 2^25 samples): otherwise KPT_ERR_INVALID (kpt_adjoint_device
+ * has no such limit).  The backward call needs the forward call's records
+ * and state: after any frame, adjoint call, scene, material, environment,
+ * settings, camera or resolution change in between it returns
+ * KPT_ERR_STATE; each forward call allows one backward call. */
+kpt_status kpt_adjoint_forward_device(kpt_context* ctx, int sample0, int nsamples, float* image);
+kpt_status kpt_adjoint_backward_device(kpt_context* ctx, const float* adjoint, double* grad);
 
 /* Test support for the adjoint's FP64 oracle: as kpt_adjoint_device, and
  * also writes every path vertex the replay visited -- all its fixed quantities

@@ -146,6 +146,8 @@ SIGNATURES = {
     "kpt_adjoint_param_count": (_S, [_P, C.POINTER(C.c_int)]),
     "kpt_adjoint_device": (_S, [_P, C.c_int, C.c_int, _P, _P, _P]),
     "kpt_adjoint": (_S, [_P, C.c_int, C.c_int, _F, C.POINTER(C.c_double), _F]),
+    "kpt_adjoint_forward_device": (_S, [_P, C.c_int, C.c_int, _P]),
+    "kpt_adjoint_backward_device": (_S, [_P, _P, _P]),
     "kpt_adjoint_record_size": (C.c_int, []),
     "kpt_sky_grad_device": (_S, [_P, C.c_int, _P, _P]),
     "kpt_adjoint_records_device": (_S, [_P, C.c_int, C.c_int, _P, _P, _P, C.c_int, C.POINTER(C.c_int)]),

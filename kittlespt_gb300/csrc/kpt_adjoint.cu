@@ -40,6 +40,7 @@ __device__ __forceinline__ void grad_begin(double* sg, int n) {
 }
 __device__ __forceinline__ void grad_end(const double* sg, int n, double* out) {
     __syncthreads();
+    if (!out) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         if (sg[i] != 0.0) atomicAdd(out + i, sg[i]);
 }
@@ -141,6 +142,8 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjP
         float3 L = nishita_grad(P, obs, r.d, J) * ls;
         float3 m;
         float3 Lc = make_float3(clamp_out(L.x, &m.x), clamp_out(L.y, &m.y), clamp_out(L.z, &m.z));
+        if (A.image) A.image[p] = make_float4(Lc.x, Lc.y, Lc.z, 0.0f);
+        if (!A.adjoint) continue;   // the forward half of a split adjoint: the image only
         const float4 a = A.adjoint[p];
         const float3 g = make_float3(a.x, a.y, a.z) * m * ls;   // mean over identical samples
         bool done = false;
@@ -150,7 +153,6 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adjoint_miss(FrameParams F, AdjP
         }
         if (!done)
             for (int k = 0; k < SKY_PARAMS; ++k) acc.add(4 * A.nmat + k, wdot(g, J[k]));
-        if (A.image) A.image[p] = make_float4(Lc.x, Lc.y, Lc.z, 0.0f);
     }
     grad_end(sg, ng, A.grad);
 }
@@ -900,13 +902,14 @@ __global__ void __launch_bounds__(PATH_BLOCK, 4) k_adj_sweep(FrameParams F, AdjP
         if (escaped) L = L + b_end * s_end;
         float3 msk;
         const float3 Lc = make_float3(clamp_out(L.x, &msk.x), clamp_out(L.y, &msk.y), clamp_out(L.z, &msk.z));
-        const float4 a = A.adjoint[p];
-        const float3 g = make_float3(a.x, a.y, a.z) * msk * inv_n;
         if (A.image) {
             atomicAdd(&A.image[p].x, Lc.x * inv_n);
             atomicAdd(&A.image[p].y, Lc.y * inv_n);
             atomicAdd(&A.image[p].z, Lc.z * inv_n);
         }
+        if (!A.adjoint) continue;   // the forward half of a split adjoint: the image only
+        const float4 a = A.adjoint[p];
+        const float3 g = make_float3(a.x, a.y, a.z) * msk * inv_n;
         if (!nonzero(g)) continue;
         float3 R = escaped ? s_end : make_float3(0.0f, 0.0f, 0.0f);
         if (escaped) {
@@ -953,6 +956,7 @@ __global__ void __launch_bounds__(PATH_BLOCK, 4) k_adj_sweep(FrameParams F, AdjP
             R = ck + xyz3(A.vr[o * AV_FIELDS + AV_W]) * R;
         }
     }
+    if (!A.adjoint) return;   // uniform over the block: the image only, no gradient
     for (int q = 0; q < SKY_PARAMS; ++q) {   // one shared add per warp per sky parameter
         const float3 J = A.sun_J[q];
         double v = gsky[q] + cs0 * J.x + cs1 * J.y + cs2 * J.z;

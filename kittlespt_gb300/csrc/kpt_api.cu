@@ -169,6 +169,19 @@ struct kpt_context {
     DBuf<float4> adj_skyqf;     // deferred single-precision sky Jacobians
     DBuf<int> adj_skyqf_count;
     DBuf<float4> adj_vr, adj_vend, adj_vsky;   // the wavefront replay's vertex and end records, escape skies
+    // the records kept by kpt_adjoint_forward_device for the backward call,
+    // and the state they were replayed in
+    struct AdjForward {
+        bool valid = false;
+        FrameParams F;
+        AdjParams A;
+        unsigned long long version = 0;
+        std::vector<kpt_material> materials;
+        kpt_environment env;
+        kpt_settings settings;
+        float inv_proj[16], inv_view[16];
+        int W = 0, H = 0;
+    } adj_fwd;
     DBuf<int> adj_esc;                          // the wavefront replay's escaped paths, then their count
     DBuf<unsigned char> adj_vis;     // the wavefront replay's light-sample visibility
     DBuf<float4> pixel_sky, radiance, sky_queue;
@@ -1300,6 +1313,7 @@ static void columns_of(const float* cm, float4* cols) {
 }
 
 static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
+    if (c) c->adj_fwd.valid = false;   // a frame reuses the wave buffers the kept records refer to
     kpt_status st = ready(c);
     if (st != KPT_OK) return st;
     if (spp <= 0) return fail(KPT_ERR_INVALID, "spp must be positive");
@@ -1726,6 +1740,7 @@ static int adjoint_params(const kpt_context* c) { return 4 * (int)c->materials.s
 
 static kpt_status adjoint_run(kpt_context* c, int sample0, int nsamples, const float* adjoint, double* grad,
                               float* image, AdjRec* rec, int max_rec) {
+    c->adj_fwd.valid = false;
     kpt_status st = ready(c);
     if (st != KPT_OK) return st;
     if (nsamples <= 0 || sample0 < 0 || !adjoint || !grad)
@@ -1860,6 +1875,151 @@ kpt_status kpt_adjoint_device(kpt_context* c, int sample0, int nsamples, const f
                               float* image) {
     if (!c) return fail(KPT_ERR_INVALID, "null context");
     return adjoint_run(c, sample0, nsamples, adjoint, grad, image, nullptr, 0);
+}
+
+// The split adjoint: the replay of every sample in one wave, its records
+// kept, and the image the gradient belongs to (forward); then the sweep of
+// the kept records with dLoss/dimage and the deferred sky Jacobians
+// (backward) -- the rays are traced once per gradient evaluation.
+kpt_status kpt_adjoint_forward_device(kpt_context* c, int sample0, int nsamples, float* image) {
+    if (!c) return fail(KPT_ERR_INVALID, "null context");
+    c->adj_fwd.valid = false;
+    kpt_status st = ready(c);
+    if (st != KPT_OK) return st;
+    if (nsamples <= 0 || sample0 < 0 || !image) return fail(KPT_ERR_INVALID, "kpt_adjoint_forward_device: bad arguments");
+    if (c->settings.max_depth + 1 > ADJ_MAX_VERTICES)
+        return fail(KPT_ERR_INVALID, "kpt_adjoint_forward_device: max_depth above 16");
+    const int ng = adjoint_params(c);
+    const size_t smem = sizeof(double) * (size_t)ng;
+    if (smem > 200 * 1024) return fail(KPT_ERR_INVALID, "kpt_adjoint_forward_device: too many materials");
+    st = ensure_work(c, nsamples);
+    if (st != KPT_OK) return st;
+    const int np = c->W * c->H;
+    const long long items = (long long)np * nsamples;
+    FrameParams F = frame_params(c, sample0, nsamples);
+    F.sky = sky_params(c->env);   // IEEE sky arithmetic, as the replay's Jacobians
+    const int D = F.max_depth;
+    const size_t per_path = sizeof(float4) * ((size_t)AV_FIELDS * (D + 1) + 2) + (size_t)(D + 1);
+    if (items > F.cap || (size_t)items * per_path > ADJ_WAVE_BYTES)
+        return fail(KPT_ERR_INVALID, "kpt_adjoint_forward_device: the samples' records exceed one replay wave "
+                                     "(use kpt_adjoint_device)");
+    F.cap = (int)items;
+    const size_t qcap = (size_t)np * ((size_t)nsamples + 1);
+    KPT_CUDA(c->sun_J.ensure(ADJ_SKY_PARAMS));
+    KPT_CUDA(c->rec_count.ensure(1));
+    KPT_CUDA(c->adj_vr.ensure((size_t)AV_FIELDS * (D + 1) * F.cap));
+    KPT_CUDA(c->adj_vend.ensure(2 * (size_t)F.cap));
+    KPT_CUDA(c->adj_vsky.ensure((size_t)F.cap));
+    KPT_CUDA(c->adj_esc.ensure((size_t)F.cap + 1));
+    KPT_CUDA(c->adj_vis.ensure((size_t)(D + 1) * F.cap));
+    KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
+    KPT_CUDA(c->adj_skyq_count.ensure(1));
+    KPT_CUDA(c->adj_skyqf.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
+    KPT_CUDA(c->adj_skyqf_count.ensure(1));
+    AdjParams A{};
+    A.image = reinterpret_cast<float4*>(image);
+    A.sun_J = c->sun_J.p;
+    A.rec_count = c->rec_count.p;
+    A.nmat = (int)c->materials.size();
+    A.skyq = c->adj_skyq.p;
+    A.skyq_count = c->adj_skyq_count.p;
+    A.skyq_cap = (int)(c->adj_skyq.n / 2);
+    A.skyqf = c->adj_skyqf.p;
+    A.skyqf_count = c->adj_skyqf_count.p;
+    A.skyqf_cap = (int)(c->adj_skyqf.n / 2);
+    A.vr = c->adj_vr.p;
+    A.vend = c->adj_vend.p;
+    A.vsky = c->adj_vsky.p;
+    A.esc = c->adj_esc.p;
+    A.esc_count = c->adj_esc.p + F.cap;
+    A.vis = c->adj_vis.p;
+    cudaStream_t s = c->stream;
+    KPT_CUDA(cudaMemsetAsync(image, 0, sizeof(float4) * (size_t)np, s));
+    KPT_CUDA(cudaMemsetAsync(c->counts.p, 0, 4 * sizeof(int), s));
+    KPT_CUDA(cudaMemsetAsync(c->level_counts.p, 0, sizeof(int) * LEVEL_WORDS * (size_t)(D + 2), s));
+    KPT_CUDA(cudaMemsetAsync(A.vis, 0, (size_t)(D + 1) * F.cap, s));
+    KPT_CUDA(cudaMemsetAsync(A.esc_count, 0, sizeof(int), s));
+    for (const void* k : {(const void*)k_adj_sweep, (const void*)k_adjoint_miss})
+        KPT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    KPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_sweep, PATH_BLOCK, smem));
+    const int grid = std::max(1, per_sm) * c->sm_count;
+    const int g_ext = persistent_grid(c, (const void*)k_extend, TRACE_BLOCK);
+    const int g_shd = persistent_grid(c, (const void*)k_adj_shadow, TRACE_BLOCK);
+    const int g_vtx = persistent_grid(c, (const void*)k_adj_shade, PATH_BLOCK);
+    c->levels_depth = D;
+    k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
+    k_primary<<<primary_blocks(c->W, c->H), PATH_BLOCK, 0, s>>>(F);
+    k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);   // the missing pixels' image
+    for (int l = 0; l <= D; ++l) {
+        if (l > 0) k_extend<<<g_ext, TRACE_BLOCK, 0, s>>>(F, l);
+        k_adj_shade<<<g_vtx, PATH_BLOCK, 0, s>>>(F, A, l, 0);
+        k_adj_shadow<<<g_shd, TRACE_BLOCK, 0, s>>>(F, A, l);
+    }
+    k_adj_sky<<<g_vtx, PATH_BLOCK, 0, s>>>(F, A, 0);
+    k_adj_sweep<<<grid, PATH_BLOCK, smem, s>>>(F, A, 0);   // the hit pixels' image
+    c->launches += 6 + 3 * D;
+    KPT_CUDA(cudaGetLastError());
+    kpt_context::AdjForward& K = c->adj_fwd;
+    K.F = F;
+    K.A = A;
+    K.A.image = nullptr;
+    K.version = c->scene_version;
+    K.materials = c->materials;
+    K.env = c->env;
+    K.settings = c->settings;
+    std::memcpy(K.inv_proj, c->inv_proj, sizeof K.inv_proj);
+    std::memcpy(K.inv_view, c->inv_view, sizeof K.inv_view);
+    K.W = c->W;
+    K.H = c->H;
+    K.valid = true;
+    return KPT_OK;
+}
+
+kpt_status kpt_adjoint_backward_device(kpt_context* c, const float* adjoint, double* grad) {
+    if (!c || !adjoint || !grad) return fail(KPT_ERR_INVALID, "kpt_adjoint_backward_device: null argument");
+    KPT_CUDA(cudaSetDevice(c->device));
+    kpt_context::AdjForward& K = c->adj_fwd;
+    const bool same = K.valid && K.version == c->scene_version && K.materials.size() == c->materials.size() &&
+                      std::memcmp(K.materials.data(), c->materials.data(), sizeof(kpt_material) * K.materials.size()) == 0 &&
+                      std::memcmp(&K.env, &c->env, sizeof K.env) == 0 &&
+                      std::memcmp(&K.settings, &c->settings, sizeof K.settings) == 0 &&
+                      std::memcmp(K.inv_proj, c->inv_proj, sizeof K.inv_proj) == 0 &&
+                      std::memcmp(K.inv_view, c->inv_view, sizeof K.inv_view) == 0 && K.W == c->W && K.H == c->H;
+    if (!same)
+        return fail(KPT_ERR_STATE, "kpt_adjoint_backward_device: no kept forward records for the current scene "
+                                   "(call kpt_adjoint_forward_device first, with nothing rendered or changed between)");
+    K.valid = false;   // one backward per forward: the sky queues and the gradient start from zero
+    const FrameParams& F = K.F;
+    AdjParams A = K.A;
+    A.adjoint = reinterpret_cast<const float4*>(adjoint);
+    A.grad = grad;
+    const int ng = adjoint_params(c);
+    const size_t smem = sizeof(double) * (size_t)ng;
+    int per_sm = 0;
+    KPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_sweep, PATH_BLOCK, smem));
+    const int grid = std::max(1, per_sm) * c->sm_count;
+    cudaStream_t s = c->stream;
+    KPT_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * ng, s));
+    KPT_CUDA(cudaMemsetAsync(A.skyq_count, 0, sizeof(int), s));
+    KPT_CUDA(cudaMemsetAsync(A.skyqf_count, 0, sizeof(int), s));
+    // the sun's double-precision Jacobian (one thread) beside the missing pixels
+    KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
+    KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
+    k_adjoint_constants<<<1, 32, 0, c->side>>>(F, A);
+    KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
+    k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);
+    KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
+    k_adj_sweep<<<grid, PATH_BLOCK, smem, s>>>(F, A, 0);
+    KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
+    KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
+    k_adjoint_sky_f<<<c->sm_count * 4, PATH_BLOCK, 0, c->side>>>(F, A);
+    KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
+    k_adjoint_sky_d<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
+    KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
+    c->launches += 5;
+    KPT_CUDA(cudaGetLastError());
+    return KPT_OK;
 }
 
 kpt_status kpt_adjoint(kpt_context* c, int sample0, int nsamples, const float* adjoint, double* grad, float* image) {

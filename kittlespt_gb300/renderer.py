@@ -360,6 +360,16 @@ class Renderer:
                                     K.fptr(img.reshape(-1)) if want_image else None))
         return g, img
 
+    def adjoint_forward_device(self, sample0: int, nsamples: int, image_ptr: int):
+        """The split adjoint's forward half: replays the samples once, keeps
+        the records, writes the image ([H][W][4] float32, device pointer)."""
+        K.check(self._L.kpt_adjoint_forward_device(self._ctx, sample0, nsamples, image_ptr))
+
+    def adjoint_backward_device(self, adjoint_ptr: int, grad_ptr: int):
+        """The split adjoint's backward half: dLoss/dimage ([H][W][4] float32,
+        device pointer) -> gradient (float64, device pointer)."""
+        K.check(self._L.kpt_adjoint_backward_device(self._ctx, adjoint_ptr, grad_ptr))
+
     # -- launch parameters (no reference counterpart) -------------------------
     def set_tuning(self, grid_scale: float = 1.0, wave_cap: int = 0, shade_block: int = 0, sort_rays: int = 0,
                    fetch_batch: int = 0, group_lobes: int = 0):

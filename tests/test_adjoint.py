@@ -36,6 +36,8 @@ def test_adjoint_api_errors_without_context():
     n = C.c_int()
     assert L.kpt_adjoint_param_count(None, C.byref(n)) == -1
     assert L.kpt_adjoint(None, 0, 1, None, None, None) == -1
+    assert L.kpt_adjoint_forward_device(None, 0, 1, None) == -1
+    assert L.kpt_adjoint_backward_device(None, None, None) == -1
     assert L.kpt_adjoint_record_size() == 192
 
 
@@ -394,5 +396,47 @@ def test_sky_gradient_matches_fp64_fd():
             scale = np.abs(fd * sky[k]).max()
             err = np.abs((J - fd) * sky[k])
             assert err.max() <= 1e-3 * scale, (k, err.max() / scale)
+    finally:
+        r.shutdown()
+
+
+@pytest.mark.gpu
+def test_split_adjoint_matches_one_call():
+    """kpt_adjoint_forward_device + kpt_adjoint_backward_device (one replay,
+    its records kept for the sweep) against kpt_adjoint_device (replay and
+    sweep in one call): the same image and gradient up to the order of
+    their atomic sums; the backward half refuses to run without kept records
+    for the current state."""
+    import torch
+    sc = _scene()
+    r = _renderer(sc)
+    try:
+        n = C.c_int()
+        K.check(r._L.kpt_adjoint_param_count(r.ctx, C.byref(n)))
+        rng = np.random.Generator(np.random.PCG64(5))
+        adj = torch.from_numpy(rng.uniform(-1.0, 1.0, (H, W, 4)).astype(np.float32)).cuda()
+        g1 = torch.zeros(n.value, dtype=torch.float64, device="cuda")
+        g2 = torch.zeros_like(g1)
+        img1 = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        img2 = torch.zeros_like(img1)
+        K.check(r._L.kpt_adjoint_device(r.ctx, 0, SPP, adj.data_ptr(), g1.data_ptr(), img1.data_ptr()))
+        r.adjoint_forward_device(0, SPP, img2.data_ptr())
+        r.adjoint_backward_device(adj.data_ptr(), g2.data_ptr())
+        r.synchronize()
+        a, b = g1.cpu().numpy(), g2.cpu().numpy()
+        np.testing.assert_allclose(b, a, rtol=1e-9, atol=1e-12 * np.abs(a).max())
+        np.testing.assert_allclose(img2.cpu().numpy(), img1.cpu().numpy(), rtol=1e-6, atol=1e-7)
+        with pytest.raises(K.KptError):
+            r.adjoint_backward_device(adj.data_ptr(), g2.data_ptr())     # one backward per forward
+        r.adjoint_forward_device(0, SPP, img2.data_ptr())
+        r.execute_rendering(16.0, 1)
+        with pytest.raises(K.KptError):
+            r.adjoint_backward_device(adj.data_ptr(), g2.data_ptr())     # a frame in between
+        r.adjoint_forward_device(0, SPP, img2.data_ptr())
+        m = sc.materials[0].copy()
+        m["roughness"] = 0.5 * m["roughness"]
+        assert r.set_material(0, m)
+        with pytest.raises(K.KptError):
+            r.adjoint_backward_device(adj.data_ptr(), g2.data_ptr())     # a parameter changed
     finally:
         r.shutdown()

@@ -203,7 +203,7 @@ def test_temporal_sequence_matches_reference_gpu(arith):
 def test_temporal_settings_and_history_errors():
     """temporal_arith takes 0 or 1; the history readback needs a frame
     rendered with temporal accumulation; the history's alpha counts the
-    blended frames (a still camera: one per sample up to 16)."""
+    blended frames (at most one per sample)."""
     from kittlespt_gb300 import _lib as K
     from kittlespt_gb300.renderer import Renderer
     sc = S.scene_small(32, 24, 1, 2)
@@ -221,8 +221,10 @@ def test_temporal_settings_and_history_errors():
         r.synchronize()
         hist = r.read_history()
         assert hist.shape == (24, 32, 4)
-        # camera hits carry 2 blended frames after 3 samples; sky pixels none
-        assert set(np.unique(hist[..., 3]).tolist()) <= {0.0, 2.0}
-        assert (hist[..., 3] == 2.0).any()
+        # history lengths are frame counts: at most one per sample, and
+        # camera hits carry history after 3 samples; sky pixels none
+        counts = hist[..., 3]
+        assert set(np.unique(counts).tolist()) <= {0.0, 1.0, 2.0, 3.0}, np.unique(counts)
+        assert counts.max() >= 2.0
     finally:
         r.shutdown()
