@@ -1949,6 +1949,12 @@ kpt_status kpt_adjoint_forward_device(kpt_context* c, int sample0, int nsamples,
     const int g_vtx = persistent_grid(c, (const void*)k_adj_shade, PATH_BLOCK);
     c->levels_depth = D;
     k_sky_constants<<<1, 32, 0, s>>>(F, c->sun_radiance.p);
+    // the sun's double-precision Jacobian (one thread; it depends on the sky
+    // parameters only) on the side stream beside the replay, for the sweep
+    KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
+    KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
+    k_adjoint_constants<<<1, 32, 0, c->side>>>(F, A);
+    KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
     k_primary<<<primary_blocks(c->W, c->H), PATH_BLOCK, 0, s>>>(F);
     k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);   // the missing pixels' image
     for (int l = 0; l <= D; ++l) {
@@ -1958,7 +1964,8 @@ kpt_status kpt_adjoint_forward_device(kpt_context* c, int sample0, int nsamples,
     }
     k_adj_sky<<<g_vtx, PATH_BLOCK, 0, s>>>(F, A, 0);
     k_adj_sweep<<<grid, PATH_BLOCK, smem, s>>>(F, A, 0);   // the hit pixels' image
-    c->launches += 6 + 3 * D;
+    KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
+    c->launches += 7 + 3 * D;
     KPT_CUDA(cudaGetLastError());
     kpt_context::AdjForward& K = c->adj_fwd;
     K.F = F;
@@ -2003,13 +2010,8 @@ kpt_status kpt_adjoint_backward_device(kpt_context* c, const float* adjoint, dou
     KPT_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * ng, s));
     KPT_CUDA(cudaMemsetAsync(A.skyq_count, 0, sizeof(int), s));
     KPT_CUDA(cudaMemsetAsync(A.skyqf_count, 0, sizeof(int), s));
-    // the sun's double-precision Jacobian (one thread) beside the missing pixels
-    KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
-    KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
-    k_adjoint_constants<<<1, 32, 0, c->side>>>(F, A);
-    KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
+    // (the sun's Jacobian, A.sun_J, came with the forward call)
     k_adjoint_miss<<<c->sm_count, PATH_BLOCK, smem, s>>>(F, A);
-    KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
     k_adj_sweep<<<grid, PATH_BLOCK, smem, s>>>(F, A, 0);
     KPT_CUDA(cudaEventRecord(c->ev_fork[0], s));
     KPT_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork[0], 0));
@@ -2017,7 +2019,7 @@ kpt_status kpt_adjoint_backward_device(kpt_context* c, const float* adjoint, dou
     KPT_CUDA(cudaEventRecord(c->ev_join[0], c->side));
     k_adjoint_sky_d<<<c->sm_count * 4, PATH_BLOCK, 0, s>>>(F, A);
     KPT_CUDA(cudaStreamWaitEvent(s, c->ev_join[0], 0));
-    c->launches += 5;
+    c->launches += 4;
     KPT_CUDA(cudaGetLastError());
     return KPT_OK;
 }
