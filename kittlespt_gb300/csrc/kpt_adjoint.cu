@@ -892,14 +892,21 @@ __global__ void __launch_bounds__(PATH_BLOCK, 4) k_adj_sweep(FrameParams F, AdjP
             const float3 kk = xyz3(A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_K]);
             return nee == 1 ? c + fcos * sun_rad * kk.x : c + fcos * kk;
         };
+        // the path's radiance: summed over its vertices, or (the backward
+        // half of a split adjoint) as the forward half stored it
         float3 L = make_float3(0.0f, 0.0f, 0.0f);
+        if (A.lpath_ready) {
+            L = xyz3(A.lpath[i]);
+        } else {
 #pragma unroll 1
-        for (int k = 0; k < nv; ++k) {
-            bool v;
-            const float3 b = xyz3(A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_BETA]);
-            L = L + b * vertex_c(k, A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_EMIT], &v);
+            for (int k = 0; k < nv; ++k) {
+                bool v;
+                const float3 b = xyz3(A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_BETA]);
+                L = L + b * vertex_c(k, A.vr[((size_t)k * cap + i) * AV_FIELDS + AV_EMIT], &v);
+            }
+            if (escaped) L = L + b_end * s_end;
+            if (A.lpath) A.lpath[i] = make_float4(L.x, L.y, L.z, 0.0f);
         }
-        if (escaped) L = L + b_end * s_end;
         float3 msk;
         const float3 Lc = make_float3(clamp_out(L.x, &msk.x), clamp_out(L.y, &msk.y), clamp_out(L.z, &msk.z));
         if (A.image) {

@@ -169,6 +169,7 @@ struct kpt_context {
     DBuf<float4> adj_skyqf;     // deferred single-precision sky Jacobians
     DBuf<int> adj_skyqf_count;
     DBuf<float4> adj_vr, adj_vend, adj_vsky;   // the wavefront replay's vertex and end records, escape skies
+    DBuf<float4> adj_lpath;                    // the split adjoint's per-path radiance
     // the records kept by kpt_adjoint_forward_device for the backward call,
     // and the state they were replayed in
     struct AdjForward {
@@ -339,7 +340,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     c->shadow.release(); c->fetch.release();
     c->sun_J.release(); c->adj_in.release(); c->adj_image.release(); c->adj_grad.release(); c->rec_count.release();
     c->adj_skyq.release(); c->adj_skyq_count.release(); c->adj_skyqf.release(); c->adj_skyqf_count.release();
-    c->adj_vr.release(); c->adj_vend.release(); c->adj_vsky.release(); c->adj_vis.release(); c->adj_esc.release();
+    c->adj_vr.release(); c->adj_vend.release(); c->adj_vsky.release(); c->adj_lpath.release(); c->adj_vis.release(); c->adj_esc.release();
     for (auto* v : {&c->ev_fork, &c->ev_join})
         for (cudaEvent_t e : *v) cudaEventDestroy(e);
     if (c->ev_sky) cudaEventDestroy(c->ev_sky);
@@ -1912,12 +1913,15 @@ kpt_status kpt_adjoint_forward_device(kpt_context* c, int sample0, int nsamples,
     KPT_CUDA(c->adj_vsky.ensure((size_t)F.cap));
     KPT_CUDA(c->adj_esc.ensure((size_t)F.cap + 1));
     KPT_CUDA(c->adj_vis.ensure((size_t)(D + 1) * F.cap));
+    KPT_CUDA(c->adj_lpath.ensure((size_t)F.cap));
     KPT_CUDA(c->adj_skyq.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
     KPT_CUDA(c->adj_skyq_count.ensure(1));
     KPT_CUDA(c->adj_skyqf.ensure(2 * std::min<size_t>(qcap, (size_t)INT32_MAX / 2)));
     KPT_CUDA(c->adj_skyqf_count.ensure(1));
     AdjParams A{};
     A.image = reinterpret_cast<float4*>(image);
+    A.lpath = c->adj_lpath.p;
+    A.lpath_ready = 0;
     A.sun_J = c->sun_J.p;
     A.rec_count = c->rec_count.p;
     A.nmat = (int)c->materials.size();
@@ -2001,6 +2005,7 @@ kpt_status kpt_adjoint_backward_device(kpt_context* c, const float* adjoint, dou
     AdjParams A = K.A;
     A.adjoint = reinterpret_cast<const float4*>(adjoint);
     A.grad = grad;
+    A.lpath_ready = 1;
     const int ng = adjoint_params(c);
     const size_t smem = sizeof(double) * (size_t)ng;
     int per_sm = 0;

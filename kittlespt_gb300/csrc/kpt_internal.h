@@ -147,6 +147,10 @@ struct AdjParams {
     int* esc;                  // [cap] slots of the wave's escaped paths, esc_count of them
     int* esc_count;
     unsigned char* vis;
+    // the split adjoint: each path's radiance, stored by the forward half's
+    // sweep (lpath_ready 0) and read by the backward half's (1); null: summed
+    float4* lpath;
+    int lpath_ready;
 };
 
 // fields of the wavefront replay's vertex record
