@@ -588,8 +588,9 @@ def adjoint_rate(steps, warmup, check_sky=True):
     differentiation workload: the split path-replay adjoint's forward half
     (one replay of 32 samples per pixel that keeps its records and gives the
     image), the loss's adjoint image, the backward half (the sweep of the
-    records), all on the device (CUDA events on the library's stream), from an initial guess within +-20%
-    of the parameters that rendered the target (target samples: seed 7, i.e.
+    records), all on the device (CUDA events on the library's stream), from
+    an initial guess within +-20% of the parameters that rendered the target
+    (target samples: seed 7, i.e.
     sample indices 7*32 .. 7*32+31).  With check_sky, the adjoint's
     derivatives for the six sky parameters -- which no sampling decision
     depends on -- are compared with central differences (h = 1e-2 relative)
