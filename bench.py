@@ -986,6 +986,28 @@ def run_profile_case(spec, tuning=()):
     r.shutdown()
 
 
+def run_batch_case(shared):
+    """Two submissions of the 32-job batch (shared ray queues, or each job's
+    frame a branch of the graph) and nothing else: the case that ncu launch
+    lists of the batch run on."""
+    from kittlespt_gb300.renderer import Batch, Renderer
+    jobs = batch_jobs()
+    rs = []
+    for sc in jobs:
+        r = Renderer(0)
+        r.initialize()
+        r.load_scene(sc)
+        rs.append(r)
+    with Batch(0) as b:
+        b.shared = shared
+        for _ in range(2):
+            b.submit(rs, [sc.spp for sc in jobs])
+            _, ms = b.wait()
+    print(f"batch case ({'shared queues' if shared else 'branches'}): {ms:.2f} ms", file=sys.stderr)
+    for r in rs:
+        r.shutdown()
+
+
 def run_adjoint_case(spec):
     """Two adjoint evaluations of the differentiation scene at a reduced size
     ("WxHxSPP") with a random adjoint image: the small case that ncu captures
@@ -1039,7 +1061,12 @@ def main():
     ap.add_argument("--adjoint-case", default=None, metavar="WxHxSPP",
                     help="run two adjoint evaluations of the differentiation scene at this size and exit "
                          "(small case for ncu)")
+    ap.add_argument("--batch-case", default=None, choices=["shared", "branches"],
+                    help="submit the 32-job batch twice in this mode and exit (case for ncu launch lists)")
     args = ap.parse_args()
+    if args.batch_case:
+        run_batch_case(args.batch_case == "shared")
+        return
     if args.profile_case:
         run_profile_case(args.profile_case, args.tuning)
         return

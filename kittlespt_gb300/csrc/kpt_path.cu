@@ -790,23 +790,42 @@ __global__ void k_temporal_gpu(TemporalParams T) {
 // job's own numbering, so each job's frame is the one it renders alone.
 
 __global__ void k_batch_level(BatchQueues Q, int level) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int e = 0, sh = 0;
-    Q.ext_prefix[0] = Q.shd_prefix[0] = 0;
-    for (int j = 0; j < Q.njobs; ++j) {
-        const BatchJob& J = Q.jobs[j];
-        if (level <= J.max_depth) {
-            int* lc = J.level_counts + LEVEL_WORDS * level;
-            sh += lc[1] + lc[2];
-            // the job's sky queue cannot grow before its k_shade(level + 1):
-            // its length ends level's range (as k_shadow records it)
-            lc[5] = J.counts[2];
-            if (level + 1 <= J.max_depth) e += J.level_counts[LEVEL_WORDS * (level + 1)];
-        }
-        Q.ext_prefix[j + 1] = e;
-        Q.shd_prefix[j + 1] = sh;
+    // one warp: lane j takes jobs j, j + 32, ...; the prefix sums by warp scans
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    if (lane == 0) {
+        Q.ext_prefix[0] = Q.shd_prefix[0] = 0;
+        Q.fetch[0] = Q.fetch[1] = 0;
     }
-    Q.fetch[0] = Q.fetch[1] = 0;
+    int e_base = 0, s_base = 0;
+    for (int j0 = 0; j0 < Q.njobs; j0 += 32) {
+        const int j = j0 + lane;
+        int e = 0, sh = 0;
+        if (j < Q.njobs) {
+            const BatchJob& J = Q.jobs[j];
+            if (level <= J.max_depth) {
+                int* lc = J.level_counts + LEVEL_WORDS * level;
+                sh = lc[1] + lc[2];
+                // the job's sky queue cannot grow before its k_shade(level + 1):
+                // its length ends level's range (as k_shadow records it)
+                lc[5] = J.counts[2];
+                if (level + 1 <= J.max_depth) e = J.level_counts[LEVEL_WORDS * (level + 1)];
+            }
+        }
+        for (int o = 1; o < 32; o <<= 1) {
+            const int te = __shfl_up_sync(0xffffffffu, e, o), ts = __shfl_up_sync(0xffffffffu, sh, o);
+            if (lane >= o) {
+                e += te;
+                sh += ts;
+            }
+        }
+        if (j < Q.njobs) {
+            Q.ext_prefix[j + 1] = e_base + e;
+            Q.shd_prefix[j + 1] = s_base + sh;
+        }
+        e_base += __shfl_sync(0xffffffffu, e, 31);
+        s_base += __shfl_sync(0xffffffffu, sh, 31);
+    }
 }
 
 // the job whose range of a prefix array holds entry i: the last j with prefix[j] <= i
