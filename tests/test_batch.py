@@ -256,3 +256,43 @@ def test_batch_follows_scene_changes():
     finally:
         for r in batched + single:
             r.shutdown()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shared", [True, False])
+def test_batch_with_post_features(shared):
+    """Jobs whose post chains differ -- temporal accumulation, lens effects,
+    FSR upscaling, auto exposure off -- batched, against the same jobs
+    rendered one by one: every job's display image and accumulation
+    bit-identical, over three submissions (the temporal history carries
+    over between them)."""
+    from kittlespt_gb300.renderer import Batch
+    from kittlespt_gb300 import scenes as S
+    jobs = [(S.scene_small(96, 64, 2, 4), 2), (S.scene_small_n(80, 48, 1, 5, 3), 3), (S.scene_full(128, 72, 1, 3), 1)]
+    settings = [dict(temporal_accumulation=1), dict(postprocess_effects=1, upscale=2), dict(auto_exposure=0, bloom=0)]
+    spp = [s for _, s in jobs]
+
+    def make():
+        rs = _renderers(jobs)
+        for r, kw in zip(rs, settings):
+            r.set_renderer_settings(**kw)
+        return rs
+
+    batched, single = make(), make()
+    try:
+        with Batch(0) as b:
+            b.shared = shared
+            for _ in range(3):
+                b.submit(batched, spp)
+                b.wait()
+                for r, s in zip(single, spp):
+                    r.execute_rendering(16.0, s)
+        for ra, rb in zip(batched, single):
+            ra.synchronize()
+            rb.synchronize()
+            np.testing.assert_array_equal(ra.get_render_target().view(np.uint32),
+                                          rb.get_render_target().view(np.uint32))
+            np.testing.assert_array_equal(ra.read_render().view(np.uint32), rb.read_render().view(np.uint32))
+    finally:
+        for r in batched + single:
+            r.shutdown()
