@@ -375,85 +375,6 @@ static __device__ __noinline__ void nishita_jacobian_d(const SkyParams& P, float
     for (int i = 0; i < SKY_PARAMS; ++i) J[i] = make_float3((float)j[i][0], (float)j[i][1], (float)j[i][2]);
 }
 
-// nishita_jacobian_d with the exponentials in single precision: positions,
-// altitudes (the ill-conditioned part: one float ulp of a 6.4e6 m vector is
-// 0.5 m) and every sum stay in double, exp runs on the single-precision
-// unit (relative error ~1e-7 times its argument); about a quarter of the
-// FP64 work.
-__device__ __forceinline__ double expd_f(double x) { return (double)expf((float)x); }
-
-static __device__ __noinline__ void nishita_jacobian_m(const SkyParams& P, float3 of, float3 df, float3* J) {
-    for (int i = 0; i < SKY_PARAMS; ++i) J[i] = make_float3(0.0f, 0.0f, 0.0f);
-    const D3 o = d3(of), d = d3(df), sun = d3(P.sun_dir);
-    double te, tx, tmin = 0.0, tmax = 1.0e300;
-    if (!sphere_hit_d(o, d, P.atm_r, &te, &tx) || tx < 0.0) return;
-    if (te > tmin && te > 0.0) tmin = te;
-    if (tx < tmax) tmax = tx;
-    const double sR[3] = {P.sigma_r.x, P.sigma_r.y, P.sigma_r.z}, sM = P.sigma_m, tM = (double)P.sigma_m + P.sigma_am;
-    const double hr = P.h_r, hm = P.h_m, er = P.earth_r;
-    const double step = (tmax - tmin) / 16.0, half = 0.5 * step;
-    double t = tmin, oR = 0.0, oM = 0.0, doR = 0.0, doM = 0.0;
-    double iR[3] = {0, 0, 0}, iM[3] = {0, 0, 0}, diR[4][3] = {}, diM[4][3] = {};
-    for (int i = 0; i < 16; ++i) {
-        const double s = t + half;
-        const D3 sp = {o.x + s * d.x, o.y + s * d.y, o.z + s * d.z};
-        const double alt = sqrt(ddot(sp, sp)) - er;
-        const double pR = expd_f(-alt / hr) * step, pM = expd_f(-alt / hm) * step;
-        const double dpR = pR * alt / (hr * hr), dpM = pM * alt / (hm * hm);
-        oR += pR;
-        oM += pM;
-        doR += dpR;
-        doM += dpM;
-        double lte, ltx;
-        sphere_hit_d(sp, sun, P.atm_r, &lte, &ltx);
-        const double lstep = ltx / 8.0;
-        double lR = 0.0, lM = 0.0, dlR = 0.0, dlM = 0.0;
-        int j;
-        for (j = 0; j < 8; ++j) {
-            const double ls = (j + 0.5) * lstep;
-            const D3 q = {sp.x + ls * sun.x, sp.y + ls * sun.y, sp.z + ls * sun.z};
-            const double altl = sqrt(ddot(q, q)) - er;
-            if (altl < 0.0) break;
-            const double eR = expd_f(-altl / hr) * lstep, eM = expd_f(-altl / hm) * lstep;
-            lR += eR;
-            lM += eM;
-            dlR += eR * altl / (hr * hr);
-            dlM += eM * altl / (hm * hm);
-        }
-        if (j == 8) {
-            const double sr = oR + lR, sm = oM + lM, dsr = doR + dlR, dsm = doM + dlM;
-            for (int c = 0; c < 3; ++c) {
-                const double Tr = expd_f(-(sR[c] * sr + tM * sm));
-                iR[c] += Tr * pR;
-                iM[c] += Tr * pM;
-                const double dtau[4] = {sr, sm, sR[c] * dsr, tM * dsm};
-                for (int k = 0; k < 4; ++k) {
-                    const double dTr = Tr == 0.0 ? 0.0 : -Tr * dtau[k];
-                    diR[k][c] += dTr * pR;
-                    diM[k][c] += dTr * pM;
-                }
-                diR[2][c] += Tr * dpR;
-                diM[3][c] += Tr * dpM;
-            }
-        }
-        t += step;
-    }
-    const double mu = ddot(d, sun);
-    const double rp = 3.0 * (1.0 + mu * mu) / (16.0 * 3.14159265358979323846);
-    const double g = 0.76;
-    const double den = (8.0 * 3.14159265358979323846) * ((2.0 + g * g) * pow(1.0 + g * g - 2.0 * g * mu, 1.5));
-    const double mp = 3.0 * ((1.0 - g * g) * (1.0 + mu * mu)) / den;
-    const double K = 6.0e5 * (double)P.sun_emission;
-    double j[SKY_PARAMS][3] = {};
-    for (int c = 0; c < 3; ++c) {
-        j[SKY_RAYLEIGH_R + c][c] = ((iR[c] + sR[c] * diR[0][c]) * rp + sM * diM[0][c] * mp) * K;
-        j[SKY_MIE][c] = (sR[c] * diR[1][c] * rp + (iM[c] + sM * diM[1][c]) * mp) * K;
-        j[SKY_RAYLEIGH_H][c] = (sR[c] * diR[2][c] * rp + sM * diM[2][c] * mp) * K;
-        j[SKY_MIE_H][c] = (sR[c] * diR[3][c] * rp + sM * diM[3][c] * mp) * K;
-    }
-    for (int i = 0; i < SKY_PARAMS; ++i) J[i] = make_float3((float)j[i][0], (float)j[i][1], (float)j[i][2]);
-}
-
 // nishita_jacobian_d in single precision, with the geometry rewritten so
 // that nothing cancels: the altitude of o + s d is h / (sqrt(R^2 + h) + R)
 // with h = |o + s d|^2 - R^2 = (|o|^2 - R^2) + s (2 o.d + s d.d) formed from
