@@ -855,9 +855,10 @@ __global__ void __launch_bounds__(PATH_BLOCK) k_adj_sky(FrameParams F, AdjParams
 
 // Every sample of the wave: its radiance from the vertex records (the
 // forward's sum), clamp, image, and the reverse sweep into the gradients.
-// the sweep and the vertex replay are held to 128 and 85 registers: left to
-// 193 and 110 they keep 8 and 16 warps per SM on latency-bound loads
-__global__ void __launch_bounds__(PATH_BLOCK, 4) k_adj_sweep(FrameParams F, AdjParams A, long long wave0) {
+// the sweep and the vertex replay are held to 64 and 85 registers: left to
+// 193 and 110 they keep 8 and 16 warps per SM on latency-bound loads (the
+// sweep's spills cost less than the warps it gains)
+__global__ void __launch_bounds__(PATH_BLOCK, 8) k_adj_sweep(FrameParams F, AdjParams A, long long wave0) {
     extern __shared__ double sg[];
     const int ng = 4 * A.nmat + ADJ_SKY_PARAMS;
     grad_begin(sg, ng);
