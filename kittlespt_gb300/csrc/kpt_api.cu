@@ -100,6 +100,7 @@ struct kpt_context {
     // device scene
     DBuf<BvhNode> d_nodes, d_tlas;
     DBuf<float4> d_tris;
+    DBuf<int> d_tri_leaf;   // per mesh, triangle id -> leaf-order slot (tri_base + id)
     DBuf<TriShade> d_shade;
     DBuf<MeshRec> d_meshes;
     DBuf<InstRec> d_inst;
@@ -324,7 +325,7 @@ kpt_status kpt_destroy(kpt_context* c) {
     for (auto& f : c->tframes)
         for (cudaEvent_t e : f.ev)
             if (e) cudaEventDestroy(e);
-    c->d_nodes.release(); c->d_tlas.release(); c->d_tris.release(); c->d_shade.release();
+    c->d_nodes.release(); c->d_tlas.release(); c->d_tris.release(); c->d_tri_leaf.release(); c->d_shade.release();
     c->d_meshes.release(); c->d_inst.release(); c->d_lights.release(); c->d_materials.release();
     c->d_textures.release(); c->d_pixels.release();
     c->acc.release(); c->albedo.release(); c->render.release(); c->image.release(); c->first_hit.release();
@@ -736,6 +737,15 @@ kpt_status kpt_commit_scene(kpt_context* c) {
     c->n_nodes = (int)nodes.size();
     c->n_tris = (int)(tris.size() / 3);
     KPT_CUDA(c->d_tris.upload(tris.data(), tris.size(), c->stream));
+    {
+        std::vector<int> tri_leaf(tris.size() / 3);
+        for (size_t mi = 0; mi < c->meshes.size(); ++mi) {
+            const HostMesh& m = c->meshes[mi];
+            const int tb = c->mesh_tri_base[mi];
+            for (int k = 0; k < m.ntris(); ++k) tri_leaf[(size_t)tb + m.order[k]] = tb + k;
+        }
+        KPT_CUDA(c->d_tri_leaf.upload(tri_leaf.data(), tri_leaf.size(), c->stream));
+    }
     KPT_CUDA(c->d_shade.upload(shade.data(), shade.size(), c->stream));
     KPT_CUDA(c->d_meshes.upload(mrec.data(), mrec.size(), c->stream));
     KPT_CUDA(c->d_lights.upload(lights.data(), lights.size(), c->stream));
@@ -1348,6 +1358,7 @@ static kpt_status prepare_frame(kpt_context* c, int spp, FrameParams* F) {
             inverse4(c->instances[i].prev_model, pinv);   // prev_inv_model_matrix
             columns_of(inv, c->h_tginst[i].inv_model);
             columns_of(pinv, c->h_tginst[i].prev_inv_model);
+            c->h_tginst[i].tri_base = c->mesh_tri_base[c->instances[i].mesh];
         }
         KPT_CUDA(c->tginst.upload(c->h_tginst.data(), ni, c->stream));
     }
@@ -1401,6 +1412,8 @@ static void enqueue_temporal(kpt_context* c, const FrameParams& F) {
         // the reference's frame k of the call: the previous camera for the
         // first, the current one after it (executeRendering ends with setView)
         T.ginst = c->tginst.p;
+        T.tris = c->d_tris.p;
+        T.tri_leaf = c->d_tri_leaf.p;
         columns_of(c->inv_proj, T.inv_proj);
         columns_of(c->inv_view, T.inv_view);
         columns_of(k == 0 ? c->prev_inv_proj : c->inv_proj, T.prev_inv_proj);

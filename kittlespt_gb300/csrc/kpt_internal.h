@@ -249,6 +249,8 @@ struct TemporalInst {
 struct TemporalGpuInst {
     float4 inv_model[4];       // curr_inv_model_matrix
     float4 prev_inv_model[4];  // prev_inv_model_matrix
+    int tri_base;              // the instance's mesh: its first triangle in tri_leaf / the leaf-order arrays
+    int pad0, pad1, pad2;
 };
 // One reference frame of the temporal path: the clamped sample `sample` of
 // every pixel blended into hist_in reprojected, written to hist_out.
@@ -271,6 +273,11 @@ struct TemporalParams {
     // this frame and of the previous one (columns), the instances' inverses
     const TemporalGpuInst* ginst;
     float4 inv_proj[4], inv_view[4], prev_inv_proj[4], prev_inv_view[4];
+    // and the visible surface as that build computes it: the hit
+    // triangle's vertices (leaf-order triangles: v0, v1 - v0, v2 - v0) and
+    // each mesh's triangle id -> leaf-order slot (tri_leaf[tri_base + id])
+    const float4* tris;
+    const int* tri_leaf;
 };
 __global__ void k_temporal(TemporalParams T);       // kpt_post.cu, IEEE
 __global__ void k_temporal_gpu(TemporalParams T);   // kpt_path.cu, the reference GPU build's arithmetic

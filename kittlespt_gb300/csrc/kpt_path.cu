@@ -734,16 +734,46 @@ __global__ void k_temporal_gpu(TemporalParams T) {
         L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float3 curr = make_float3(fmaxf(0.0f, fminf(L.x, 1.0e8f)), fmaxf(0.0f, fminf(L.y, 1.0e8f)),
                                     fmaxf(0.0f, fminf(L.z, 1.0e8f)));
-    const float4 vs = T.vis[p];
-    if (T.depth_out) T.depth_out[p] = vs.w;
     float4 out = make_float4(curr.x, curr.y, curr.z, 0.0f);
-    if (j >= 0) {
-        const TemporalGpuInst& I = T.ginst[T.primary[p].inst];
+    if (j < 0) {
+        if (T.depth_out) T.depth_out[p] = T.vis[p].w;
+    } else {
+        const PrimaryRec pr = T.primary[p];
+        const TemporalGpuInst& I = T.ginst[pr.inst];
+        // the visible surface as the reference's GPU build finds it
+        // (VisibleSurface, packing.cuh:156-176): the camera ray of
+        // Camera::generateRay (camera.cuh:16-25) with the pixel's
+        // uv = (pixel + 1/2) / resolution (shading_kernel.cuh:23), the hit
+        // triangle's distance by Triangle::intersect (triangle.cuh:66-102) on
+        // the ray in object space (Ray::transform), the point o + t d
+        // (Ray::getPointAt), the distance as its depth
+        const float ux = ((float)x + 0.5f) / (float)T.W, uy = ((float)y + 0.5f) / (float)T.H;
+        const float4 tc = m4_apply(m4_load(T.inv_proj), make_float4(2.0f * ux - 1.0f, 2.0f * uy - 1.0f, 1.0f, 1.0f));
+        float3 v = make_float3(tc.x / tc.w, tc.y / tc.w, tc.z / tc.w);
+        v = v * rsqrtf(dot(v, v));
+        const float4 tw = m4_apply(m4_load(T.inv_view), make_float4(v.x, v.y, v.z, 0.0f));
+        float3 rd = make_float3(tw.x, tw.y, tw.z);
+        rd = rd * rsqrtf(dot(rd, rd));
+        const float3 ro = make_float3(T.inv_view[3].x, T.inv_view[3].y, T.inv_view[3].z);
+        const M4 im = m4_load(I.inv_model);
+        const float4 oo = m4_apply(im, make_float4(ro.x, ro.y, ro.z, 1.0f));
+        const float4 od = m4_apply(im, make_float4(rd.x, rd.y, rd.z, 0.0f));
+        const int li = T.tri_leaf[I.tri_base + pr.tri];
+        const float4 ta = T.tris[3 * (size_t)li], tb = T.tris[3 * (size_t)li + 1], tc2 = T.tris[3 * (size_t)li + 2];
+        const float3 v0 = make_float3(ta.x, ta.y, ta.z), e1 = make_float3(tb.x, tb.y, tb.z),
+                     e2 = make_float3(tc2.x, tc2.y, tc2.z);
+        const float3 pvec = cross(make_float3(od.x, od.y, od.z), e2);
+        const float inv_det = 1.0f / dot(e1, pvec);
+        const float3 tvec = make_float3(oo.x, oo.y, oo.z) - v0;
+        const float3 qvec = cross(tvec, e1);
+        const float th = inv_det * dot(e2, qvec);
+        const float3 wp = ro + th * rd;
+        if (T.depth_out) T.depth_out[p] = th;
         // computeVelocity (kernels.cu:164-192)
         const M4 cvp = m4_mul(m4_inverse(m4_load(T.inv_proj)), m4_inverse(m4_load(T.inv_view)));
         const M4 pvp = m4_mul(m4_inverse(m4_load(T.prev_inv_proj)), m4_inverse(m4_load(T.prev_inv_view)));
         const M4 pmodel = m4_inverse(m4_load(I.prev_inv_model));
-        const float4 pos = make_float4(vs.x, vs.y, vs.z, 1.0f);
+        const float4 pos = make_float4(wp.x, wp.y, wp.z, 1.0f);
         const float4 l4 = m4_apply(m4_load(I.inv_model), pos);
         const float4 local = make_float4(l4.x, l4.y, l4.z, 1.0f);
         const float4 cc = m4_apply(cvp, pos);

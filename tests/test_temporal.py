@@ -132,14 +132,17 @@ def test_temporal_sequence_matches_reference_gpu(arith):
     ulps, and its reprojection truncates the previous pixel coordinate: a
     pixel whose coordinate lands an ulp below an integer takes its history
     length (point-sampled) and bilinear weights from the texel one over.
-    Those ulps also follow the visible-surface position, which the CUDA path
-    takes from its IEEE camera ray and traversal.  Measured (history lengths
-    equal to the reference's / modulated images within 1e-4 relative, after
-    2, 3, 6, 7 and 9 frames): temporal_arith 1: 95.3/99.97, 95.4/95.4,
-    90.1/90.1, 89.7/89.5, 86.2/89.8%; temporal_arith 0: 94.2/99.97,
-    94.3/94.2, 89.2/88.9, 88.9/88.4, 87.1/89.2% -- a pixel whose decision
-    differed once keeps a different history until it saturates at 16
-    frames.  The test asserts 85% for both after every call."""
+    Those ulps also follow the visible-surface position and depth, which
+    temporal_arith 1 recomputes as that build does (its fast-maths camera
+    ray, the hit triangle's distance by its fast-maths triangle test, o + t
+    d).  Measured (history lengths equal to the reference's / modulated
+    images within 1e-4 relative, after 2, 3, 6, 7 and 9 frames):
+    temporal_arith 1: 100/99.97, 100/100, 100/99.97, 100/99.97, 100/99.93%;
+    temporal_arith 0 (IEEE, the oracle's arithmetic): 94.2/99.97, 94.3/94.2,
+    89.2/88.9, 88.9/88.4, 87.1/89.2% -- a pixel whose decision differed once
+    keeps a different history until it saturates at 16 frames.  The test
+    asserts 99.9% / 99.5% after every call for temporal_arith 1, 85% for
+    IEEE."""
     from kittlespt_gb300.renderer import Renderer
     if not O.available("refgpu"):
         pytest.skip("reference GPU build absent (reference sources not staged)")
@@ -193,7 +196,8 @@ def test_temporal_sequence_matches_reference_gpu(arith):
                 print(f"temporal_arith {arith}, after {frame} frames: history lengths equal on {same_hist:.4f} "
                       f"(oracle's: {same_oracle:.4f}), images within 1e-4 on {close:.4f} of the pixels")
                 seen.append((frame, same_hist, close))
-        assert all(h >= 0.85 and c >= 0.85 for _, h, c in seen), seen
+        floor_h, floor_c = (0.999, 0.995) if arith == 1 else (0.85, 0.85)
+        assert all(h >= floor_h and c >= floor_c for _, h, c in seen), seen
         assert (racc[..., 3] >= 2).any()
     finally:
         r.shutdown()
