@@ -106,10 +106,12 @@ typedef struct kpt_settings {
     int32_t temporal_arith;    /* arithmetic of the temporal reprojection (temporal_accumulation =
                                   1): 1 (the default) that of the reference's GPU build, which
                                   inverts the camera and previous model matrices for every pixel
-                                  with contracted products and an approximate reciprocal (a still
-                                  camera then has a velocity of a few ulps, and the truncated
-                                  previous pixel and the bilinear weights follow them); 0 IEEE
-                                  single precision with the matrices inverted once on the host. */
+                                  with contracted products and an approximate reciprocal, and
+                                  whose visible-surface position and depth come from its
+                                  fast-maths camera ray and triangle test (a still camera then
+                                  has a velocity of a few ulps, and the truncated previous pixel
+                                  and the bilinear weights follow them); 0 IEEE single precision
+                                  with the matrices inverted once on the host. */
 } kpt_settings;
 
 /* ExposureValues (pod_types.hpp:9-33) with the compensation and white/black
