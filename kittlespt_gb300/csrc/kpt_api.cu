@@ -2004,7 +2004,9 @@ kpt_status kpt_adjoint_backward_device(kpt_context* c, const float* adjoint, dou
     if (!c || !adjoint || !grad) return fail(KPT_ERR_INVALID, "kpt_adjoint_backward_device: null argument");
     KPT_CUDA(cudaSetDevice(c->device));
     kpt_context::AdjForward& K = c->adj_fwd;
-    const bool same = K.valid && K.version == c->scene_version && K.materials.size() == c->materials.size() &&
+    // (a transform set since the forward call leaves the TLAS to rebuild)
+    const bool same = K.valid && !c->tlas_dirty && K.version == c->scene_version &&
+                      K.materials.size() == c->materials.size() &&
                       std::memcmp(K.materials.data(), c->materials.data(), sizeof(kpt_material) * K.materials.size()) == 0 &&
                       std::memcmp(&K.env, &c->env, sizeof K.env) == 0 &&
                       std::memcmp(&K.settings, &c->settings, sizeof K.settings) == 0 &&

@@ -438,5 +438,11 @@ def test_split_adjoint_matches_one_call():
         assert r.set_material(0, m)
         with pytest.raises(K.KptError):
             r.adjoint_backward_device(adj.data_ptr(), g2.data_ptr())     # a parameter changed
+        r.adjoint_forward_device(0, SPP, img2.data_ptr())
+        model = np.array(sc.instances[0].model, np.float32)
+        model[1, 3] += 0.25
+        assert r.set_mesh_transform(0, model)
+        with pytest.raises(K.KptError):
+            r.adjoint_backward_device(adj.data_ptr(), g2.data_ptr())     # an instance moved
     finally:
         r.shutdown()
