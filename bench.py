@@ -911,7 +911,9 @@ def run_temporal(args):
     frame, blended into the reprojected history), the camera moving a little
     before every call; the same frames with the running mean beside them.
     Device time per call over K calls (CUDA events on the library's stream, L2
-    flushed between calls)."""
+    flushed between calls).  The temporal blend in the reference GPU build's
+    arithmetic (temporal_arith 1, the default: per-pixel matrix inverses and
+    the visible surface recomputed) and in IEEE (0)."""
     import torch
     from kittlespt_gb300 import scenes as S
     from kittlespt_gb300.renderer import Renderer
@@ -924,8 +926,8 @@ def run_temporal(args):
     ip = sc.camera.inv_proj.astype(np.float32)
     res = {}
     try:
-        for mode, name in ((0, "running_mean"), (1, "temporal")):
-            r.set_renderer_settings(temporal_accumulation=mode)
+        for mode, arith, name in ((0, 0, "running_mean"), (1, 0, "temporal_ieee"), (1, 1, "temporal")):
+            r.set_renderer_settings(temporal_accumulation=mode, temporal_arith=arith)
             k = 0
 
             def frame():
